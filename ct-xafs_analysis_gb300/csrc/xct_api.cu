@@ -1,0 +1,403 @@
+// xct_api.cu -- the C ABI of libxct (include/xct.h): device context, OS-EM plans, the
+// subset/iteration loop and the operator entry points.
+//
+// Replaces, for the OS-EM path of CT_reconstruction:
+//   OCL_platform_device (share source/OCL_platform_device_class.cpp:55-208)  -> xct_ctx_*
+//   OSEM_programBuild   (CT_reconstruction/GPU.cpp:513-559)                  -> xct_osem_plan_create
+//   OSEM_execution      (GPU.cpp:125-240) + OSEM_thread copies (:440-463)    -> xct_osem_run[_device]
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+
+#include "xct_internal.h"
+
+std::atomic<long long> g_xct_launches{0};
+
+namespace {
+thread_local std::string t_last_error;
+}
+
+int xct_fail(int code, const std::string &msg)
+{
+    t_last_error = msg;
+    return code;
+}
+
+int xct_cuda_fail(cudaError_t e, const char *what)
+{
+    char buf[512];
+    snprintf(buf, sizeof buf, "CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+    t_last_error = buf;
+    return e == cudaErrorMemoryAllocation ? XCT_E_NOMEM : XCT_E_CUDA;
+}
+
+// Per-angle (cos, sin): angle_pr = angle[th]*PI/180.0f with PI a double literal
+// (OSEM.cl:2,57), stored to float; then the float cos/sin of that float, correctly
+// rounded.  The oracle builds the identical table (oracle/xct_oracle.c, xo_trig_f32).
+void xct_trig_table(const float *ang_deg, int pa, std::vector<float2> &cs)
+{
+    cs.resize(pa);
+    for (int th = 0; th < pa; ++th) {
+        const float phi = (float)(((double)ang_deg[th] * 3.14159265358979323846) / 180.0);
+        cs[th].x = (float)cos((double)phi);
+        cs[th].y = (float)sin((double)phi);
+    }
+}
+
+// Subset order of OSEM_ocl (GPU.cpp:564-582): a power-of-two ss gives the bit-reversal
+// permutation (0, ss/2, ss/4, 3ss/4, ...); any other ss the identity.
+void xct_subset_order_host(int ss, int *sub)
+{
+    if (ss <= 0) return;
+    if ((ss & (ss - 1)) == 0) {
+        int bits = 0;
+        while ((1 << bits) < ss) ++bits;
+        for (int j = 0; j < ss; ++j) {
+            int r = 0;
+            for (int b = 0; b < bits; ++b)
+                if (j & (1 << b)) r |= 1 << (bits - 1 - b);
+            sub[j] = r;
+        }
+    } else {
+        for (int j = 0; j < ss; ++j) sub[j] = j;
+    }
+}
+
+extern "C" {
+
+const char *xct_last_error(void) { return t_last_error.c_str(); }
+int xct_abi_version(void) { return XCT_ABI_VERSION; }
+long long xct_launch_count(void) { return g_xct_launches.load(); }
+
+int xct_subset_order(int ss, int *sub)
+{
+    if (ss <= 0 || sub == nullptr) return xct_fail(XCT_E_INVALID, "xct_subset_order: ss must be > 0");
+    xct_subset_order_host(ss, sub);
+    return XCT_OK;
+}
+
+int xct_device_count(int *count)
+{
+    if (!count) return xct_fail(XCT_E_INVALID, "xct_device_count: null");
+    XCT_CUDA_TRY(cudaGetDeviceCount(count));
+    return XCT_OK;
+}
+
+int xct_device_name(int device, char *buf, int buflen)
+{
+    if (!buf || buflen <= 0) return xct_fail(XCT_E_INVALID, "xct_device_name: bad buffer");
+    cudaDeviceProp p;
+    XCT_CUDA_TRY(cudaGetDeviceProperties(&p, device));
+    snprintf(buf, buflen, "%s", p.name);
+    return XCT_OK;
+}
+
+int xct_ctx_create(int device, xct_ctx **out)
+{
+    if (!out) return xct_fail(XCT_E_INVALID, "xct_ctx_create: out is null");
+    *out = nullptr;
+    int n = 0;
+    XCT_CUDA_TRY(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) {
+        char b[128];
+        snprintf(b, sizeof b, "xct_ctx_create: device %d out of range (%d devices)", device, n);
+        return xct_fail(XCT_E_INVALID, b);
+    }
+    cudaDeviceProp p;
+    XCT_CUDA_TRY(cudaGetDeviceProperties(&p, device));
+    if (!(p.major == 10 && p.minor == 3)) {
+        char b[512];
+        snprintf(b, sizeof b, "libxct is built for sm_103a (GB300); device %d (%s) is sm_%d%d", device, p.name,
+                 p.major, p.minor);
+        return xct_fail(XCT_E_UNSUPPORTED, b);
+    }
+    XCT_CUDA_TRY(cudaSetDevice(device));
+    xct_ctx *c = new (std::nothrow) xct_ctx();
+    if (!c) return xct_fail(XCT_E_NOMEM, "xct_ctx_create: host allocation failed");
+    c->device = device;
+    c->sm_count = p.multiProcessorCount;
+    c->max_smem_optin = (int)p.sharedMemPerBlockOptin;
+    snprintf(c->name, sizeof c->name, "%s", p.name);
+    *out = c;
+    return XCT_OK;
+}
+
+int xct_ctx_destroy(xct_ctx *ctx)
+{
+    delete ctx;
+    return XCT_OK;
+}
+
+static void plan_free(xct_plan *p)
+{
+    if (!p) return;
+    cudaFree(p->d_trig);
+    cudaFree(p->d_sino);
+    cudaFree(p->d_img);
+    cudaFree(p->d_ratio);
+    cudaFree(p->d_corr);
+    cudaFree(p->d_corr_ang);
+    cudaFree(p->d_corr_bin);
+    cudaFree(p->d_acc);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+static int check_geom(const xct_geom *g)
+{
+    if (!g) return xct_fail(XCT_E_INVALID, "geometry is null");
+    if (g->nx <= 0 || g->ny <= 0 || g->px <= 0 || g->pa <= 0 || g->ss <= 0 || g->it < 0)
+        return xct_fail(XCT_E_INVALID, "geometry: nx, ny, px, pa, ss must be > 0 and it >= 0");
+    if (g->ox != g->nx || g->oy != g->ny)
+        return xct_fail(XCT_E_INVALID,
+                        "geometry: output ROI smaller than the reconstruction (ox < nx) is not supported; the "
+                        "reference's own ROI path updates a different region than it reads back (GPU.cpp:152-170)");
+    if (g->ss > g->pa) return xct_fail(XCT_E_INVALID, "geometry: more subsets than angles");
+    if (!g->angles_deg) return xct_fail(XCT_E_INVALID, "geometry: angles_deg is null");
+    if (g->nx > 16384 || g->ny > 16384 || g->px > 65536 || g->pa > 65536)
+        return xct_fail(XCT_E_INVALID, "geometry: size beyond the supported maximum (16384 px image, 65536 bins)");
+    if (g->measured_fetch_mode != XCT_FETCH_EXACT && g->measured_fetch_mode != XCT_FETCH_AVG2X2)
+        return xct_fail(XCT_E_INVALID, "geometry: measured_fetch_mode must be XCT_FETCH_EXACT or XCT_FETCH_AVG2X2");
+    if (g->subset_mode != XCT_SUBSETS_REF && g->subset_mode != XCT_SUBSETS_COVER)
+        return xct_fail(XCT_E_INVALID, "geometry: subset_mode must be XCT_SUBSETS_REF or XCT_SUBSETS_COVER");
+    if (g->correction_mode < 0 || g->correction_mode > 4)
+        return xct_fail(XCT_E_INVALID, "geometry: correction_mode must be 0..4");
+    if (g->max_batch <= 0) return xct_fail(XCT_E_INVALID, "geometry: max_batch must be > 0");
+    if (g->kernels != XCT_KERNELS_TILED && g->kernels != XCT_KERNELS_PLAIN)
+        return xct_fail(XCT_E_INVALID, "geometry: kernels must be XCT_KERNELS_TILED or XCT_KERNELS_PLAIN");
+    for (int i = 0; i < g->pa; ++i)
+        if (!(fabsf(g->angles_deg[i]) < 1.0e6f)) return xct_fail(XCT_E_INVALID, "geometry: non-finite angle");
+    return XCT_OK;
+}
+
+int xct_osem_plan_create(xct_ctx *ctx, const xct_geom *geom, xct_plan **out)
+{
+    if (!ctx || !out) return xct_fail(XCT_E_INVALID, "xct_osem_plan_create: null argument");
+    *out = nullptr;
+    int rc = check_geom(geom);
+    if (rc) return rc;
+    XCT_CUDA_TRY(cudaSetDevice(ctx->device));
+    xct_plan *p = new (std::nothrow) xct_plan();
+    if (!p) return xct_fail(XCT_E_NOMEM, "xct_osem_plan_create: host allocation failed");
+    p->ctx = ctx;
+    p->g = *geom;
+    p->angles.assign(geom->angles_deg, geom->angles_deg + geom->pa);
+    p->g.angles_deg = nullptr;
+    p->sub_default.resize(geom->ss);
+    xct_subset_order_host(geom->ss, p->sub_default.data());
+    KGeom &k = p->kg;
+    k.nx = geom->nx;
+    k.ny = geom->ny;
+    k.px = geom->px;
+    k.pa = geom->pa;
+    k.ss = geom->ss;
+    k.depth = std::max(geom->nx, geom->ny);
+    k.hx = (float)geom->nx * 0.5f;
+    k.hy = (float)geom->ny * 0.5f;
+    k.hd = (float)k.depth * 0.5f;
+    k.cx = geom->center_bin < 0.0f ? (float)geom->px * 0.5f : geom->center_bin;
+    k.fetch = geom->measured_fetch_mode;
+
+    auto fail = [&](cudaError_t e, const char *what) {
+        int r = xct_cuda_fail(e, what);
+        plan_free(p);
+        return r;
+    };
+    const size_t nb = (size_t)geom->max_batch;
+    const size_t nimg = (size_t)geom->nx * geom->ny, nprj = (size_t)geom->px * geom->pa;
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+    if ((e = cudaEventCreate(&p->ev0)) != cudaSuccess) return fail(e, "event");
+    if ((e = cudaEventCreate(&p->ev1)) != cudaSuccess) return fail(e, "event");
+    if ((e = cudaMalloc(&p->d_trig, sizeof(float2) * geom->pa)) != cudaSuccess) return fail(e, "cudaMalloc trig");
+    if ((e = cudaMalloc(&p->d_sino, sizeof(float) * nb * nprj)) != cudaSuccess) return fail(e, "cudaMalloc sino");
+    if ((e = cudaMalloc(&p->d_img, sizeof(float) * nb * nimg)) != cudaSuccess) return fail(e, "cudaMalloc img");
+    if ((e = cudaMalloc(&p->d_ratio, sizeof(float) * nb * nprj)) != cudaSuccess) return fail(e, "cudaMalloc ratio");
+    if ((e = cudaMemsetAsync(p->d_ratio, 0, sizeof(float) * nb * nprj, p->stream)) != cudaSuccess)
+        return fail(e, "memset ratio");
+    std::vector<float2> cs;
+    xct_trig_table(p->angles.data(), geom->pa, cs);
+    if ((e = cudaMemcpyAsync(p->d_trig, cs.data(), sizeof(float2) * geom->pa, cudaMemcpyHostToDevice, p->stream)) !=
+        cudaSuccess)
+        return fail(e, "upload trig");
+    if (geom->correction_mode > 0) {
+        // sinogramCorrection factors (reconstShare.cl:44-64): angle_pr = angle/180*PI
+        // (float division, then a double PI, stored to float); a = b = 0.5
+        // (GPU.cpp:182-183).
+        std::vector<float> af(2 * (size_t)geom->pa), bf(geom->px);
+        for (int th = 0; th < geom->pa; ++th) {
+            const float q = p->angles[th] / 180.0f;
+            const float apr = (float)((double)q * 3.14159265358979323846);
+            const float ca = (float)cos((double)apr);
+            af[2 * th] = ca;
+            af[2 * th + 1] = 0.5f + 0.5f * ca;
+        }
+        for (int X = 0; X < geom->px; ++X) {
+            const float theta = 2.0f * fabsf((float)X - (float)geom->px / 2.0f) / (float)geom->px;
+            const float as = (float)asin((double)theta);
+            bf[X] = (float)cos((double)as);
+        }
+        if ((e = cudaMalloc(&p->d_corr, sizeof(float) * nb * nprj)) != cudaSuccess) return fail(e, "cudaMalloc corr");
+        if ((e = cudaMalloc(&p->d_corr_ang, sizeof(float) * af.size())) != cudaSuccess) return fail(e, "corr ang");
+        if ((e = cudaMalloc(&p->d_corr_bin, sizeof(float) * bf.size())) != cudaSuccess) return fail(e, "corr bin");
+        if ((e = cudaMemcpy(p->d_corr_ang, af.data(), sizeof(float) * af.size(), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+            return fail(e, "upload corr ang");
+        if ((e = cudaMemcpy(p->d_corr_bin, bf.data(), sizeof(float) * bf.size(), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+            return fail(e, "upload corr bin");
+    }
+    if ((e = cudaStreamSynchronize(p->stream)) != cudaSuccess) return fail(e, "plan sync");
+    *out = p;
+    return XCT_OK;
+}
+
+int xct_osem_plan_destroy(xct_plan *plan)
+{
+    if (plan) cudaSetDevice(plan->ctx->device);
+    plan_free(plan);
+    return XCT_OK;
+}
+
+// Rows OSEM1 forward-projects for subset `sub` (GPU.cpp:169: pa/ss rows), or every row
+// OSEM2 reads (ceil((pa - sub)/ss)) in XCT_SUBSETS_COVER mode.
+static inline int subset_rows(const xct_plan *p, int sub)
+{
+    const int pa = p->g.pa, ss = p->g.ss;
+    return p->g.subset_mode == XCT_SUBSETS_COVER ? (pa - sub + ss - 1) / ss : pa / ss;
+}
+
+// The subset/iteration loop of OSEM_execution (GPU.cpp:199-229) for dN slices already on
+// the device.  The dest image and its copy-back (GPU.cpp:165, 226) are folded away: the
+// backprojection update is done in place, which is equivalent because each pixel's new
+// value depends only on its own old value and the ratio image.
+static int osem_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it,
+                     cudaStream_t st)
+{
+    const KGeom &g = p->kg;
+    const float *meas = d_sino;
+    if (p->g.correction_mode > 0) {
+        int rc = launch_sino_correction(g, d_sino, p->d_corr, p->d_corr_ang, p->d_corr_bin, p->g.correction_mode, dN,
+                                        st);
+        if (rc) return rc;
+        meas = p->d_corr;
+    }
+    for (int i = 0; i < it; ++i)
+        for (int k = 0; k < p->g.ss; ++k) {
+            const int s = sub[k];
+            int rc = launch_fwd_plain(g, p->d_trig, d_img, meas, p->d_ratio, dN, s, g.ss, subset_rows(p, s), st);
+            if (rc) return rc;
+            rc = launch_bp_update_plain(g, p->d_trig, d_img, p->d_ratio, dN, s, st);
+            if (rc) return rc;
+        }
+    return XCT_OK;
+}
+
+static int check_run(xct_plan *p, int dN, const int *sub, int it)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "plan is null");
+    if (dN <= 0 || dN > p->g.max_batch) {
+        char b[160];
+        snprintf(b, sizeof b, "dN=%d outside [1, max_batch=%d] of the plan", dN, p->g.max_batch);
+        return xct_fail(XCT_E_INVALID, b);
+    }
+    if (it < 0) return xct_fail(XCT_E_INVALID, "iterations must be >= 0");
+    if (sub)
+        for (int k = 0; k < p->g.ss; ++k)
+            if (sub[k] < 0 || sub[k] >= p->g.ss) return xct_fail(XCT_E_INVALID, "subset order entry out of range");
+    return XCT_OK;
+}
+
+int xct_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, void *stream)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_osem_run_device: null device pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    return osem_loop(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, st);
+}
+
+int xct_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, const int *sub, int it)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!sino_host || !img_host) return xct_fail(XCT_E_INVALID, "xct_osem_run: null host array");
+    for (int i = 0; i < dN; ++i)
+        if (!sino_host[i] || !img_host[i]) return xct_fail(XCT_E_INVALID, "xct_osem_run: null slice pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    const size_t nimg = (size_t)p->g.nx * p->g.ny, nprj = (size_t)p->g.px * p->g.pa;
+    cudaStream_t st = p->stream;
+    // host -> device (OSEM_thread, GPU.cpp:440-445)
+    for (int i = 0; i < dN; ++i) {
+        XCT_CUDA_TRY(cudaMemcpyAsync(p->d_sino + i * nprj, sino_host[i], sizeof(float) * nprj,
+                                     cudaMemcpyHostToDevice, st));
+        XCT_CUDA_TRY(
+            cudaMemcpyAsync(p->d_img + i * nimg, img_host[i], sizeof(float) * nimg, cudaMemcpyHostToDevice, st));
+    }
+    XCT_CUDA_TRY(cudaEventRecord(p->ev0, st));
+    rc = osem_loop(p, dN, p->d_sino, p->d_img, sub ? sub : p->sub_default.data(), it, st);
+    if (rc) return rc;
+    XCT_CUDA_TRY(cudaEventRecord(p->ev1, st));
+    // device -> host (GPU.cpp:460-463)
+    for (int i = 0; i < dN; ++i)
+        XCT_CUDA_TRY(
+            cudaMemcpyAsync(img_host[i], p->d_img + i * nimg, sizeof(float) * nimg, cudaMemcpyDeviceToHost, st));
+    XCT_CUDA_TRY(cudaStreamSynchronize(st));
+    XCT_CUDA_TRY(cudaEventElapsedTime(&p->last_ms, p->ev0, p->ev1));
+    return XCT_OK;
+}
+
+int xct_fwd(xct_plan *p, int dN, const float *d_img, float *d_sino, void *stream)
+{
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if (!d_img || !d_sino) return xct_fail(XCT_E_INVALID, "xct_fwd: null device pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    return launch_fwd_plain(p->kg, p->d_trig, d_img, nullptr, d_sino, dN, 0, 1, p->g.pa, st);
+}
+
+int xct_bp_ref(xct_plan *p, int dN, const float *d_sino, float *d_img, void *stream)
+{
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if (!d_img || !d_sino) return xct_fail(XCT_E_INVALID, "xct_bp_ref: null device pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    return launch_bp_ref_plain(p->kg, p->d_trig, d_sino, d_img, dN, 0, 1, st);
+}
+
+int xct_adj(xct_plan *p, int dN, const float *d_sino, float *d_img, void *stream)
+{
+    (void)p;
+    (void)dN;
+    (void)d_sino;
+    (void)d_img;
+    (void)stream;
+    return xct_fail(XCT_E_UNSUPPORTED, "xct_adj: not built yet");
+}
+
+int xct_plan_sync(xct_plan *p)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "plan is null");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    XCT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return XCT_OK;
+}
+
+int xct_plan_last_ms(xct_plan *p, float *ms)
+{
+    if (!p || !ms) return xct_fail(XCT_E_INVALID, "null argument");
+    *ms = p->last_ms;
+    return XCT_OK;
+}
+
+}  // extern "C"

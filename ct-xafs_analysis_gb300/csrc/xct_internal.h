@@ -1,0 +1,80 @@
+// xct_internal.h -- internal declarations shared by the libxct translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "../../include/xct.h"
+
+// Geometry as the kernels see it (passed by value).  Half sizes are precomputed exactly
+// as the reference's expressions produce them (IMAGESIZE_X*0.5f etc., OSEM.cl:58-59,95).
+struct KGeom {
+    int nx, ny;      // image
+    int px, pa;      // sinogram
+    int ss;          // subsets
+    int depth;       // samples per ray, max(nx, ny)
+    float hx, hy;    // nx*0.5f, ny*0.5f
+    float hd;        // depth*0.5f
+    float cx;        // detector centre (px*0.5f in the reference)
+    int fetch;       // XCT_FETCH_*
+};
+
+struct xct_ctx {
+    int device;
+    int sm_count;
+    int max_smem_optin;
+    char name[256];
+};
+
+struct xct_plan {
+    xct_ctx *ctx;
+    xct_geom g;
+    KGeom kg;
+    std::vector<float> angles;
+    std::vector<int> sub_default;
+    float2 *d_trig = nullptr;    // [pa] (cos, sin) of the float angle (see trig table)
+    float *d_sino = nullptr;     // [max_batch][pa][px] staging for host-buffer runs
+    float *d_img = nullptr;      // [max_batch][ny][nx] staging for host-buffer runs
+    float *d_ratio = nullptr;    // [max_batch][pa][px] ratio image (never-written rows stay 0)
+    float *d_corr = nullptr;     // [max_batch][pa][px] corrected sinogram (correction_mode > 0)
+    float *d_corr_ang = nullptr; // [pa] x 2 per-angle correction factors
+    float *d_corr_bin = nullptr; // [px] per-bin correction factors
+    float *d_acc = nullptr;      // tiled forward: per-ray partial sums [max_batch][rows][px]
+    size_t acc_elems = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_ms = 0.0f;
+};
+
+// ---- error handling (per-thread last error) ----
+int xct_fail(int code, const std::string &msg);
+int xct_cuda_fail(cudaError_t e, const char *what);
+#define XCT_CUDA_TRY(expr)                                          \
+    do {                                                            \
+        cudaError_t e_ = (expr);                                    \
+        if (e_ != cudaSuccess) return xct_cuda_fail(e_, #expr);     \
+    } while (0)
+
+extern std::atomic<long long> g_xct_launches;
+
+// ---- host-side tables (identical to the oracle's) ----
+void xct_trig_table(const float *ang_deg, int pa, std::vector<float2> &cs);
+void xct_subset_order_host(int ss, int *sub);
+
+// ---- kernel launchers (xct_plain.cu / xct_tiled.cu / xct_misc.cu) ----
+// Forward projection of rows th = sub + k*step, k < nrows, for dN slices.
+//   ratio mode (meas != nullptr): OSEM1 ratio (OSEM.cl:38-68) into out;
+//   raw mode   (meas == nullptr): projection sums (reconstShare.cl:213-241) into out.
+int launch_fwd_plain(const KGeom &g, const float2 *trig, const float *img, const float *meas, float *out, int dN,
+                     int sub, int step, int nrows, cudaStream_t st);
+// OSEM2 backprojection + multiplicative update, in place on img (OSEM.cl:71-105).
+int launch_bp_update_plain(const KGeom &g, const float2 *trig, float *img, const float *ratio, int dN, int sub,
+                           cudaStream_t st);
+// backProjection (reconstShare.cl:245-275) with subset (sub, step): img = B prj.
+int launch_bp_ref_plain(const KGeom &g, const float2 *trig, const float *prj, float *img, int dN, int sub, int step,
+                        cudaStream_t st);
+// sinogramCorrection (reconstShare.cl:35-70), modes 1..4, src -> dst.
+int launch_sino_correction(const KGeom &g, const float *src, float *dst, const float *ang_fac, const float *bin_fac,
+                           int mode, int dN, cudaStream_t st);

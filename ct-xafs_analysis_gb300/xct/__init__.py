@@ -1,0 +1,272 @@
+"""Python front end of libxct, the GB300 OS-EM library (ctypes over include/xct.h).
+
+The product is the C ABI in ``libxct.so``; this module loads it and mirrors the
+reference's host interface for the OS-EM path of CT_reconstruction
+(CT_reconstruction/CT_reconstruction.hpp:68-90, GPU.cpp:125-663):
+
+* ``Context``      -- replaces OCL_platform_device (one CUDA device);
+* ``OSEMPlan``     -- replaces OSEM_programBuild + the image objects of OSEM_execution;
+* ``OSEM_execution(plan, sub, reconst_img, prj_img, dN, it, prjCorrection)`` -- the
+  reference's executor on device tensors, same argument meaning;
+* ``OSEM_thread(plan, sub, imgs, prjs, startN, endN, it)`` -- host arrays in, results
+  written back into ``imgs`` (the reference's host<->device staging, GPU.cpp:408-476).
+
+Errors raise ``XCTError`` carrying the library's status code and message (the reference
+prints and exits, GPU.cpp:231-237; callers that want that behaviour catch and exit).
+There is no CPU fallback: if the CUDA library is missing, importing works but every
+call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libxct.so")
+
+XCT_OK = 0
+XCT_E_INVALID = -1
+XCT_E_CUDA = -2
+XCT_E_NOMEM = -3
+XCT_E_UNSUPPORTED = -4
+XCT_E_TIMEOUT = -5
+XCT_E_IO = -6
+
+FETCH_EXACT = 0
+FETCH_AVG2X2 = 1
+SUBSETS_REF = 0
+SUBSETS_COVER = 1
+KERNELS_TILED = 0
+KERNELS_PLAIN = 1
+
+# Every function include/xct.h declares (checked by the tests against the header).
+EXPORTS = (
+    "xct_ctx_create", "xct_ctx_destroy", "xct_device_count", "xct_device_name",
+    "xct_osem_plan_create", "xct_osem_plan_destroy", "xct_subset_order",
+    "xct_osem_run", "xct_osem_run_device", "xct_fwd", "xct_bp_ref", "xct_adj",
+    "xct_plan_sync", "xct_plan_last_ms", "xct_launch_count", "xct_last_error", "xct_abi_version",
+)
+
+
+class XCTError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("xct error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Geom(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("ox", ctypes.c_int), ("oy", ctypes.c_int),
+        ("px", ctypes.c_int), ("pa", ctypes.c_int),
+        ("ss", ctypes.c_int), ("it", ctypes.c_int),
+        ("angles_deg", ctypes.POINTER(ctypes.c_float)),
+        ("center_bin", ctypes.c_float),
+        ("measured_fetch_mode", ctypes.c_int),
+        ("subset_mode", ctypes.c_int),
+        ("correction_mode", ctypes.c_int),
+        ("max_batch", ctypes.c_int),
+        ("kernels", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def load():
+    """Load libxct.so (raises if it was not built: no CPU fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise XCTError(XCT_E_UNSUPPORTED, "libxct.so not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, ip, fp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)
+    L.xct_ctx_create.argtypes = [ip, ctypes.POINTER(vp)]
+    L.xct_ctx_destroy.argtypes = [vp]
+    L.xct_device_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    L.xct_device_name.argtypes = [ip, ctypes.c_char_p, ip]
+    L.xct_osem_plan_create.argtypes = [vp, ctypes.POINTER(Geom), ctypes.POINTER(vp)]
+    L.xct_osem_plan_destroy.argtypes = [vp]
+    L.xct_subset_order.argtypes = [ip, ctypes.POINTER(ctypes.c_int)]
+    L.xct_osem_run.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int), ip]
+    L.xct_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, vp]
+    for n in ("xct_fwd", "xct_bp_ref", "xct_adj"):
+        getattr(L, n).argtypes = [vp, ip, vp, vp, vp]
+    L.xct_plan_sync.argtypes = [vp]
+    L.xct_plan_last_ms.argtypes = [vp, fp]
+    L.xct_launch_count.restype = ctypes.c_longlong
+    L.xct_last_error.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != XCT_OK:
+        raise XCTError(rc, load().xct_last_error().decode(errors="replace"))
+
+
+def subset_order(ss):
+    """Subset order of OSEM_ocl (GPU.cpp:564-582)."""
+    out = (ctypes.c_int * ss)()
+    _check(load().xct_subset_order(ss, out))
+    return np.array(out[:], dtype=np.int32)
+
+
+def launch_count():
+    return int(load().xct_launch_count())
+
+
+def device_count():
+    n = ctypes.c_int(0)
+    _check(load().xct_device_count(ctypes.byref(n)))
+    return n.value
+
+
+def _ptr(t):
+    """Device pointer of a contiguous float32 CUDA tensor (or an int address)."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if not t.is_contiguous():
+        raise XCTError(XCT_E_INVALID, "tensor must be contiguous")
+    if str(t.dtype) != "torch.float32":
+        raise XCTError(XCT_E_INVALID, "tensor must be float32")
+    if not t.is_cuda:
+        raise XCTError(XCT_E_INVALID, "tensor must be on a CUDA device")
+    return t.data_ptr()
+
+
+def _stream(stream):
+    if stream is None:
+        try:
+            import torch
+            return torch.cuda.current_stream().cuda_stream
+        except Exception:
+            return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Context:
+    """One CUDA device (replaces OCL_platform_device for a single device)."""
+
+    def __init__(self, device=0):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        _check(self._lib.xct_ctx_create(device, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self._lib.xct_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OSEMPlan:
+    """An OS-EM plan: geometry, angle table and device work buffers for up to
+    ``max_batch`` slices per call."""
+
+    def __init__(self, ctx, nx, ny, px, angles_deg, ss, it, center_bin=None, fetch_mode=FETCH_EXACT,
+                 subset_mode=SUBSETS_REF, correction_mode=0, max_batch=1, kernels=KERNELS_TILED):
+        self._lib = load()
+        self.ctx = ctx
+        self.angles = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        self.nx, self.ny, self.px, self.pa, self.ss, self.it = nx, ny, px, int(self.angles.size), ss, it
+        self.max_batch = max_batch
+        g = Geom(nx, ny, nx, ny, px, self.pa, ss, it,
+                 self.angles.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                 -1.0 if center_bin is None else float(center_bin),
+                 fetch_mode, subset_mode, correction_mode, max_batch, kernels)
+        h = ctypes.c_void_p()
+        _check(self._lib.xct_osem_plan_create(ctx.handle, ctypes.byref(g), ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self._lib.xct_osem_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _sub(self, sub):
+        if sub is None:
+            return None
+        a = (ctypes.c_int * self.ss)(*[int(v) for v in sub])
+        return a
+
+    # ---- host arrays (blocking) --------------------------------------------------------
+    def run(self, sinos, imgs, sub=None, it=-1):
+        """OS-EM on host arrays: ``sinos`` dN float32 [pa][px], ``imgs`` dN float32
+        [ny][nx] (initial images in, reconstructions written back in place)."""
+        dN = len(sinos)
+        fp = ctypes.POINTER(ctypes.c_float)
+        for a in list(sinos) + list(imgs):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                raise XCTError(XCT_E_INVALID, "host arrays must be C-contiguous float32 numpy arrays")
+        s_arr = (fp * dN)(*[s.ctypes.data_as(fp) for s in sinos])
+        i_arr = (fp * dN)(*[i.ctypes.data_as(fp) for i in imgs])
+        _check(self._lib.xct_osem_run(self.handle, dN, s_arr, i_arr, self._sub(sub), it))
+        return imgs
+
+    def last_ms(self):
+        v = ctypes.c_float()
+        _check(self._lib.xct_plan_last_ms(self.handle, ctypes.byref(v)))
+        return v.value
+
+    # ---- device tensors (asynchronous on the stream) ----------------------------------
+    def run_device(self, d_sino, d_img, dN=None, sub=None, it=-1, stream=None):
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_osem_run_device(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
+                                             _stream(stream)))
+
+    def fwd(self, d_img, d_sino, dN=None, stream=None):
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_fwd(self.handle, dN, _ptr(d_img), _ptr(d_sino), _stream(stream)))
+
+    def bp_ref(self, d_sino, d_img, dN=None, stream=None):
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_bp_ref(self.handle, dN, _ptr(d_sino), _ptr(d_img), _stream(stream)))
+
+    def adj(self, d_sino, d_img, dN=None, stream=None):
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_adj(self.handle, dN, _ptr(d_sino), _ptr(d_img), _stream(stream)))
+
+    def sync(self):
+        _check(self._lib.xct_plan_sync(self.handle))
+
+
+# ---------------------------------------------------------------- reference-named mirrors
+def OSEM_execution(plan, sub, reconst_img, prj_img, dN, it, prjCorrection=True, stream=None):
+    """Mirror of ``int OSEM_execution(queue, kernels, angle_buffer, int *sub,
+    Image2DArray reconst_img, Image2DArray prj_img, int dN, int it, bool prjCorrection)``
+    (CT_reconstruction.hpp:77, GPU.cpp:125-240) on device tensors: reconst_img [dN][ny][nx]
+    is updated in place from prj_img [dN][pa][px].  The sinogram correction is part of the
+    plan (correction_mode); prjCorrection=False runs with it disabled only if the plan's
+    mode is 0.  Returns 0."""
+    if not prjCorrection and plan is not None and getattr(plan, "_correction", 0):
+        raise XCTError(XCT_E_INVALID, "plan was built with a sinogram correction mode")
+    plan.run_device(prj_img, reconst_img, dN=dN, sub=sub, it=it, stream=stream)
+    return 0
+
+
+def OSEM_thread(plan, sub, imgs, prjs, startN, endN, it):
+    """Mirror of OSEM_thread (CT_reconstruction.hpp:88-90, GPU.cpp:408-476) without the
+    output thread: imgs[i] and prjs[i] for slices startN..endN are host arrays; the
+    reconstructions are written back into imgs.  Returns 0."""
+    dN = endN - startN + 1
+    plan.run(list(prjs[:dN]), list(imgs[:dN]), sub=sub, it=it)
+    return 0

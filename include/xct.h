@@ -1,0 +1,117 @@
+/*
+ * xct.h -- C ABI of the GB300 OS-EM library (libxct.so).
+ *
+ * Drop-in replacement for the OpenCL platform/queue layer and the OS-EM executors of
+ * NozomuIshiguro/CT-XAFS_analysis (CT_reconstruction).  Plain C types only: no CUDA,
+ * torch or C++ types cross this boundary.  Every call returns an int status (XCT_OK = 0,
+ * negative XCT_E_* on failure; the message is in xct_last_error(), per thread).
+ *
+ * Layouts are the reference's: a sinogram is float32 [pa][px] (bins fastest,
+ * CT_reconstruction/fileIO.cpp:25-33, image (px, pa, layer) in GPU.cpp:423); an image is
+ * float32 [ny][nx] (x fastest, GPU.cpp:434-443, fileIO.cpp:35-43).  A batch of dN slices
+ * is dN such arrays back to back (the reference's image2d_array layers, GPU.cpp:139-140).
+ * Angles are degrees, one per projection (fileIO.cpp:11-23).
+ */
+#ifndef XCT_H
+#define XCT_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XCT_ABI_VERSION 1
+
+enum {
+    XCT_OK = 0,
+    XCT_E_INVALID = -1,     /* bad argument / shape                                   */
+    XCT_E_CUDA = -2,        /* CUDA runtime error                                     */
+    XCT_E_NOMEM = -3,       /* device or host allocation failed                       */
+    XCT_E_UNSUPPORTED = -4, /* device is not sm_103, or feature not built             */
+    XCT_E_TIMEOUT = -5,     /* a bounded device-side wait gave up                     */
+    XCT_E_IO = -6           /* file read/write error (host helpers)                    */
+};
+
+/* How OSEM1's read of the measured sinogram at integer coordinates with a LINEAR sampler
+ * (OSEM.cl:64, undefined in OpenCL 1.2) is interpreted. */
+enum { XCT_FETCH_EXACT = 0, XCT_FETCH_AVG2X2 = 1 };
+
+/* Rows of the ratio image that OSEM1 never writes when pa % ss != 0 (OSEM2 still reads
+ * them): XCT_SUBSETS_REF reads them as 0 (the reference's launch shape, GPU.cpp:169);
+ * XCT_SUBSETS_COVER forward-projects every row OSEM2 reads. */
+enum { XCT_SUBSETS_REF = 0, XCT_SUBSETS_COVER = 1 };
+
+/* Kernel family used by a plan: the optimised tiled kernels (default) or the plain
+ * one-thread-per-ray / one-thread-per-pixel kernels (the reference's launch shape). */
+enum { XCT_KERNELS_TILED = 0, XCT_KERNELS_PLAIN = 1 };
+
+typedef struct xct_ctx xct_ctx;
+typedef struct xct_plan xct_plan;
+
+/* Problem geometry of one OS-EM plan (the -D macros of OSEM_programBuild,
+ * GPU.cpp:538-548, plus the globals g_it, g_ss of main.cpp:29,35). */
+typedef struct {
+    int nx, ny;                /* reconstruction size (IMAGESIZE_X, IMAGESIZE_Y)              */
+    int ox, oy;                /* output ROI; must equal nx, ny (see DESIGN: ROI < full)      */
+    int px, pa;                /* detector bins (PRJ_IMAGESIZE), angles (PRJ_ANGLESIZE)       */
+    int ss;                    /* subsets (SS)                                                 */
+    int it;                    /* iterations (g_it)                                            */
+    const float *angles_deg;   /* [pa], copied at plan creation                                */
+    float center_bin;          /* rotation centre in bins; < 0 selects px/2 (the reference)    */
+    int measured_fetch_mode;   /* XCT_FETCH_*                                                  */
+    int subset_mode;           /* XCT_SUBSETS_*                                                */
+    int correction_mode;       /* sinogramCorrection mode 0..4 (reconstShare.cl:35-70); 0 none */
+    int max_batch;             /* largest dN passed to the run calls (numParallel, main.cpp:41)*/
+    int kernels;               /* XCT_KERNELS_*                                                */
+} xct_geom;
+
+/* ---- context: replaces OCL_platform_device (share source/OpenCL_analysis.hpp:126-147) */
+int xct_ctx_create(int device, xct_ctx **out);
+int xct_ctx_destroy(xct_ctx *ctx);
+/* Number of CUDA devices and the name of one (OpenCL_Device_Info equivalent). */
+int xct_device_count(int *count);
+int xct_device_name(int device, char *buf, int buflen);
+
+/* ---- plan: replaces OSEM_programBuild (GPU.cpp:513-559) -- no JIT, shapes are runtime */
+int xct_osem_plan_create(xct_ctx *ctx, const xct_geom *geom, xct_plan **out);
+int xct_osem_plan_destroy(xct_plan *plan);
+
+/* Subset order of OSEM_ocl (GPU.cpp:564-582): bit reversal for power-of-two ss. */
+int xct_subset_order(int ss, int *sub);
+
+/* ---- OS-EM: replaces OSEM_execution (GPU.cpp:125-240) + the host<->device image copies
+ * of OSEM_thread (GPU.cpp:440-445, 460-463).  sino_host[i] is slice i's [pa][px]
+ * sinogram, img_host[i] its [ny][nx] image (initial image in, reconstruction out).
+ * Blocking.  sub may be NULL (the plan's subset order).  it < 0 uses the plan's it. */
+int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *const *img_host, const int *sub,
+                 int it);
+
+/* Same on device memory: d_sino [dN][pa][px], d_img [dN][ny][nx] (in/out), enqueued on
+ * `stream` (a cudaStream_t; NULL = the plan's own stream).  Asynchronous. */
+int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
+                        void *stream);
+
+/* ---- operators on device memory (all angles, dN slices) ----------------------------
+ * xct_fwd    : the reference forward projector `projection` (reconstShare.cl:213-241),
+ *              bilinear ray sums, d_sino[dN][pa][px] = A d_img.
+ * xct_bp_ref : the reference plain backprojector `backProjection`
+ *              (reconstShare.cl:245-275) with ss = 1, sub = 0 (all angles).
+ * xct_adj    : the exact adjoint A^T of xct_fwd (d_img = A^T d_sino).               */
+int xct_fwd(xct_plan *plan, int dN, const float *d_img, float *d_sino, void *stream);
+int xct_bp_ref(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
+int xct_adj(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
+
+/* Synchronise the plan's stream; report the device time of the last xct_osem_run (ms). */
+int xct_plan_sync(xct_plan *plan);
+int xct_plan_last_ms(xct_plan *plan, float *ms);
+
+/* Kernel launches issued by this process since load (for launch accounting). */
+long long xct_launch_count(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *xct_last_error(void);
+int xct_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,77 @@
+"""Recipe for oracle/_ref: the reference's own OpenCL kernels compiled on the host.
+
+TEST INFRASTRUCTURE ONLY.  The reference (NozomuIshiguro/CT-XAFS_analysis) has no tests
+and no CPU build; its kernels are OpenCL C JIT-compiled at run time with the problem shape
+as -D macros (CT_reconstruction/GPU.cpp:537-550).  This recipe compiles
+CT_reconstruction/OSEM.cl and CT_reconstruction/reconstShare.cl, where they lie in the
+reference checkout, with g++ against oracle/ref_shim/cl_shim.hpp (an OpenCL-C environment
+written for this project).  The only change to the kernel text is mechanical and happens
+in the build output: OpenCL vector literals ``(float4)(a,b,c,d)`` become constructor calls
+``float4(a,b,c,d)`` (C++ would parse the former as a comma expression).  The generated
+translation unit and the shared objects go to oracle/_ref/ (git-ignored), one library per
+problem shape, exactly as the reference JIT-builds one program per shape.
+
+The reference checkout is only present where the project is developed; on a machine
+without it ``available()`` is False and the tests that use this build skip.
+"""
+import os
+import re
+import subprocess
+import hashlib
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("XCT_REFERENCE_ROOT", "/root/reference")
+OUT = os.path.join(HERE, "_ref")
+KERNELS = ("CT_reconstruction/OSEM.cl", "CT_reconstruction/reconstShare.cl")
+_VEC = re.compile(r"\((float|int)([234])\)\s*\(")
+
+
+def available():
+    return all(os.path.isfile(os.path.join(REF_ROOT, k)) for k in KERNELS)
+
+
+def _rewrite(text):
+    text = text.lstrip("﻿")
+    return _VEC.sub(lambda m: "%s%s(" % (m.group(1), m.group(2)), text)
+
+
+def build(nx, ny, px, pa, ss, force=False):
+    """Compile the reference kernels for one shape; return the .so path."""
+    if not available():
+        raise FileNotFoundError("reference kernel sources not found under %s" % REF_ROOT)
+    os.makedirs(OUT, exist_ok=True)
+    parts = ['#include "%s"' % os.path.join(HERE, "ref_shim", "cl_shim.hpp"), "namespace clk {"]
+    for k in KERNELS:
+        with open(os.path.join(REF_ROOT, k), encoding="utf-8") as f:
+            parts.append("// ---- %s (vector literals rewritten) ----" % k)
+            parts.append(_rewrite(f.read()))
+    parts.append("}  // namespace clk")
+    parts.append('#include "%s"' % os.path.join(HERE, "ref_shim", "ref_driver.inc"))
+    src = "\n".join(parts) + "\n"
+    tag = "%dx%d_%dx%d_s%d" % (nx, ny, px, pa, ss)
+    h = hashlib.sha1(src.encode())
+    for dep in ("cl_shim.hpp", "ref_driver.inc"):
+        with open(os.path.join(HERE, "ref_shim", dep), "rb") as f:
+            h.update(f.read())
+    digest = h.hexdigest()[:10]
+    cpp = os.path.join(OUT, "ref_kernels_%s.cpp" % tag)
+    so = os.path.join(OUT, "libref_%s_%s.so" % (tag, digest))
+    if os.path.exists(so) and not force:
+        return so
+    with open(cpp, "w") as f:
+        f.write(src)
+    defs = [
+        "-DIMAGESIZE_X=%d" % nx, "-DIMAGESIZE_Y=%d" % ny, "-DIMAGESIZE_M=%d" % (nx * ny),
+        "-DDEPTHSIZE=%d" % max(nx, ny), "-DPRJ_IMAGESIZE=%d" % px, "-DPRJ_ANGLESIZE=%d" % pa,
+        "-DPRJ_IMAGESIZE_M=%d" % (px * pa), "-DSS=%d" % ss, "-DLAMBDA_FISTA=0.0001",
+    ]
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-shared", "-fPIC",
+           "-w", "-o", so, cpp] + defs
+    subprocess.run(cmd, check=True)
+    return so
+
+
+if __name__ == "__main__":
+    import sys
+    shape = [int(v) for v in sys.argv[1:6]] if len(sys.argv) >= 6 else [64, 64, 64, 90, 10]
+    print(build(*shape))

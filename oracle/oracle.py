@@ -1,0 +1,270 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import
+this module, as the checker.  It wraps oracle/liboracle.so (the C restatement in
+xct_oracle.c) and, where it was built, oracle/_ref (the reference's own OpenCL kernels
+compiled through oracle/ref_shim; see build_ref.py).
+"""
+import ctypes
+import os
+import platform
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+ORDER_CANONICAL = 0
+ORDER_FWD_LITERAL = 1
+ORDER_BP_LITERAL = 2
+ORDER_LITERAL = 3
+ORDER_GPU = 2
+
+
+class Geom(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("px", ctypes.c_int), ("pa", ctypes.c_int),
+        ("ss", ctypes.c_int), ("depth", ctypes.c_int),
+        ("cx", ctypes.c_double),
+        ("order", ctypes.c_int), ("fetch_mode", ctypes.c_int),
+    ]
+
+
+def make_geom(nx, ny, px, pa, ss, cx=None, order=ORDER_CANONICAL, fetch_mode=0):
+    return Geom(nx, ny, px, pa, ss, max(nx, ny), px * 0.5 if cx is None else float(cx), order, fetch_mode)
+
+
+def build(force=False):
+    """Compile oracle/liboracle.so from xct_oracle.c (no contraction; OpenMP)."""
+    src = os.path.join(HERE, "xct_oracle.c")
+    deps = [src, os.path.join(HERE, "xct_oracle_body.h"), os.path.join(HERE, "xct_oracle.h")]
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(d) for d in deps)):
+        return LIB_PATH
+    flags = ["-O2", "-fopenmp", "-ffp-contract=off", "-shared", "-fPIC"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags.append("-mfma")  # hardware fmaf (same correctly rounded result as a libm call)
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    subprocess.run(["gcc"] + flags + ["-o", tmp, src, "-lm"], check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        fp = ctypes.POINTER(ctypes.c_float)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        gp = ctypes.POINTER(Geom)
+        for sfx, p, r in (("_f32", fp, ctypes.c_float), ("_f64", dp, ctypes.c_double)):
+            getattr(L, "xo_projection" + sfx).argtypes = [p, p, gp, ctypes.c_int, ctypes.c_int, ctypes.c_int, p]
+            getattr(L, "xo_osem1" + sfx).argtypes = [p, p, p, gp, ctypes.c_int, ctypes.c_int, p]
+            getattr(L, "xo_osem2" + sfx).argtypes = [p, p, p, p, gp, ctypes.c_int]
+            getattr(L, "xo_backprojection" + sfx).argtypes = [p, p, gp, ctypes.c_int, p]
+            getattr(L, "xo_aart1" + sfx).argtypes = [p, p, p, gp, ctypes.c_int, ctypes.c_int, p]
+            getattr(L, "xo_fista_bp" + sfx).argtypes = [p, p, p, p, gp, ctypes.c_int, r, r]
+            getattr(L, "xo_bp_fbp" + sfx).argtypes = [p, p, gp, p]
+            getattr(L, "xo_sino_correction" + sfx).argtypes = [p, p, fp, gp, ctypes.c_int]
+            getattr(L, "xo_osem_run" + sfx).argtypes = [p, p, p, gp, ip, ctypes.c_int, ctypes.c_int]
+        L.xo_trig_f32.argtypes = [fp, ctypes.c_int, fp]
+        L.xo_trig_f64.argtypes = [fp, ctypes.c_int, dp]
+        L.xo_subset_order.argtypes = [ctypes.c_int, ip]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a.dtype == np.float32:
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    if a.dtype == np.float64:
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    if a.dtype == np.int32:
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    raise TypeError(a.dtype)
+
+
+def _sfx(dtype):
+    return "_f32" if np.dtype(dtype) == np.float32 else "_f64"
+
+
+def trig(angles_deg, dtype=np.float32):
+    a = np.ascontiguousarray(angles_deg, dtype=np.float32)
+    cs = np.empty((a.size, 2), dtype=dtype)
+    getattr(lib(), "xo_trig" + _sfx(dtype))(_p(a), a.size, _p(cs))
+    return cs
+
+
+def subset_order(ss):
+    out = np.zeros(max(ss, 1), dtype=np.int32)
+    lib().xo_subset_order(ss, _p(out))
+    return out[:ss]
+
+
+def projection(img, angles_deg, px, ss=1, sub=0, nrows=None, cx=None, order=ORDER_CANONICAL, dtype=np.float32):
+    img = np.ascontiguousarray(img, dtype=dtype)
+    ny, nx = img.shape
+    pa = len(angles_deg)
+    g = make_geom(nx, ny, px, pa, ss, cx, order)
+    cs = trig(angles_deg, dtype)
+    nrows = pa // ss if nrows is None else nrows
+    out = np.zeros((pa, px), dtype=dtype)
+    getattr(lib(), "xo_projection" + _sfx(dtype))(_p(img), _p(cs), ctypes.byref(g), sub, ss, nrows, _p(out))
+    return out
+
+
+def osem1(img, meas, angles_deg, ss, sub, nrows=None, cx=None, order=ORDER_CANONICAL, fetch_mode=0,
+          dtype=np.float32, ratio=None):
+    img = np.ascontiguousarray(img, dtype=dtype)
+    meas = np.ascontiguousarray(meas, dtype=dtype)
+    ny, nx = img.shape
+    pa, px = meas.shape
+    g = make_geom(nx, ny, px, pa, ss, cx, order, fetch_mode)
+    cs = trig(angles_deg, dtype)
+    nrows = pa // ss if nrows is None else nrows
+    out = np.zeros((pa, px), dtype=dtype) if ratio is None else ratio
+    getattr(lib(), "xo_osem1" + _sfx(dtype))(_p(img), _p(meas), _p(cs), ctypes.byref(g), sub, nrows, _p(out))
+    return out
+
+
+def osem2(img, ratio, angles_deg, ss, sub, cx=None, order=ORDER_CANONICAL, dtype=np.float32):
+    img = np.ascontiguousarray(img, dtype=dtype)
+    ratio = np.ascontiguousarray(ratio, dtype=dtype)
+    ny, nx = img.shape
+    pa, px = ratio.shape
+    g = make_geom(nx, ny, px, pa, ss, cx, order)
+    cs = trig(angles_deg, dtype)
+    out = np.empty_like(img)
+    getattr(lib(), "xo_osem2" + _sfx(dtype))(_p(img), _p(out), _p(ratio), _p(cs), ctypes.byref(g), sub)
+    return out
+
+
+def backprojection(prj, angles_deg, nx, ny, ss=1, sub=0, order=ORDER_CANONICAL, dtype=np.float32):
+    prj = np.ascontiguousarray(prj, dtype=dtype)
+    pa, px = prj.shape
+    g = make_geom(nx, ny, px, pa, ss, None, order)
+    cs = trig(angles_deg, dtype)
+    out = np.empty((ny, nx), dtype=dtype)
+    getattr(lib(), "xo_backprojection" + _sfx(dtype))(_p(prj), _p(cs), ctypes.byref(g), sub, _p(out))
+    return out
+
+
+def aart1(img, meas, angles_deg, ss, sub, nrows=None, dtype=np.float32):
+    img = np.ascontiguousarray(img, dtype=dtype)
+    meas = np.ascontiguousarray(meas, dtype=dtype)
+    ny, nx = img.shape
+    pa, px = meas.shape
+    g = make_geom(nx, ny, px, pa, ss, None, ORDER_LITERAL)
+    cs = trig(angles_deg, dtype)
+    nrows = pa // ss if nrows is None else nrows
+    out = np.zeros((pa, px), dtype=dtype)
+    getattr(lib(), "xo_aart1" + _sfx(dtype))(_p(img), _p(meas), _p(cs), ctypes.byref(g), sub, nrows, _p(out))
+    return out
+
+
+def fista_bp(img, dprj, angles_deg, ss, sub, alpha, L, dtype=np.float32):
+    img = np.ascontiguousarray(img, dtype=dtype)
+    dprj = np.ascontiguousarray(dprj, dtype=dtype)
+    ny, nx = img.shape
+    pa, px = dprj.shape
+    g = make_geom(nx, ny, px, pa, ss, None, ORDER_LITERAL)
+    cs = trig(angles_deg, dtype)
+    out = np.empty_like(img)
+    getattr(lib(), "xo_fista_bp" + _sfx(dtype))(_p(img), _p(out), _p(dprj), _p(cs), ctypes.byref(g), sub,
+                                                 alpha, L)
+    return out
+
+
+def bp_fbp(fprj, angles_deg, nx, ny, cx=None, dtype=np.float32):
+    fprj = np.ascontiguousarray(fprj, dtype=dtype)
+    pa, px = fprj.shape
+    g = make_geom(nx, ny, px, pa, 1, cx, ORDER_LITERAL)
+    cs = trig(angles_deg, dtype)
+    out = np.empty((ny, nx), dtype=dtype)
+    getattr(lib(), "xo_bp_fbp" + _sfx(dtype))(_p(fprj), _p(cs), ctypes.byref(g), _p(out))
+    return out
+
+
+def sino_correction(meas, angles_deg, mode, dtype=np.float32):
+    """sinogramCorrection (reconstShare.cl:35-70), modes 0..4."""
+    meas = np.ascontiguousarray(meas, dtype=dtype)
+    pa, px = meas.shape
+    g = make_geom(px, px, px, pa, 1)
+    ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+    out = np.empty_like(meas)
+    getattr(lib(), "xo_sino_correction" + _sfx(dtype))(_p(meas), _p(out), _p(ang), ctypes.byref(g), mode)
+    return out
+
+
+def osem_run(img0, meas, angles_deg, ss, it, sub_order=None, cx=None, order=ORDER_CANONICAL, fetch_mode=0,
+             cover=False, dtype=np.float32):
+    """Full OS-EM of one slice (OSEM_execution's loop); returns the updated image."""
+    img = np.array(img0, dtype=dtype, copy=True, order="C")
+    meas = np.ascontiguousarray(meas, dtype=dtype)
+    ny, nx = img.shape
+    pa, px = meas.shape
+    g = make_geom(nx, ny, px, pa, ss, cx, order, fetch_mode)
+    cs = trig(angles_deg, dtype)
+    so = subset_order(ss) if sub_order is None else np.ascontiguousarray(sub_order, dtype=np.int32)
+    getattr(lib(), "xo_osem_run" + _sfx(dtype))(_p(img), _p(meas), _p(cs), ctypes.byref(g), _p(so), it,
+                                                 1 if cover else 0)
+    return img
+
+
+# ----------------------------------------------------------------------------- oracle/_ref
+class RefKernels:
+    """The reference's OSEM.cl/reconstShare.cl compiled for one shape (see build_ref.py)."""
+
+    def __init__(self, nx, ny, px, pa, ss):
+        import build_ref  # noqa: local module beside this file
+        self.shape = (nx, ny, px, pa, ss)
+        self.lib = ctypes.CDLL(build_ref.build(nx, ny, px, pa, ss))
+        fp = ctypes.POINTER(ctypes.c_float)
+        ip = ctypes.POINTER(ctypes.c_int)
+        self.lib.ref_osem_execution.argtypes = [fp, fp, fp, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        self.lib.ref_projection.argtypes = [fp, fp, ctypes.c_int, fp]
+        self.lib.ref_backprojection.argtypes = [fp, fp, ctypes.c_int, fp]
+        self.lib.ref_sino_correction.argtypes = [fp, fp, ctypes.c_int, fp]
+
+    def osem_execution(self, imgs, prjs, angles_deg, sub_order, it, fetch_mode=0):
+        imgs = np.array(imgs, dtype=np.float32, copy=True, order="C")
+        prjs = np.ascontiguousarray(prjs, dtype=np.float32)
+        dN = imgs.shape[0] if imgs.ndim == 3 else 1
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        so = np.ascontiguousarray(sub_order, dtype=np.int32)
+        self.lib.ref_osem_execution(_p(imgs), _p(prjs), _p(ang), _p(so), dN, it, fetch_mode)
+        return imgs
+
+    def projection(self, img, angles_deg, sub=0):
+        nx, ny, px, pa, ss = self.shape
+        out = np.zeros((pa, px), dtype=np.float32)
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        self.lib.ref_projection(_p(np.ascontiguousarray(img, dtype=np.float32)), _p(ang), sub, _p(out))
+        return out
+
+    def sino_correction(self, prj, angles_deg, mode):
+        nx, ny, px, pa, ss = self.shape
+        out = np.zeros((pa, px), dtype=np.float32)
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        self.lib.ref_sino_correction(_p(np.ascontiguousarray(prj, dtype=np.float32)), _p(ang), mode, _p(out))
+        return out
+
+    def backprojection(self, prj, angles_deg, sub=0):
+        nx, ny, px, pa, ss = self.shape
+        out = np.zeros((ny, nx), dtype=np.float32)
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        self.lib.ref_backprojection(_p(np.ascontiguousarray(prj, dtype=np.float32)), _p(ang), sub, _p(out))
+        return out
+
+
+def ref_available():
+    import build_ref
+    return build_ref.available()

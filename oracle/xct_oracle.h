@@ -1,0 +1,60 @@
+/*
+ * xct_oracle.h -- declarations of the CPU oracle (TEST INFRASTRUCTURE ONLY; see
+ * xct_oracle.c).  Layouts follow the reference: a sinogram is float [pa][px] (px
+ * fastest), an image is float [ny][nx] (x fastest); cs is (cos, sin) per angle.
+ */
+#ifndef XCT_ORACLE_H
+#define XCT_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XO_ABI_VERSION 1
+
+enum {
+    XO_ORDER_CANONICAL = 0,
+    XO_ORDER_FWD_LITERAL = 1,
+    XO_ORDER_BP_LITERAL = 2,
+    XO_ORDER_LITERAL = 3,  /* both stages exactly as written in the reference   */
+    XO_ORDER_GPU = 2       /* canonical forward + literal backprojection: CUDA's */
+};
+
+typedef struct {
+    int nx, ny;     /* reconstruction size (IMAGESIZE_X/Y)                        */
+    int px, pa;     /* detector bins, projection angles (PRJ_IMAGESIZE/ANGLESIZE) */
+    int ss;         /* subsets (SS)                                               */
+    int depth;      /* samples per ray, max(nx, ny) (DEPTHSIZE, GPU.cpp:542)     */
+    double cx;      /* detector centre in bins, px/2 in the reference             */
+    int order;      /* XO_ORDER_*                                                 */
+    int fetch_mode; /* measured read at integer coords: 0 exact texel, 1 2x2 avg  */
+} xo_geom;
+
+void xo_trig_f32(const float *ang_deg, int pa, float *cs);
+void xo_trig_f64(const float *ang_deg, int pa, double *cs);
+int xo_subset_order(int ss, int *sub);
+int xo_abi_version(void);
+
+#define XO_DECL(T, S)                                                                                   \
+    void xo_projection##S(const T *img, const T *cs, const xo_geom *g, int sub, int ss, int nrows, T *prj); \
+    void xo_osem1##S(const T *img, const T *meas, const T *cs, const xo_geom *g, int sub, int nrows,      \
+                     T *ratio);                                                                         \
+    void xo_osem2##S(const T *src, T *dst, const T *ratio, const T *cs, const xo_geom *g, int sub);       \
+    void xo_backprojection##S(const T *prj, const T *cs, const xo_geom *g, int sub, T *dst);               \
+    void xo_aart1##S(const T *img, const T *meas, const T *cs, const xo_geom *g, int sub, int nrows,      \
+                     T *dprj);                                                                          \
+    void xo_fista_bp##S(const T *src, T *dst, const T *dprj, const T *cs, const xo_geom *g, int sub,      \
+                        T alpha, T L);                                                                  \
+    void xo_bp_fbp##S(const T *fprj, const T *cs, const xo_geom *g, T *dst);                               \
+    void xo_sino_correction##S(const T *src, T *dst, const float *ang_deg, const xo_geom *g, int mode);    \
+    void xo_osem_run##S(T *img, const T *meas, const T *cs, const xo_geom *g, const int *sub_order, int it, \
+                        int cover);
+
+XO_DECL(float, _f32)
+XO_DECL(double, _f64)
+#undef XO_DECL
+
+#ifdef __cplusplus
+}
+#endif
+#endif

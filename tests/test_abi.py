@@ -1,0 +1,66 @@
+"""CPU checks of the C ABI: the library loads without a GPU, exports every function the
+public header declares, and its host-side logic (argument checks, subset order) works."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER_DIR = os.path.join(REPO, "include")
+
+
+def _declared_functions():
+    names = set()
+    for fn in os.listdir(HEADER_DIR):
+        if not fn.endswith(".h"):
+            continue
+        text = open(os.path.join(HEADER_DIR, fn)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[a-z_][a-z0-9_ ]*[\s\*]+(xct_[a-z0-9_]+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_expected_entry_points():
+    import xct
+    declared = _declared_functions()
+    assert declared, "no declarations parsed"
+    assert set(xct.EXPORTS) == declared
+
+
+def test_library_exports_every_declared_symbol(xct_lib):
+    for name in _declared_functions():
+        assert hasattr(xct_lib, name), name
+
+
+def test_abi_version_and_error_string(xct_lib):
+    assert xct_lib.xct_abi_version() == 1
+    assert isinstance(xct_lib.xct_last_error(), bytes)
+
+
+def test_subset_order_via_abi(xct_lib):
+    import xct
+    assert list(xct.subset_order(8)) == [0, 4, 2, 6, 1, 5, 3, 7]
+    assert list(xct.subset_order(10)) == list(range(10))
+    with pytest.raises(xct.XCTError) as e:
+        xct.subset_order(0)
+    assert e.value.code == xct.XCT_E_INVALID
+
+
+def test_null_arguments_rejected_without_gpu(xct_lib):
+    import xct
+    h = ctypes.c_void_p()
+    assert xct_lib.xct_osem_plan_create(None, None, ctypes.byref(h)) == xct.XCT_E_INVALID
+    assert b"null" in xct_lib.xct_last_error()
+    assert xct_lib.xct_osem_run_device(None, 1, None, None, None, 1, None) == xct.XCT_E_INVALID
+    assert xct_lib.xct_fwd(None, 1, None, None, None) == xct.XCT_E_INVALID
+
+
+def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
+    import xct
+    monkeypatch.setattr(xct, "LIB_PATH", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(xct, "_lib", None)
+    with pytest.raises(xct.XCTError):
+        xct.load()
