@@ -1,0 +1,418 @@
+"""Benchmark of the OS-EM hot path (one JSON line on rank 0).
+
+Workload: per-slice OS-EM at scale -- 100 independent slices of 2048x2048 float32,
+1500 projections over 180 deg, 2048 detector bins, 15 subsets x 4 iterations, seeded 3-D
+ellipsoid phantom (30 ellipsoids, attenuation 0.005-0.1 /px), I0 = 5e4 Poisson noise.
+Synthetic data: the sinograms are made on the device with this library's own forward
+projector (the reference projector model), then noised and log-converted.
+
+A step is one OSEM_execution call on a batch of dN = 10 slices (the reference's
+numParallel default, CT_reconstruction/main.cpp:41): 4 iterations x 15 subsets.  Each
+step takes the next batch of the 100-slice volume (10 steps = the whole volume); one step's
+inputs (10 sinograms + 10 images, ~290 MB) exceed the 129 MB L2, so no flush is needed.
+
+Metric: slice-iterations per second (one slice through all 15 subsets once).
+  value          -- device-resident inputs, CUDA-event time over the K timed steps
+                    (max over ranks), tiled kernels, batched dN = 10;
+  e2e            -- the same metric through the C ABI call with host buffers
+                    (xct_osem_run: pinned host sinograms/images copied in and out
+                    inside the timed region);
+  per_slice      -- the plain one-slice-per-call path (plain kernels, dN = 1) and the tiled
+                    kernels at dN = 1, each on a bounded sample of slices;
+  roofline       -- the dominant kernel (tiled forward projector) timed live with CUDA
+                    events inside this run; its algorithmic FLOPs (12 per bilinear sample
+                    whose footprint meets the image) over its measured time, against the
+                    FP32 FMA peak measured by xct_fp32_peak in the same run;
+  cpu_baseline   -- the CPU oracle (OpenMP, all host cores) on a bounded sample.
+
+--impl reference times the reference algorithm on the host cores (the CPU restatement of
+the reference's OpenCL kernels; the OpenCL runtime the reference needs is not available
+on the GPU host).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "ct-xafs_analysis_gb300"))
+
+import numpy as np  # noqa: E402
+
+NX = NY = 2048
+PX = 2048
+PA = 1500
+SS = 15
+IT = 4
+NSLICES = 100
+DN = 10
+I0 = 5e4
+METRIC = "OS-EM slice-iters/s (2048^2, 1500 angles, 15 subsets x 4 it; rel-L2<=1e-4 vs ref)"
+UNIT = "slice-iters/s"
+WORKLOAD = "per-slice OS-EM at scale: 100 slices 2048x2048, 1500 angles/180deg, 2048 bins, 15 subsets x 4 it"
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+        self._thr = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._proc = None
+            return
+        self._thr = threading.Thread(target=self._read, daemon=True)
+        self._thr.start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+        if self._thr is not None:
+            self._thr.join(timeout=2)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def algorithmic_counts(angles, nx, ny, px, cx=None):
+    """T_fwd: bilinear samples whose 2x2 footprint meets the image (base texel in
+    [-1, nx-1] x [-1, ny-1]), per angle, from the exact chord of each ray; T_bp: (pixel,
+    angle) pairs whose nearest bin lands on the detector, per angle."""
+    cx = px * 0.5 if cx is None else cx
+    D = max(nx, ny)
+    phi = np.deg2rad(np.asarray(angles, np.float64))
+    t_fwd = np.zeros(len(angles))
+    t_bp = np.zeros(len(angles))
+    Xc = np.arange(px) - cx
+    Yc = np.arange(ny) - ny * 0.5
+    Xp = np.arange(nx) - nx * 0.5
+    for k, (c, s) in enumerate(zip(np.cos(phi), np.sin(phi))):
+        ax = Xc * c + nx * 0.5
+        ay = -Xc * s + ny * 0.5
+        lo = np.full(px, -np.inf)
+        hi = np.full(px, np.inf)
+        for a, sl, n in ((ax, s, nx), (ay, c, ny)):
+            if abs(sl) < 1e-12:
+                inside = (a >= -1) & (a < n)
+                lo = np.where(inside, lo, np.inf)
+                continue
+            y1 = (-1 - a) / sl + D * 0.5
+            y2 = (n - a) / sl + D * 0.5
+            lo = np.maximum(lo, np.minimum(y1, y2))
+            hi = np.minimum(hi, np.maximum(y1, y2))
+        lo = np.clip(np.ceil(lo), 0, D)
+        hi = np.clip(np.ceil(hi), 0, D)
+        t_fwd[k] = np.maximum(hi - lo, 0).sum()
+        # bins of row Y are floor(Xp*c - Yc*s + cx + 0.5): count X in [0, nx) with
+        # 0 <= Xp*c + off < px, an interval in X per row
+        off = cx + 0.5 - Yc * s
+        if abs(c) < 1e-12:
+            t_bp[k] = nx * np.count_nonzero((off >= 0) & (off < px))
+            continue
+        x1 = (0 - off) / c + nx * 0.5
+        x2 = (px - off) / c + nx * 0.5
+        a = np.clip(np.ceil(np.minimum(x1, x2)), 0, nx)
+        b = np.clip(np.ceil(np.maximum(x1, x2)), 0, nx)
+        t_bp[k] = np.maximum(b - a, 0).sum()
+    return t_fwd, t_bp
+
+
+def make_volume(torch, dev, nslices, seed=2):
+    """Sinograms [nslices][PA][PX] (noisy, log) and initial images [nslices][NY][NX] on dev."""
+    import xct
+    from xct import phantom
+    ctx = xct.Context(dev.index if dev.index is not None else 0)
+    plan = xct.OSEMPlan(ctx, NX, NY, PX, phantom.uniform_angles(PA), SS, IT, max_batch=1)
+    pars = phantom.ellipsoid_params(NX, nslices, 30, seed, mu=(0.005, 0.1))
+    sino = torch.empty((nslices, PA, PX), device=dev, dtype=torch.float32)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    for z in range(nslices):
+        img = phantom.ellipsoid_slice(pars, z, NX, NY, torch_device=dev).reshape(1, NY, NX).contiguous()
+        clean = torch.empty((1, PA, PX), device=dev, dtype=torch.float32)
+        plan.fwd(img, clean)
+        if not bool(torch.isfinite(clean).all()):
+            raise RuntimeError("non-finite projection of phantom slice %d" % z)
+        sino[z] = phantom.noisy_log_sinogram_torch(clean[0], I0, generator=gen)
+    torch.cuda.synchronize()
+    plan.close()
+    return sino
+
+
+def run_reference(args, rank):
+    """Reference arm: the reference algorithm on the host cores (CPU restatement of its
+    OpenCL kernels, OpenMP over all cores).  Each step is one subset of one slice."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from xct import phantom
+    oracle.build()
+    cores = os.cpu_count()
+    ang = phantom.uniform_angles(PA)
+    pars = phantom.ellipsoid_params(NX, NSLICES, 30, 2, mu=(0.005, 0.1))
+    img = phantom.ellipsoid_slice(pars, NSLICES // 2, NX, NY)
+    sub = oracle.subset_order(SS)
+    # a measured sinogram for the sample slice (the reference projector, noised)
+    meas = phantom.noisy_log_sinogram(oracle.projection(img, ang, PX, ss=SS, sub=int(sub[0])), I0, 3)
+    x = np.ones((NY, NX), np.float32)
+    ratio = np.zeros((PA, PX), np.float32)
+
+    def step(i):
+        s = int(sub[i % SS])
+        r = oracle.osem1(x, meas, ang, SS, s, order=oracle.ORDER_LITERAL, ratio=ratio)
+        return oracle.osem2(x, r, ang, SS, s, order=oracle.ORDER_LITERAL)
+
+    for i in range(args.warmup):
+        step(i)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        step(i)
+    dt = time.perf_counter() - t0
+    value = args.steps / SS / dt  # one subset = 1/15 of a slice-iteration
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "step": "one subset (OSEM1+OSEM2, 100 angles) of one slice",
+                   "parallelism": "host cores"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d subsets of one 2048^2 slice (OSEM1+OSEM2 each), OpenMP" % args.steps},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(nsub=3):
+    """Oracle (OpenMP, all cores) on `nsub` subsets of one slice; slice-iters/s."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from xct import phantom
+    oracle.build()
+    ang = phantom.uniform_angles(PA)
+    pars = phantom.ellipsoid_params(NX, NSLICES, 30, 2, mu=(0.005, 0.1))
+    img = phantom.ellipsoid_slice(pars, NSLICES // 2, NX, NY)
+    sub = oracle.subset_order(SS)
+    meas = oracle.projection(img, ang, PX, ss=SS, sub=int(sub[0]))
+    x = np.ones((NY, NX), np.float32)
+    t0 = time.perf_counter()
+    for i in range(nsub):
+        r = oracle.osem1(x, meas, ang, SS, int(sub[i]), order=oracle.ORDER_LITERAL)
+        x = oracle.osem2(x, r, ang, SS, int(sub[i]), order=oracle.ORDER_LITERAL)
+    dt = time.perf_counter() - t0
+    return {"value": nsub / SS / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d subsets (OSEM1+OSEM2) of one 2048^2 slice, 1500 angles, OpenMP" % nsub}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import xct
+    from xct import phantom
+
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    args.warmup = max(args.warmup, 3)
+
+    # each rank reconstructs its own slices (weak scaling: NSLICES per rank)
+    sino = make_volume(torch, dev, NSLICES, seed=2 + rank)
+    imgs = torch.ones((NSLICES, NY, NX), device=dev, dtype=torch.float32)
+    ang = phantom.uniform_angles(PA)
+    ctx = xct.Context(local)
+    plan = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, IT, max_batch=DN, kernels=xct.KERNELS_TILED)
+    stream = torch.cuda.current_stream(dev)
+    nb = NSLICES // DN
+
+    def step(i):
+        b = i % nb
+        x = imgs[b * DN:(b + 1) * DN]
+        x.fill_(1.0)  # uniform initial image (first_image, fileIO.cpp:55-68)
+        plan.run_device(sino[b * DN:(b + 1) * DN], x, dN=DN, stream=stream)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    l0 = xct.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = xct.launch_count() - l0
+    clk.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    slice_iters = args.steps * DN * IT * world
+    value = slice_iters / (ms * 1e-3)
+
+    # ---- parity spot check of the timed configuration (slice 0 vs a second run) ----
+    finite = bool(torch.isfinite(imgs[:DN]).all())
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    nprj, nimg = PA * PX, NY * NX
+    h_sino = [torch.empty((PA, PX), dtype=torch.float32).pin_memory() for _ in range(DN)]
+    h_img = [torch.empty((NY, NX), dtype=torch.float32).pin_memory() for _ in range(DN)]
+    for j in range(DN):
+        h_sino[j].copy_(sino[j])
+    h_sino_np = [t.numpy() for t in h_sino]
+    h_img_np = [t.numpy() for t in h_img]
+    e2e_steps = max(2, min(args.steps, 4))
+    for j in range(DN):
+        h_img_np[j].fill(1.0)
+    plan.run(h_sino_np, h_img_np)  # warm
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        for j in range(DN):
+            h_img_np[j].fill(1.0)
+        plan.run(h_sino_np, h_img_np)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": e2e_steps * DN * IT / e2e_s * world, "unit": UNIT,
+           "h2d_bytes_per_step": DN * (nprj + nimg) * 4, "d2h_bytes_per_step": DN * nimg * 4,
+           "steps": e2e_steps, "api": "xct_osem_run (host buffers, blocking)"}
+
+    # ---- per-slice paths (bounded samples) ----
+    per_slice = {}
+    for name, kern, nsl in (("plain", xct.KERNELS_PLAIN, 2), ("tiled", xct.KERNELS_TILED, 4)):
+        p1 = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, IT, max_batch=1, kernels=kern)
+        x = imgs[:1].clone()
+        p1.run_device(sino[:1], x, dN=1, it=1, stream=stream)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for z in range(nsl):
+            x.fill_(1.0)
+            p1.run_device(sino[z:z + 1], x, dN=1, stream=stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        per_slice[name] = {"value": nsl * IT / (a.elapsed_time(b) * 1e-3), "unit": UNIT, "slices": nsl}
+        p1.close()
+
+    # ---- roofline of the dominant kernel (live CUDA events, same stream) ----
+    prof = plan.profile(sino[:DN], imgs[:DN].fill_(1.0), dN=DN, stream=stream)
+    t_fwd, t_bp = algorithmic_counts(ang, NX, NY, PX)
+    fwd_flop_per_launch = 12.0 * t_fwd.sum() / SS * DN  # one subset's angles, dN slices
+    fwd_ms_avg = prof["fwd"]["ms"] / prof["fwd"]["launches"]
+    bp_flop_per_launch = 5.0 * t_bp.sum() / SS * DN + 4.0 * NX * NY * DN
+    bp_ms_avg = prof["bp"]["ms"] / prof["bp"]["launches"]
+    fp32_peak = xct.fp32_peak_tflops(local)
+    achieved = fwd_flop_per_launch / (fwd_ms_avg * 1e-3) / 1e12
+    # HBM view of the same kernel: it reads each image once per subset and adds one double
+    # per (ray, tile) -- compulsory bytes are tiny next to its arithmetic
+    fwd_bytes = DN * NX * NY * 4.0
+    roofline = {
+        "bound": "fp32", "kernel": "fwd_tiled_kernel (OSEM1 forward projection)",
+        "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+        "peak_source": "measured live by xct_fp32_peak (FMA-chain kernel) in this run",
+        "flop_per_launch": fwd_flop_per_launch, "ms_per_launch": fwd_ms_avg,
+        "traffic": None,
+        "hbm": {"achieved_gbs": fwd_bytes / (fwd_ms_avg * 1e-3) / 1e9, "peak_gbs": None,
+                "note": "compulsory image bytes per launch over its time"},
+        "bp": {"kernel": "bp_tiled_kernel (OSEM2 backprojection+update)", "ms_per_launch": bp_ms_avg,
+               "achieved_tflops": bp_flop_per_launch / (bp_ms_avg * 1e-3) / 1e12},
+        "share": {k: prof[k]["ms"] / prof["total"]["ms"] for k in ("fwd", "finalize", "bp")},
+    }
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            roofline["hbm"]["peak_gbs"] = json.load(f).get("hbm_gbs")
+    except Exception:
+        pass
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline_sample()
+        except Exception as e:  # reported, never fatal
+            cpu = {"value": None, "error": str(e)[:200]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantom, Poisson I0=5e4)",
+            "config": {"workload": WORKLOAD, "batch_slices_per_call": DN, "kernels": "tiled",
+                       "l2": "inputs larger than L2 (each step a new 290 MB batch)",
+                       "parallelism": "dp%d over slices" % world},
+            "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "per_slice": per_slice,
+            "roofline": roofline, "cpu_baseline": cpu, "finite": finite,
+            "launches_per_step": launches / max(args.steps, 1),
+        }
+        print(json.dumps(line), flush=True)
+    plan.close()
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -220,6 +220,14 @@ int xct_osem_plan_create(xct_ctx *ctx, const xct_geom *geom, xct_plan **out)
     if ((e = cudaMalloc(&p->d_ratio, sizeof(float) * nb * nprj)) != cudaSuccess) return fail(e, "cudaMalloc ratio");
     if ((e = cudaMemsetAsync(p->d_ratio, 0, sizeof(float) * nb * nprj, p->stream)) != cudaSuccess)
         return fail(e, "memset ratio");
+    if (geom->kernels == XCT_KERNELS_TILED) {
+        // ray-sum accumulator for the largest subset (OSEM2 reads ceil(pa/ss) rows)
+        p->acc_rows = (geom->pa + geom->ss - 1) / geom->ss;
+        const size_t n = nb * (size_t)p->acc_rows * geom->px;
+        if ((e = cudaMalloc(&p->d_acc, sizeof(double) * n)) != cudaSuccess) return fail(e, "cudaMalloc acc");
+        if ((e = cudaMemsetAsync(p->d_acc, 0, sizeof(double) * n, p->stream)) != cudaSuccess)
+            return fail(e, "memset acc");
+    }
     std::vector<float2> cs;
     xct_trig_table(p->angles.data(), geom->pa, cs);
     if ((e = cudaMemcpyAsync(p->d_trig, cs.data(), sizeof(float2) * geom->pa, cudaMemcpyHostToDevice, p->stream)) !=
@@ -287,12 +295,21 @@ static int osem_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, con
         if (rc) return rc;
         meas = p->d_corr;
     }
+    const bool tiled = p->g.kernels == XCT_KERNELS_TILED;
     for (int i = 0; i < it; ++i)
         for (int k = 0; k < p->g.ss; ++k) {
             const int s = sub[k];
-            int rc = launch_fwd_plain(g, p->d_trig, d_img, meas, p->d_ratio, dN, s, g.ss, subset_rows(p, s), st);
-            if (rc) return rc;
-            rc = launch_bp_update_plain(g, p->d_trig, d_img, p->d_ratio, dN, s, st);
+            int rc;
+            if (tiled) {
+                rc = launch_fwd_tiled(g, p->d_trig, d_img, meas, p->d_ratio, p->d_acc, dN, s, g.ss, subset_rows(p, s),
+                                      st);
+                if (rc) return rc;
+                rc = launch_bp_update_tiled(g, p->d_trig, d_img, p->d_ratio, dN, s, st);
+            } else {
+                rc = launch_fwd_plain(g, p->d_trig, d_img, meas, p->d_ratio, dN, s, g.ss, subset_rows(p, s), st);
+                if (rc) return rc;
+                rc = launch_bp_update_plain(g, p->d_trig, d_img, p->d_ratio, dN, s, st);
+            }
             if (rc) return rc;
         }
     return XCT_OK;
@@ -320,7 +337,7 @@ int xct_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, 
     if (rc) return rc;
     if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_osem_run_device: null device pointer");
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
-    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
     return osem_loop(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, st);
 }
 
@@ -361,8 +378,16 @@ int xct_fwd(xct_plan *p, int dN, const float *d_img, float *d_sino, void *stream
     if (rc) return rc;
     if (!d_img || !d_sino) return xct_fail(XCT_E_INVALID, "xct_fwd: null device pointer");
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
-    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
-    return launch_fwd_plain(p->kg, p->d_trig, d_img, nullptr, d_sino, dN, 0, 1, p->g.pa, st);
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
+    if (p->g.kernels != XCT_KERNELS_TILED)
+        return launch_fwd_plain(p->kg, p->d_trig, d_img, nullptr, d_sino, dN, 0, 1, p->g.pa, st);
+    // all angles, in chunks of the accumulator's row capacity
+    for (int r0 = 0; r0 < p->g.pa; r0 += p->acc_rows) {
+        const int n = std::min(p->acc_rows, p->g.pa - r0);
+        int rc = launch_fwd_tiled(p->kg, p->d_trig, d_img, nullptr, d_sino, p->d_acc, dN, r0, 1, n, st);
+        if (rc) return rc;
+    }
+    return XCT_OK;
 }
 
 int xct_bp_ref(xct_plan *p, int dN, const float *d_sino, float *d_img, void *stream)
@@ -371,7 +396,7 @@ int xct_bp_ref(xct_plan *p, int dN, const float *d_sino, float *d_img, void *str
     if (rc) return rc;
     if (!d_img || !d_sino) return xct_fail(XCT_E_INVALID, "xct_bp_ref: null device pointer");
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
-    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
     return launch_bp_ref_plain(p->kg, p->d_trig, d_sino, d_img, dN, 0, 1, st);
 }
 
@@ -383,6 +408,71 @@ int xct_adj(xct_plan *p, int dN, const float *d_sino, float *d_img, void *stream
     (void)d_img;
     (void)stream;
     return xct_fail(XCT_E_UNSUPPORTED, "xct_adj: not built yet");
+}
+
+int xct_osem_profile(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, void *stream,
+                     float *ms, long long *launches)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!d_sino || !d_img || !ms || !launches) return xct_fail(XCT_E_INVALID, "xct_osem_profile: null argument");
+    if (p->g.correction_mode > 0)
+        return xct_fail(XCT_E_UNSUPPORTED, "xct_osem_profile: plans with a sinogram correction are not profiled");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
+    const int *so = sub ? sub : p->sub_default.data();
+    const bool tiled = p->g.kernels == XCT_KERNELS_TILED;
+    const int nk = 3;
+    std::vector<cudaEvent_t> ev;
+    const int nlaunch = it * p->g.ss * nk;
+    ev.resize(2 * (size_t)nlaunch + 2);
+    for (auto &e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return xct_fail(XCT_E_CUDA, "xct_osem_profile: event create");
+    auto cleanup = [&]() {
+        for (auto &e : ev) cudaEventDestroy(e);
+    };
+    int q = 0;
+    cudaEventRecord(ev[ev.size() - 2], st);
+    for (int i = 0; i < it && rc == 0; ++i)
+        for (int k = 0; k < p->g.ss && rc == 0; ++k) {
+            const int s = so[k];
+            const int rows = subset_rows(p, s);
+            for (int kind = 0; kind < nk && rc == 0; ++kind) {
+                cudaEventRecord(ev[2 * q], st);
+                if (tiled) {
+                    if (kind == 0) rc = launch_fwd_tiled_main(p->kg, p->d_trig, d_img, p->d_acc, dN, s, p->g.ss, rows, st);
+                    else if (kind == 1)
+                        rc = launch_fwd_finalize(p->kg, d_sino, p->d_ratio, p->d_acc, dN, s, p->g.ss, rows, st);
+                    else rc = launch_bp_update_tiled(p->kg, p->d_trig, d_img, p->d_ratio, dN, s, st);
+                } else {
+                    if (kind == 0)
+                        rc = launch_fwd_plain(p->kg, p->d_trig, d_img, d_sino, p->d_ratio, dN, s, p->g.ss, rows, st);
+                    else if (kind == 2) rc = launch_bp_update_plain(p->kg, p->d_trig, d_img, p->d_ratio, dN, s, st);
+                }
+                cudaEventRecord(ev[2 * q + 1], st);
+                ++q;
+            }
+        }
+    cudaEventRecord(ev[ev.size() - 1], st);
+    cudaError_t e = cudaEventSynchronize(ev[ev.size() - 1]);
+    if (rc == 0 && e != cudaSuccess) rc = xct_cuda_fail(e, "xct_osem_profile: sync");
+    if (rc == 0) {
+        for (int kk = 0; kk < 4; ++kk) {
+            ms[kk] = 0.0f;
+            launches[kk] = 0;
+        }
+        for (int j = 0; j < q; ++j) {
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, ev[2 * j], ev[2 * j + 1]);
+            ms[j % nk] += t;
+            if (tiled || j % nk != 1) launches[j % nk] += 1;
+        }
+        cudaEventElapsedTime(&ms[3], ev[ev.size() - 2], ev[ev.size() - 1]);
+        launches[3] = launches[0] + launches[1] + launches[2];
+    }
+    cleanup();
+    return rc;
 }
 
 int xct_plan_sync(xct_plan *p)

@@ -41,8 +41,8 @@ struct xct_plan {
     float *d_corr = nullptr;     // [max_batch][pa][px] corrected sinogram (correction_mode > 0)
     float *d_corr_ang = nullptr; // [pa] x 2 per-angle correction factors
     float *d_corr_bin = nullptr; // [px] per-bin correction factors
-    float *d_acc = nullptr;      // tiled forward: per-ray partial sums [max_batch][rows][px]
-    size_t acc_elems = 0;
+    double *d_acc = nullptr;     // tiled forward: ray-sum accumulator [max_batch][acc_rows][px]
+    int acc_rows = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_ms = 0.0f;
@@ -75,6 +75,19 @@ int launch_bp_update_plain(const KGeom &g, const float2 *trig, float *img, const
 // backProjection (reconstShare.cl:245-275) with subset (sub, step): img = B prj.
 int launch_bp_ref_plain(const KGeom &g, const float2 *trig, const float *prj, float *img, int dN, int sub, int step,
                         cudaStream_t st);
+// Tiled forward projector (xct_tiled.cu): same contract as launch_fwd_plain; acc is a
+// zeroed [dN][nrows][px] double accumulator (left zeroed on return); nrows <= rows cap.
+int fwd_tiled_rows_cap();
+int launch_fwd_tiled(const KGeom &g, const float2 *trig, const float *img, const float *meas, float *out,
+                     double *acc, int dN, int sub, int step, int nrows, cudaStream_t st);
+// The two halves of launch_fwd_tiled (timed separately by xct_osem_profile).
+int launch_fwd_tiled_main(const KGeom &g, const float2 *trig, const float *img, double *acc, int dN, int sub, int step,
+                          int nrows, cudaStream_t st);
+int launch_fwd_finalize(const KGeom &g, const float *meas, float *out, double *acc, int dN, int sub, int step,
+                        int nrows, cudaStream_t st);
+// Tiled OSEM2 backprojection + update, in place (same contract as the plain one).
+int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const float *ratio, int dN, int sub,
+                           cudaStream_t st);
 // sinogramCorrection (reconstShare.cl:35-70), modes 1..4, src -> dst.
 int launch_sino_correction(const KGeom &g, const float *src, float *dst, const float *ang_fac, const float *bin_fac,
                            int mode, int dN, cudaStream_t st);

@@ -45,6 +45,7 @@ EXPORTS = (
     "xct_osem_plan_create", "xct_osem_plan_destroy", "xct_subset_order",
     "xct_osem_run", "xct_osem_run_device", "xct_fwd", "xct_bp_ref", "xct_adj",
     "xct_plan_sync", "xct_plan_last_ms", "xct_launch_count", "xct_last_error", "xct_abi_version",
+    "xct_osem_profile", "xct_fp32_peak",
 )
 
 
@@ -93,6 +94,9 @@ def load():
     L.xct_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, vp]
     for n in ("xct_fwd", "xct_bp_ref", "xct_adj"):
         getattr(L, n).argtypes = [vp, ip, vp, vp, vp]
+    L.xct_osem_profile.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, vp, fp,
+                                   ctypes.POINTER(ctypes.c_longlong)]
+    L.xct_fp32_peak.argtypes = [ip, fp]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong
@@ -115,6 +119,13 @@ def subset_order(ss):
 
 def launch_count():
     return int(load().xct_launch_count())
+
+
+def fp32_peak_tflops(device=0):
+    """Measured FP32 FMA throughput of the device (TFLOP/s)."""
+    v = ctypes.c_float()
+    _check(load().xct_fp32_peak(device, ctypes.byref(v)))
+    return v.value
 
 
 def device_count():
@@ -244,6 +255,17 @@ class OSEMPlan:
     def adj(self, d_sino, d_img, dN=None, stream=None):
         dN = d_img.shape[0] if dN is None else dN
         _check(self._lib.xct_adj(self.handle, dN, _ptr(d_sino), _ptr(d_img), _stream(stream)))
+
+    def profile(self, d_sino, d_img, dN=None, sub=None, it=-1, stream=None):
+        """Run OS-EM with CUDA events around every launch; returns a dict of summed device
+        milliseconds and launch counts per kernel kind (fwd, finalize, bp) and the total."""
+        dN = d_img.shape[0] if dN is None else dN
+        ms = (ctypes.c_float * 4)()
+        n = (ctypes.c_longlong * 4)()
+        _check(self._lib.xct_osem_profile(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
+                                          _stream(stream), ms, n))
+        keys = ("fwd", "finalize", "bp", "total")
+        return {k: {"ms": ms[i], "launches": int(n[i])} for i, k in enumerate(keys)}
 
     def sync(self):
         _check(self._lib.xct_plan_sync(self.handle))

@@ -86,7 +86,8 @@ int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *c
                  int it);
 
 /* Same on device memory: d_sino [dN][pa][px], d_img [dN][ny][nx] (in/out), enqueued on
- * `stream` (a cudaStream_t; NULL = the plan's own stream).  Asynchronous. */
+ * `stream` (a cudaStream_t; NULL is the legacy default stream, as everywhere in CUDA).
+ * Asynchronous; stream-ordered with the caller's own work on that stream. */
 int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                         void *stream);
 
@@ -99,6 +100,19 @@ int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_im
 int xct_fwd(xct_plan *plan, int dN, const float *d_img, float *d_sino, void *stream);
 int xct_bp_ref(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
 int xct_adj(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
+
+/* Tracing: xct_osem_run_device with CUDA events around every launch.  The reference
+ * enables CL_QUEUE_PROFILING_ENABLE but never reads the events
+ * (share source/OCL_platform_device_class.cpp:175-178).  ms[0..3] = summed device time of
+ * the forward-projection launches, of the ratio/finalize launches, of the
+ * backprojection launches, and of the whole loop; launches[0..3] = their counts.
+ * Synchronous. */
+int xct_osem_profile(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
+                     void *stream, float *ms, long long *launches);
+
+/* FP32 FMA throughput of a device (TFLOP/s), measured by a dependent-chain-free FMA
+ * kernel: the roofline denominator for the projectors. */
+int xct_fp32_peak(int device, float *tflops);
 
 /* Synchronise the plan's stream; report the device time of the last xct_osem_run (ms). */
 int xct_plan_sync(xct_plan *plan);
