@@ -372,6 +372,32 @@ int xct_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *cons
     return XCT_OK;
 }
 
+int xct_osem1(xct_plan *p, int dN, int sub, const float *d_img, const float *d_sino, float *d_ratio, void *stream)
+{
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if (!d_img || !d_sino || !d_ratio) return xct_fail(XCT_E_INVALID, "xct_osem1: null device pointer");
+    if (sub < 0 || sub >= p->g.ss) return xct_fail(XCT_E_INVALID, "xct_osem1: subset out of range");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
+    const int rows = subset_rows(p, sub);
+    if (p->g.kernels == XCT_KERNELS_TILED)
+        return launch_fwd_tiled(p->kg, p->d_trig, d_img, d_sino, d_ratio, p->d_acc, dN, sub, p->g.ss, rows, st);
+    return launch_fwd_plain(p->kg, p->d_trig, d_img, d_sino, d_ratio, dN, sub, p->g.ss, rows, st);
+}
+
+int xct_osem2(xct_plan *p, int dN, int sub, float *d_img, const float *d_ratio, void *stream)
+{
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if (!d_img || !d_ratio) return xct_fail(XCT_E_INVALID, "xct_osem2: null device pointer");
+    if (sub < 0 || sub >= p->g.ss) return xct_fail(XCT_E_INVALID, "xct_osem2: subset out of range");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
+    if (p->g.kernels == XCT_KERNELS_TILED) return launch_bp_update_tiled(p->kg, p->d_trig, d_img, d_ratio, dN, sub, st);
+    return launch_bp_update_plain(p->kg, p->d_trig, d_img, d_ratio, dN, sub, st);
+}
+
 int xct_fwd(xct_plan *p, int dN, const float *d_img, float *d_sino, void *stream)
 {
     int rc = check_run(p, dN, nullptr, 0);

@@ -2,79 +2,82 @@
 //
 // Forward projector (OSEM1 / projection, OSEM.cl:38-68, reconstShare.cl:213-241),
 // tile-stationary:
-//   * one CTA owns an image tile: the taps whose base texel (floor(x), floor(y)) lies in
+//   * one CTA owns an image tile: the samples whose base texel (floor(x), floor(y)) lies in
 //     [x0, x0+T) x [y0, y0+T), with x0 = -1 + bx*T (base texel -1 still reaches texel 0).
-//     It stages texels [x0, x0+T] x [y0, y0+T] (zero outside the image: the sampler's
-//     CLK_ADDRESS_CLAMP border) in shared memory ONCE and serves every angle of its angle
-//     chunk from there, so the image is read from L2 once per subset instead of once per
-//     angle;
-//   * a warp takes one angle and 32 consecutive rays; each lane computes the exact range of
-//     sample indices Y whose base texel is in the tile (the sample coordinates are monotone
-//     in Y, so the range is an interval), then sums those bilinear samples from shared
-//     memory with the same arithmetic as the plain kernel;
-//   * the per-tile partial ray sums are added into a double-precision accumulator with
-//     atomics (one per ray and tile; ~1 per 50-130 samples).
-// A finalize/ratio kernel turns the accumulator into the OSEM1 ratio (or the raw
-// projection) and clears it for the next subset.
+//     It stages the tile ONCE per subset in shared memory as (t, t[x+1] - t) pairs, so
+//     the x-lerp of a bilinear sample is one FMA and its 2x2 footprint is two 64-bit
+//     loads, and serves every angle of its angle chunk from there;
+//   * a warp takes one angle and 32 consecutive rays; each lane finds the exact interval of
+//     sample indices Y whose base texel lies in the tile (the coordinates are monotone in
+//     Y), then sums those samples with packed f32x2 coordinate/floor/fraction arithmetic;
+//   * per-tile partial ray sums go into a double-precision accumulator with one atomic per
+//     ray and tile.
+// A finalize kernel turns the accumulator into the OSEM1 ratio (or the raw projection)
+// and clears it for the next subset.
 //
 // Backprojector (OSEM2, OSEM.cl:71-105), footprint-staged:
-//   * one CTA owns a 32x32 pixel tile; for each angle of the subset it stages the window of
-//     ratio bins that the tile's pixels hit (bin coordinates are monotone in X and in Y, so
-//     the four corners bound the window exactly; <= 46 bins for 32x32) into shared memory
-//     with coalesced loads, then every thread gathers its 4 pixels' bins from there, in
-//     angle order, with the reference's own bin arithmetic (no contraction);
-//   * the multiplicative update is fused into the same kernel.
+//   * one CTA owns a 64x32 pixel tile; per angle it stages the window of ratio bins its
+//     pixels hit (bin coordinates are monotone in X and in Y, so the tile corners bound the
+//     window exactly) into shared memory with coalesced loads;
+//   * each thread gathers 8 pixels per angle, in angle order, evaluating the reference's
+//     bin expression ((Xc*c - Yc*s) + cx) + 0.5 with packed f32x2 instructions (each lane
+//     rounds exactly like the scalar expression) and the nearest rule as a round-down add;
+//   * the multiplicative update is fused.
 #include "xct_device.cuh"
+#include "xct_f32x2.cuh"
 
 namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kFwdTile = 64;           // owned base texels per tile side
-constexpr int kFwdPitch = kFwdTile + 1; // staged texels per row (T + 1)
-constexpr int kAngChunk = 128;          // angles per CTA (forward) / per staging pass (back)
-constexpr int kBpTile = 32;             // pixels per backprojection tile side
-constexpr int kBpWin = 48;              // staged bins per angle (>= 31*(|c|+|s|) + 3)
+constexpr int kAngChunk = 128;  // angles per CTA (forward) / per staging pass (back)
+
+constexpr int kFwdT = 96;             // owned base texels per tile side
+constexpr int kFwdP = kFwdT + 1;      // element pitch (odd: spreads 64-bit banks)
+constexpr int kFwdRows = kFwdT + 1;   // a base row r reads element rows r and r+1
+constexpr size_t kFwdSmem = (size_t)kFwdP * kFwdRows * sizeof(float2) + kAngChunk * sizeof(float2);
+
+constexpr int kBpTX = 64, kBpTY = 32;  // backprojection tile (pixels)
+constexpr int kBpW = 76;               // staged bins per angle (>= 63|c| + 31|s| + 3)
+
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 
 // ---------------------------------------------------------------------- ray intervals
-// Sample coordinate along a ray: u(Y) = fma(Y - hd, sl, a), monotone in Y.
 __device__ __forceinline__ float ray_coord(int Y, float hd, float sl, float a)
 {
     return fmaf((float)Y - hd, sl, a);
 }
 
-// First Y in [0, D] where the monotone predicate P(Y) holds (D if none):
-//   sl > 0: P(Y) = u(Y) >= b ;  sl < 0: P(Y) = u(Y) < b.
-// Estimate from the real crossing point, correct with a few exact evaluations, and fall
-// back to a binary search (11-12 steps) when the slope is too small for the estimate.
-__device__ int first_true(float b, float a, float sl, float inv_sl, float hd, int D)
+// First Y in [0, D] where the monotone predicate P holds (D if none), with the sentinels
+// P(-1) = false, P(D) = true:  sl > 0: P(Y) = u(Y) >= b;  sl < 0: P(Y) = u(Y) < b,
+// u(Y) = fma(Y - hd, sl, a).  The estimate from the real crossing point is checked with
+// two exact evaluations; a binary search settles the rare cases it misses.
+__device__ __noinline__ int first_true_search(float b, float a, float sl, float hd, int D)
 {
     const bool up = sl > 0.0f;
-    auto P = [&](int Y) {
-        const float u = ray_coord(Y, hd, sl, a);
-        return up ? (u >= b) : (u < b);
-    };
+    int lo = 0, hi = D;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const float u = ray_coord(mid, hd, sl, a);
+        if (up ? (u >= b) : (u < b)) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int first_true(float b, float a, float sl, float inv_sl, float hd, int D)
+{
+    const bool up = sl > 0.0f;
     float e = fmaf(b - a, inv_sl, hd);
     e = fminf(fmaxf(e, -1.0f), (float)D + 1.0f);  // also maps +-inf; NaN -> -1
     int Y = (int)ceilf(e);
-    Y = Y < 0 ? 0 : (Y > D ? D : Y);
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        if (Y > 0 && P(Y - 1)) --Y;
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        if (Y < D && !P(Y)) ++Y;
-    const bool ok = (Y == 0 || !P(Y - 1)) && (Y == D || P(Y));
-    if (!ok) {
-        int lo = 0, hi = D;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (P(mid)) hi = mid;
-            else lo = mid + 1;
-        }
-        Y = lo;
-    }
-    return Y;
+    Y = min(max(Y, 0), D);
+    const float ul = ray_coord(Y - 1, hd, sl, a);
+    const float uh = ray_coord(Y, hd, sl, a);
+    const bool pl = (Y > 0) && (up ? (ul >= b) : (ul < b));
+    const bool ph = (Y >= D) || (up ? (uh >= b) : (uh < b));
+    if (!pl && ph) return Y;
+    return first_true_search(b, a, sl, hd, D);
 }
 
 // Y range [ya, yb) of samples whose coordinate u lies in [lo, hi).
@@ -94,39 +97,66 @@ __device__ __forceinline__ void coord_range(float lo, float hi, float a, float s
     }
 }
 
+__device__ __forceinline__ void lds_f2(unsigned addr, float &a, float &b)
+{
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(a), "=f"(b) : "r"(addr));
+}
+__device__ __forceinline__ void lds_f2_next_row(unsigned addr, float &a, float &b)
+{
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(a), "=f"(b) : "r"(addr), "n"(kFwdP * 8));
+}
+__device__ __forceinline__ float lds_f1(unsigned addr)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+
 // ----------------------------------------------------------------- forward projector
-// grid: (ntx*nty tiles, angle chunks, dN).  acc: [dN][rows][px] doubles.
+// grid: (ntx*nty tiles, angle chunks, dN).  acc: [dN][nrows][px] doubles.
 __global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__restrict__ img,
                                                              double *__restrict__ acc,
                                                              const float2 *__restrict__ trig, KGeom g, int sub,
                                                              int step, int nrows, int ntx)
 {
-    __shared__ float tile[kFwdPitch * kFwdPitch];
-    __shared__ float2 scs[kAngChunk];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *tile = reinterpret_cast<float2 *>(smem_raw);
+    float2 *scs = reinterpret_cast<float2 *>(smem_raw + (size_t)kFwdP * kFwdRows * sizeof(float2));
 
     const int bx = blockIdx.x % ntx, by = blockIdx.x / ntx;
     const int z = blockIdx.z;
     const int k0 = blockIdx.y * kAngChunk;
     const int kn = min(kAngChunk, nrows - k0);
-    const int x0 = -1 + bx * kFwdTile, y0 = -1 + by * kFwdTile;
+    const int x0 = -1 + bx * kFwdT, y0 = -1 + by * kFwdT;
     const float *im = img + (size_t)z * g.nx * g.ny;
 
-    for (int i = threadIdx.x; i < kFwdPitch * kFwdPitch; i += kThreads) {
-        const int r = i / kFwdPitch, c = i - r * kFwdPitch;
+    // element (c, r) = (t(x0+c, y0+r), t(x0+c+1, y0+r) - t(x0+c, y0+r)), zero border
+    for (int i = threadIdx.x; i < kFwdT * kFwdRows; i += kThreads) {
+        const int r = i / kFwdT, c = i - r * kFwdT;
         const int gx = x0 + c, gy = y0 + r;
-        float v = 0.0f;
-        if ((unsigned)gx < (unsigned)g.nx && (unsigned)gy < (unsigned)g.ny) v = __ldg(im + (size_t)gy * g.nx + gx);
-        tile[i] = v;
+        float t0 = 0.0f, t1 = 0.0f;
+        if ((unsigned)gy < (unsigned)g.ny) {
+            const float *row = im + (size_t)gy * g.nx;
+            if ((unsigned)gx < (unsigned)g.nx) t0 = __ldg(row + gx);
+            if ((unsigned)(gx + 1) < (unsigned)g.nx) t1 = __ldg(row + gx + 1);
+        }
+        tile[r * kFwdP + c] = make_float2(t0, t1 - t0);
     }
     for (int k = threadIdx.x; k < kn; k += kThreads) scs[k] = trig[sub + (k0 + k) * step];
     __syncthreads();
 
-    // owned base-texel ranges (the union over tiles is [-1, n-1]: base texel -1 reaches
-    // texel 0, base texel n-1 still reads texel n-1)
-    const float xlo = (float)x0, xhi = (float)min(x0 + kFwdTile, g.nx);
-    const float ylo = (float)y0, yhi = (float)min(y0 + kFwdTile, g.ny);
+    // owned base-texel ranges (the union over tiles is [-1, n-1])
+    const float xlo = (float)x0, xhi = (float)min(x0 + kFwdT, g.nx);
+    const float ylo = (float)y0, yhi = (float)min(y0 + kFwdT, g.ny);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int D = g.depth;
+    // shared address of element (col, row) from the floor bits (col + BIAS + x0, ...):
+    // base2 + iy_bits * 8P + ix_bits * 8, with the biases folded into base2 (mod 2^32)
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(tile);
+    const unsigned bias = (unsigned)XCT_FLOOR_BIAS;
+    const unsigned base2 = sbase - (((bias + (unsigned)y0) * (unsigned)kFwdP + bias + (unsigned)x0) * 8u);
+    const f2x MM = f2_pack(kMagic, kMagic);
+    const f2x one2 = f2_pack(1.0f, 1.0f);
 
     for (int k = warp; k < kn; k += kWarps) {
         const float c = scs[k].x, s = scs[k].y;
@@ -144,6 +174,7 @@ __global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__rest
         }
         const int Xlo = max(0, (int)floorf(pmin) - 1);
         const int Xhi = min(g.px - 1, (int)ceilf(pmax) + 1);
+        const f2x sc = f2_pack(s, c);
         for (int base = Xlo; base <= Xhi; base += 32) {
             const int X = base + lane;
             int ya = 0, yb = 0;
@@ -158,22 +189,29 @@ __global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__rest
                 ya = max(a0, b0);
                 yb = min(a1, b1);
             }
+            const int n = yb - ya;
+            const float yc0 = (float)ya - g.hd;
+            f2x yc2 = f2_pack(yc0, yc0);
+            const f2x axy = f2_pack(ax, ay);
             float sum = 0.0f;
-            for (int Y = ya; Y < yb; ++Y) {
-                const float Yc = (float)Y - g.hd;
-                const float x = fmaf(Yc, s, ax);
-                const float y = fmaf(Yc, c, ay);
-                const int bxs = xct_floor_bits(x), bys = xct_floor_bits(y);
-                const float fx = x - (__int_as_float(bxs) - 12582912.0f);
-                const float fy = y - (__int_as_float(bys) - 12582912.0f);
-                const int col = bxs - XCT_FLOOR_BIAS - x0;
-                const int row = bys - XCT_FLOOR_BIAS - y0;
-                const float *t = tile + row * kFwdPitch + col;
-                const float q0 = xct_lerp(fx, t[0], t[1]);
-                const float q1 = xct_lerp(fx, t[kFwdPitch], t[kFwdPitch + 1]);
-                sum += xct_lerp(fy, q0, q1);
+            for (int i = 0; i < n; ++i) {
+                const f2x xy = f2_fma(yc2, sc, axy);       // (fma(Yc,s,ax), fma(Yc,c,ay))
+                const f2x tb = f2_add_rd(xy, MM);          // floor in the low mantissa bits
+                const f2x fr = f2_sub(xy, f2_sub(tb, MM)); // (fx, fy) = (x, y) - floor
+                int ixb, iyb;
+                f2_unpack_bits(tb, ixb, iyb);
+                float fx, fy;
+                f2_unpack(fr, fx, fy);
+                const unsigned addr = (unsigned)iyb * (unsigned)(kFwdP * 8) + (unsigned)ixb * 8u + base2;
+                float t00, d0, t01, d1;
+                lds_f2(addr, t00, d0);
+                lds_f2_next_row(addr, t01, d1);
+                const float r0 = fmaf(fx, d0, t00);
+                const float r1 = fmaf(fx, d1, t01);
+                sum += fmaf(fy, r1 - r0, r0);
+                yc2 = f2_add(yc2, one2);
             }
-            if (yb > ya) atomicAdd(acc + ((size_t)z * nrows + k0 + k) * g.px + X, (double)sum);
+            if (n > 0) atomicAdd(acc + ((size_t)z * nrows + k0 + k) * g.px + X, (double)sum);
         }
     }
 }
@@ -205,34 +243,43 @@ __global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ 
                                                             const float2 *__restrict__ trig, KGeom g, int sub,
                                                             int nang, int ntx, float ssf, float paf)
 {
-    __shared__ float win[kAngChunk * kBpWin];
-    __shared__ float2 scs[kAngChunk];
-    __shared__ int sbase[kAngChunk];
+    __shared__ float win[kAngChunk * kBpW];
+    __shared__ float2 scs[kAngChunk];    // (c, s)
+    __shared__ int slo[kAngChunk];       // first staged bin of the angle's window
+    __shared__ unsigned soff[kAngChunk]; // byte address of window entry (bits - BIAS - lo)
 
     const int bx = blockIdx.x % ntx, by = blockIdx.x / ntx;
     const int z = blockIdx.z;
-    const int X0 = bx * kBpTile, Y0 = by * kBpTile;
-    const int X1 = min(X0 + kBpTile, g.nx) - 1, Y1 = min(Y0 + kBpTile, g.ny) - 1;
-    const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;  // 8 x 4 pixels per row, 32 rows
+    const int X0 = bx * kBpTX, Y0 = by * kBpTY;
+    const int X1 = min(X0 + kBpTX, g.nx) - 1, Y1 = min(Y0 + kBpTY, g.ny) - 1;
+    const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;  // 8 threads x 8 pixels, 32 rows
     const int Y = Y0 + ty;
     // threads past the image edge of a partial tile gather for the edge pixel (inside the
     // staged window) and write nothing
     const float Yc = (float)min(Y, Y1) - g.hy;
-    float Xc[4], b[4];
+    f2x xcp[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        Xc[i] = (float)min(X0 + tx * 4 + i, X1) - g.hx;
-        b[i] = 0.0f;
+    for (int j = 0; j < 4; ++j) {
+        const float a = (float)min(X0 + tx * 8 + 2 * j, X1) - g.hx;
+        const float b = (float)min(X0 + tx * 8 + 2 * j + 1, X1) - g.hx;
+        xcp[j] = f2_pack(a, b);
     }
+    float acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = 0.0f;
+    const f2x cxp = f2_pack(g.cx, g.cx);
+    const f2x hp = f2_pack(0.5f, 0.5f);
+    const f2x MM = f2_pack(kMagic, kMagic);
     const float *rt = ratio + (size_t)z * g.pa * g.px;
+    const unsigned wbase = (unsigned)__cvta_generic_to_shared(win);
 
     for (int k0 = 0; k0 < nang; k0 += kAngChunk) {
         const int kn = min(kAngChunk, nang - k0);
-        __syncthreads();  // previous chunk's gathers are done with win/scs/sbase
+        __syncthreads();  // the previous chunk's gathers are done with the shared arrays
         for (int k = threadIdx.x; k < kn; k += kThreads) {
             const float2 cs = trig[sub + (k0 + k) * g.ss];
             scs[k] = cs;
-            // bin coordinate is monotone in X and in Y: the corners bound the window
+            // the bin coordinate is monotone in X and in Y: the corners bound the window
             const float xa = (float)X0 - g.hx, xb = (float)X1 - g.hx;
             const float yA = (float)Y0 - g.hy, yB = (float)Y1 - g.hy;
             const float qa = yA * cs.y, qb = yB * cs.y;
@@ -240,12 +287,15 @@ __global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ 
             lo = min(lo, xct_floor_bits(xct_bin_coord(xb, cs.x, qa, g.cx)));
             lo = min(lo, xct_floor_bits(xct_bin_coord(xa, cs.x, qb, g.cx)));
             lo = min(lo, xct_floor_bits(xct_bin_coord(xb, cs.x, qb, g.cx)));
-            sbase[k] = lo - XCT_FLOOR_BIAS;
+            slo[k] = lo - XCT_FLOOR_BIAS;
+            // entry for floor bits fb: wbase + 4*(k*W + fb - lo)  (mod 2^32)
+            soff[k] = wbase + 4u * (unsigned)(k * kBpW) - 4u * (unsigned)lo;
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < kn * kBpWin; i += kThreads) {
-            const int k = i / kBpWin, j = i - k * kBpWin;
-            const int bin = sbase[k] + j;
+        // element j of angle k holds ratio[th][lo_k + j] (0 off the detector)
+        for (int i = threadIdx.x; i < kn * kBpW; i += kThreads) {
+            const int k = i / kBpW, j = i - k * kBpW;
+            const int bin = slo[k] + j;
             const int th = sub + (k0 + k) * g.ss;
             win[i] = ((unsigned)bin < (unsigned)g.px) ? __ldg(rt + (size_t)th * g.px + bin) : 0.0f;
         }
@@ -253,22 +303,30 @@ __global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ 
         for (int k = 0; k < kn; ++k) {
             const float c = scs[k].x;
             const float q = Yc * scs[k].y;
-            const int off = k * kBpWin - (sbase[k] + XCT_FLOOR_BIAS);
+            const unsigned off = soff[k];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int bits = xct_floor_bits(xct_bin_coord(Xc[i], c, q, g.cx));
-                b[i] += win[bits + off];
+            for (int j = 0; j < 4; ++j) {
+                // Xc*c - q in scalar: ptxas contracts a packed multiply feeding a packed
+                // subtract into one fused operation whatever the rounding modifiers, and the
+                // reference rounds the product and the difference separately.  The three
+                // additions that follow are packed: ((.) + cx) + 0.5, then floor.
+                float xa, xb;
+                f2_unpack(xcp[j], xa, xb);
+                const float da = xa * c - q, db = xb * c - q;
+                const f2x t = f2_add_rd(f2_add(f2_add(f2_pack(da, db), cxp), hp), MM);
+                int b0, b1;
+                f2_unpack_bits(t, b0, b1);
+                acc[2 * j] += lds_f1((unsigned)b0 * 4u + off);
+                acc[2 * j + 1] += lds_f1((unsigned)b1 * 4u + off);
             }
         }
     }
     if (Y <= Y1) {
+        float *row = img + ((size_t)z * g.ny + Y) * g.nx;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int X = X0 + tx * 4 + i;
-            if (X <= X1) {
-                float *p = img + ((size_t)z * g.ny + Y) * g.nx + X;
-                *p = xct_update(*p, b[i], ssf, paf);
-            }
+        for (int i = 0; i < 8; ++i) {
+            const int X = X0 + tx * 8 + i;
+            if (X <= X1) row[X] = xct_update(row[X], acc[i], ssf, paf);
         }
     }
 }
@@ -277,29 +335,32 @@ __global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ 
 
 int fwd_tiled_rows_cap() { return kAngChunk; }
 
-int launch_fwd_tiled(const KGeom &g, const float2 *trig, const float *img, const float *meas, float *out,
-                     double *acc, int dN, int sub, int step, int nrows, cudaStream_t st)
+static int fwd_grid(const KGeom &g, int nrows, int dN, dim3 &grid, int &ntx)
 {
-    if (nrows <= 0 || dN <= 0) return XCT_OK;
-    const int ntx = (g.nx + 1 + kFwdTile - 1) / kFwdTile;  // base texels -1 .. nx-1
-    const int nty = (g.ny + 1 + kFwdTile - 1) / kFwdTile;
+    ntx = (g.nx + 1 + kFwdT - 1) / kFwdT;  // base texels -1 .. nx-1
+    const int nty = (g.ny + 1 + kFwdT - 1) / kFwdT;
     const int nch = (nrows + kAngChunk - 1) / kAngChunk;
-    dim3 grid(ntx * nty, nch, dN);
-    fwd_tiled_kernel<<<grid, kThreads, 0, st>>>(img, acc, trig, g, sub, step, nrows, ntx);
-    g_xct_launches.fetch_add(1, std::memory_order_relaxed);
-    XCT_CUDA_TRY(cudaGetLastError());
-    return launch_fwd_finalize(g, meas, out, acc, dN, sub, step, nrows, st);
+    grid = dim3(ntx * nty, nch, dN);
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        XCT_CUDA_TRY(cudaFuncSetAttribute(fwd_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kFwdSmem));
+        attr_set[dev] = true;
+    }
+    return XCT_OK;
 }
 
 int launch_fwd_tiled_main(const KGeom &g, const float2 *trig, const float *img, double *acc, int dN, int sub, int step,
                           int nrows, cudaStream_t st)
 {
     if (nrows <= 0 || dN <= 0) return XCT_OK;
-    const int ntx = (g.nx + 1 + kFwdTile - 1) / kFwdTile;
-    const int nty = (g.ny + 1 + kFwdTile - 1) / kFwdTile;
-    const int nch = (nrows + kAngChunk - 1) / kAngChunk;
-    dim3 grid(ntx * nty, nch, dN);
-    fwd_tiled_kernel<<<grid, kThreads, 0, st>>>(img, acc, trig, g, sub, step, nrows, ntx);
+    dim3 grid;
+    int ntx;
+    int rc = fwd_grid(g, nrows, dN, grid, ntx);
+    if (rc) return rc;
+    fwd_tiled_kernel<<<grid, kThreads, kFwdSmem, st>>>(img, acc, trig, g, sub, step, nrows, ntx);
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;
@@ -316,12 +377,20 @@ int launch_fwd_finalize(const KGeom &g, const float *meas, float *out, double *a
     return XCT_OK;
 }
 
+int launch_fwd_tiled(const KGeom &g, const float2 *trig, const float *img, const float *meas, float *out,
+                     double *acc, int dN, int sub, int step, int nrows, cudaStream_t st)
+{
+    int rc = launch_fwd_tiled_main(g, trig, img, acc, dN, sub, step, nrows, st);
+    if (rc) return rc;
+    return launch_fwd_finalize(g, meas, out, acc, dN, sub, step, nrows, st);
+}
+
 int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const float *ratio, int dN, int sub,
                            cudaStream_t st)
 {
     if (dN <= 0) return XCT_OK;
     const int nang = (g.pa - sub + g.ss - 1) / g.ss;  // OSEM2's angle loop (OSEM.cl:93)
-    const int ntx = (g.nx + kBpTile - 1) / kBpTile, nty = (g.ny + kBpTile - 1) / kBpTile;
+    const int ntx = (g.nx + kBpTX - 1) / kBpTX, nty = (g.ny + kBpTY - 1) / kBpTY;
     dim3 grid(ntx * nty, 1, dN);
     bp_tiled_kernel<<<grid, kThreads, 0, st>>>(img, ratio, trig, g, sub, nang, ntx, (float)g.ss, (float)g.pa);
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);

@@ -45,7 +45,7 @@ EXPORTS = (
     "xct_osem_plan_create", "xct_osem_plan_destroy", "xct_subset_order",
     "xct_osem_run", "xct_osem_run_device", "xct_fwd", "xct_bp_ref", "xct_adj",
     "xct_plan_sync", "xct_plan_last_ms", "xct_launch_count", "xct_last_error", "xct_abi_version",
-    "xct_osem_profile", "xct_fp32_peak",
+    "xct_osem_profile", "xct_fp32_peak", "xct_osem1", "xct_osem2",
 )
 
 
@@ -97,6 +97,8 @@ def load():
     L.xct_osem_profile.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, vp, fp,
                                    ctypes.POINTER(ctypes.c_longlong)]
     L.xct_fp32_peak.argtypes = [ip, fp]
+    L.xct_osem1.argtypes = [vp, ip, ip, vp, vp, vp, vp]
+    L.xct_osem2.argtypes = [vp, ip, ip, vp, vp, vp]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong
@@ -243,6 +245,17 @@ class OSEMPlan:
         dN = d_img.shape[0] if dN is None else dN
         _check(self._lib.xct_osem_run_device(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
                                              _stream(stream)))
+
+    def osem1(self, sub, d_img, d_sino, d_ratio, dN=None, stream=None):
+        """OSEM1 (OSEM.cl:38-68) alone: ratio rows of subset ``sub`` into d_ratio."""
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_osem1(self.handle, dN, sub, _ptr(d_img), _ptr(d_sino), _ptr(d_ratio),
+                                   _stream(stream)))
+
+    def osem2(self, sub, d_img, d_ratio, dN=None, stream=None):
+        """OSEM2 (OSEM.cl:71-105) alone: backprojection of d_ratio + update of d_img."""
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_osem2(self.handle, dN, sub, _ptr(d_img), _ptr(d_ratio), _stream(stream)))
 
     def fwd(self, d_img, d_sino, dN=None, stream=None):
         dN = d_img.shape[0] if dN is None else dN

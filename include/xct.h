@@ -91,6 +91,16 @@ int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *c
 int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                         void *stream);
 
+/* ---- the two OS-EM kernels as separate steps (dN slices, device memory) -------------
+ * xct_osem1 : OSEM1 (OSEM.cl:38-68) for subset `sub`: forward-projects d_img and writes
+ *             the measured/estimated ratio rows of the subset into d_ratio [dN][pa][px]
+ *             (other rows untouched).
+ * xct_osem2 : OSEM2 (OSEM.cl:71-105) for subset `sub`: backprojects d_ratio over the
+ *             subset's angles and applies the multiplicative update to d_img in place. */
+int xct_osem1(xct_plan *plan, int dN, int sub, const float *d_img, const float *d_sino, float *d_ratio,
+              void *stream);
+int xct_osem2(xct_plan *plan, int dN, int sub, float *d_img, const float *d_ratio, void *stream);
+
 /* ---- operators on device memory (all angles, dN slices) ----------------------------
  * xct_fwd    : the reference forward projector `projection` (reconstShare.cl:213-241),
  *              bilinear ray sums, d_sino[dN][pa][px] = A d_img.
