@@ -45,7 +45,7 @@ EXPORTS = (
     "xct_osem_plan_create", "xct_osem_plan_destroy", "xct_subset_order",
     "xct_osem_run", "xct_osem_run_device", "xct_fwd", "xct_bp_ref", "xct_adj",
     "xct_plan_sync", "xct_plan_last_ms", "xct_launch_count", "xct_last_error", "xct_abi_version",
-    "xct_osem_profile", "xct_fp32_peak", "xct_osem1", "xct_osem2",
+    "xct_osem_profile", "xct_fp32_peak", "xct_osem1", "xct_osem2", "xct_osem_run_static",
 )
 
 
@@ -99,6 +99,7 @@ def load():
     L.xct_fp32_peak.argtypes = [ip, fp]
     L.xct_osem1.argtypes = [vp, ip, ip, vp, vp, vp, vp]
     L.xct_osem2.argtypes = [vp, ip, ip, vp, vp, vp]
+    L.xct_osem_run_static.argtypes = [ctypes.POINTER(Geom), ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, vp]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong

@@ -91,6 +91,35 @@ int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *c
 int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                         void *stream);
 
+/* ---- OS-EM without any allocation ----------------------------------------------------
+ * No counterpart in the reference: the reference allocates its image objects on every call.
+ *
+ * For callers that cannot allocate device memory -- an acquisition loop that must never
+ * stall on cudaMalloc (it can synchronise the device), an application whose device memory
+ * is all owned by its own pool, code running where allocation is forbidden.  Same work as
+ * xct_osem_run_device with the tiled kernels, but without a plan: the caller passes the
+ * geometry, its device sinograms d_sino [dN][pa][px] and images d_img [dN][ny][nx] (initial
+ * image in, reconstruction out), and the function calls no cudaMalloc, cudaFree or other
+ * allocating routine.  Its scratch (angle table, ratio image, ray-sum accumulator) is one
+ * file-scope device array of XCT_STATIC_SCRATCH_BYTES bytes that every GPU that loads the
+ * library holds until the process exits.
+ *   - Limit: round256(8*pa) + round256(8*dN*ceil(pa/ss)*px) + 4*dN*pa*px bytes must fit in
+ *     XCT_STATIC_SCRATCH_BYTES = 16 MiB (e.g. one 2048x2048 slice with 1500 angles and 15
+ *     subsets needs 13.9 MB; round256 rounds up to a multiple of 256); larger problems get
+ *     XCT_E_INVALID with the byte counts in the message.  Sinogram correction modes are not
+ *     available here (XCT_E_UNSUPPORTED).
+ *   - Runs on the CURRENT device.  The first call on a device looks up the array's device
+ *     address (cudaGetSymbolAddress) for that device; make that first call before any
+ *     stream capture.
+ *   - Every call uses the same array and it keeps the last call's contents (each call clears
+ *     what must start at zero).  Calls whose GPU work overlaps -- on different streams or
+ *     host threads -- race on the array and give wrong results: serialise them.
+ *   - it < 0 uses geom->it; sub may be NULL (the reference's subset order); NULL stream is
+ *     the legacy default stream.  Asynchronous, like xct_osem_run_device. */
+#define XCT_STATIC_SCRATCH_BYTES (16u << 20)
+int xct_osem_run_static(const xct_geom *geom, int dN, const float *d_sino, float *d_img, const int *sub, int it,
+                        void *stream);
+
 /* ---- the two OS-EM kernels as separate steps (dN slices, device memory) -------------
  * xct_osem1 : OSEM1 (OSEM.cl:38-68) for subset `sub`: forward-projects d_img and writes
  *             the measured/estimated ratio rows of the subset into d_ratio [dN][pa][px]
