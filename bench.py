@@ -246,6 +246,26 @@ def cpu_baseline_sample(nsub=3):
             "sample": "%d subsets (OSEM1+OSEM2) of one 2048^2 slice, 1500 angles, OpenMP" % nsub}
 
 
+def profile_case():
+    """Small case for profilers: one 2048^2 slice of the workload, its sinogram made with the
+    forward projector (15 launches), then one OS-EM iteration (15 subsets: forward, finalize,
+    backprojection) with the tiled kernels.  ~150 MB on the device."""
+    import torch
+    import xct
+    from xct import phantom
+    ang = phantom.uniform_angles(PA)
+    ctx = xct.Context(0)
+    plan = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, 1, max_batch=1)
+    pars = phantom.ellipsoid_params(NX, NSLICES, 30, 2, mu=(0.005, 0.1))
+    img = phantom.ellipsoid_slice(pars, NSLICES // 2, NX, NY, torch_device="cuda").reshape(1, NY, NX).contiguous()
+    sino = torch.empty((1, PA, PX), device="cuda")
+    plan.fwd(img, sino)
+    x = torch.ones((1, NY, NX), device="cuda")
+    plan.run_device(sino, x, it=1)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "ok", "mean": float(x.mean())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -253,7 +273,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run the small profiling case (one slice, one iteration) and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case()
+        return
 
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
@@ -385,6 +410,17 @@ def main():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
             roofline["hbm"]["peak_gbs"] = json.load(f).get("hbm_gbs")
+    except Exception:
+        pass
+    # DRAM traffic of the forward kernel from the committed ncu capture of one slice, scaled
+    # to the DN slices of a bench launch (each slice's image is read once; 10 images exceed L2)
+    try:
+        with open(os.path.join(REPO, "profiles", "fwd_tiled_kernel_2048x2048_1500ang.md")) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_slice_launch:"):
+                    roofline["traffic"] = float(line.split(":")[1]) * DN
+                    roofline["traffic_source"] = ("ncu dram__bytes_read+write of one slice launch "
+                                                  "(profiles/fwd_tiled_kernel_2048x2048_1500ang.md) x %d slices" % DN)
     except Exception:
         pass
 

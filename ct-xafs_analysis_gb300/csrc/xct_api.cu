@@ -428,12 +428,11 @@ int xct_bp_ref(xct_plan *p, int dN, const float *d_sino, float *d_img, void *str
 
 int xct_adj(xct_plan *p, int dN, const float *d_sino, float *d_img, void *stream)
 {
-    (void)p;
-    (void)dN;
-    (void)d_sino;
-    (void)d_img;
-    (void)stream;
-    return xct_fail(XCT_E_UNSUPPORTED, "xct_adj: not built yet");
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if (!d_img || !d_sino) return xct_fail(XCT_E_INVALID, "xct_adj: null device pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return launch_adj_tiled(p->kg, p->d_trig, d_sino, d_img, dN, (cudaStream_t)stream);
 }
 
 int xct_osem_profile(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, void *stream,

@@ -88,6 +88,8 @@ int launch_fwd_finalize(const KGeom &g, const float *meas, float *out, double *a
 // Tiled OSEM2 backprojection + update, in place (same contract as the plain one).
 int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const float *ratio, int dN, int sub,
                            cudaStream_t st);
+// Exact adjoint of the forward projector over all angles: img = A^T sino (overwrites img).
+int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, cudaStream_t st);
 // sinogramCorrection (reconstShare.cl:35-70), modes 1..4, src -> dst.
 int launch_sino_correction(const KGeom &g, const float *src, float *dst, const float *ang_fac, const float *bin_fac,
                            int mode, int dN, cudaStream_t st);

@@ -216,6 +216,87 @@ __global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__rest
     }
 }
 
+// ------------------------------------------------------------------- exact adjoint
+// A^T of the forward projector: img[t] = sum over samples of w_t(sample) * sino[th][X], with
+// the bilinear weights w00 = (1-fx)(1-fy), w10 = fx(1-fy), w01 = (1-fx)fy, w11 = fx fy of the
+// sample's 2x2 footprint.  A CTA owns a T x T texel tile; it visits every sample whose base
+// texel lies in [x0-1, x0+T) x [y0-1, y0+T) (exactly those whose footprint touches the
+// tile), scatters its four weighted values into a shared (T+2)^2 accumulator with shared
+// atomics, and writes its own T x T texels once -- no global atomics, no overlap between
+// tiles.  grid: (ntx*nty tiles, 1, dN).
+constexpr int kAdjT = 64;
+constexpr int kAdjP = kAdjT + 2;
+
+__global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__restrict__ sino,
+                                                             float *__restrict__ img,
+                                                             const float2 *__restrict__ trig, KGeom g, int ntx)
+{
+    __shared__ float accs[kAdjP * kAdjP];
+    const int bx = blockIdx.x % ntx, by = blockIdx.x / ntx;
+    const int z = blockIdx.z;
+    const int x0 = bx * kAdjT, y0 = by * kAdjT;  // owned texels [x0, x0+T) x [y0, y0+T)
+    for (int i = threadIdx.x; i < kAdjP * kAdjP; i += kThreads) accs[i] = 0.0f;
+    __syncthreads();
+    const float *sn = sino + (size_t)z * g.pa * g.px;
+    // base texels whose footprint touches the tile
+    const float xlo = (float)(x0 - 1), xhi = (float)min(x0 + kAdjT, g.nx);
+    const float ylo = (float)(y0 - 1), yhi = (float)min(y0 + kAdjT, g.ny);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int D = g.depth;
+    for (int th = warp; th < g.pa; th += kWarps) {
+        const float2 cs = trig[th];
+        const float c = cs.x, s = cs.y;
+        const float inv_s = 1.0f / s, inv_c = 1.0f / c;
+        float pmin = 3.0e38f, pmax = -3.0e38f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float px_ = (q & 1) ? xhi + 2.0f : xlo - 2.0f;
+            const float py_ = (q & 2) ? yhi + 2.0f : ylo - 2.0f;
+            const float p = (px_ - g.hx) * c - (py_ - g.hy) * s + g.cx;
+            pmin = fminf(pmin, p);
+            pmax = fmaxf(pmax, p);
+        }
+        const int Xlo = max(0, (int)floorf(pmin) - 1);
+        const int Xhi = min(g.px - 1, (int)ceilf(pmax) + 1);
+        for (int base = Xlo; base <= Xhi; base += 32) {
+            const int X = base + lane;
+            int ya = 0, yb = 0;
+            float ax = 0.0f, ay = 0.0f, v = 0.0f;
+            if (X <= Xhi) {
+                v = __ldg(sn + (size_t)th * g.px + X);
+                const float Xc = (float)X - g.cx;
+                ax = fmaf(Xc, c, g.hx);
+                ay = fmaf(Xc, -s, g.hy);
+                int a0, a1, b0, b1;
+                coord_range(xlo, xhi, ax, s, inv_s, g.hd, D, a0, a1);
+                coord_range(ylo, yhi, ay, c, inv_c, g.hd, D, b0, b1);
+                ya = max(a0, b0);
+                yb = v != 0.0f ? min(a1, b1) : ya;  // a zero ray contributes nothing
+            }
+            for (int Y = ya; Y < yb; ++Y) {
+                const float Yc = (float)Y - g.hd;
+                const float x = fmaf(Yc, s, ax), y = fmaf(Yc, c, ay);
+                const float fi = floorf(x), fj = floorf(y);
+                const float fx = x - fi, fy = y - fj;
+                const int col = (int)fi - (x0 - 1), row = (int)fj - (y0 - 1);
+                const float gx = 1.0f - fx, gy = 1.0f - fy;
+                float *a = accs + row * kAdjP + col;
+                atomicAdd(a, gx * gy * v);
+                atomicAdd(a + 1, fx * gy * v);
+                atomicAdd(a + kAdjP, gx * fy * v);
+                atomicAdd(a + kAdjP + 1, fx * fy * v);
+            }
+        }
+    }
+    __syncthreads();
+    float *im = img + (size_t)z * g.nx * g.ny;
+    for (int i = threadIdx.x; i < kAdjT * kAdjT; i += kThreads) {
+        const int r = i / kAdjT, cc = i - r * kAdjT;
+        const int X = x0 + cc, Y = y0 + r;
+        if (X < g.nx && Y < g.ny) im[(size_t)Y * g.nx + X] = accs[(r + 1) * kAdjP + cc + 1];
+    }
+}
+
 // acc -> OSEM1 ratio (meas != nullptr) or raw projection, rows th = sub + k*step; clears acc.
 __global__ void fwd_finalize_kernel(double *__restrict__ acc, const float *__restrict__ meas,
                                     float *__restrict__ out, KGeom g, int sub, int step, int nrows)
@@ -383,6 +464,17 @@ int launch_fwd_tiled(const KGeom &g, const float2 *trig, const float *img, const
     int rc = launch_fwd_tiled_main(g, trig, img, acc, dN, sub, step, nrows, st);
     if (rc) return rc;
     return launch_fwd_finalize(g, meas, out, acc, dN, sub, step, nrows, st);
+}
+
+int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, cudaStream_t st)
+{
+    if (dN <= 0) return XCT_OK;
+    const int ntx = (g.nx + kAdjT - 1) / kAdjT, nty = (g.ny + kAdjT - 1) / kAdjT;
+    dim3 grid(ntx * nty, 1, dN);
+    adj_tiled_kernel<<<grid, kThreads, 0, st>>>(sino, img, trig, g, ntx);
+    g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+    XCT_CUDA_TRY(cudaGetLastError());
+    return XCT_OK;
 }
 
 int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const float *ratio, int dN, int sub,

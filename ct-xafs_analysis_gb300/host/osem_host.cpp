@@ -1,0 +1,202 @@
+// osem_host.cpp -- the OS-EM driver of the drop-in CT_reconstruction on libxct.
+//
+// Same structure as the reference (CT_reconstruction/GPU.cpp): a mode switch (GPU(),
+// :23-97) and, per device, a three-stage thread pipeline -- an input thread reads a batch of
+// dN sinograms and initial images (OSEM_input_thread, :483-510), a reconstruction thread runs
+// OS-EM on them (OSEM_thread, :408-476) and an output thread writes the slices (output_thread,
+// :99-123) -- fed round-robin with batches [N, N+dN-1] by the dispatcher of OSEM_ocl
+// (:562-663).  The OpenCL context/queue/program/image objects are replaced by one libxct
+// context and plan per device; the reconstruction thread calls xct_osem_run, which does the
+// host<->device copies and the whole subset/iteration loop on the device.
+#include <sys/stat.h>
+#include <time.h>
+
+#include <atomic>
+#include <iomanip>
+#include <iostream>
+#include <memory>
+#include <thread>
+
+#include "ct_reconstruction_gb300.hpp"
+
+namespace {
+
+struct DeviceSlot {
+    int device = 0;
+    int dN = 1;
+    xct_ctx *ctx = nullptr;
+    xct_plan *plan = nullptr;
+    std::thread input_th, reconst_th, output_th;
+};
+
+std::vector<int> g_sub;           // subset order (GPU.cpp:564-582)
+std::atomic<int> g_status{0};     // first failure (the reference exits on the spot)
+time_t g_t0 = 0;
+
+void fail(int code)
+{
+    int expected = 0;
+    g_status.compare_exchange_strong(expected, code);
+}
+
+void join(std::thread &t)
+{
+    if (t.joinable()) t.join();
+}
+
+// output_thread (GPU.cpp:99-123): write slices startN..endN, report, free the images.
+void output_thread(int startN, int endN, std::vector<float *> imgs, bool ok)
+{
+    const size_t n = (size_t)g_ox * g_oy;
+    if (ok)
+        for (int i = startN; i <= endN; ++i)
+            if (!write_data_output(g_d2, slice_name(g_f2, i), imgs[i - startN], n)) fail(XCT_E_IO);
+    time_t t1;
+    time(&t1);
+    for (int i = startN; i <= endN; ++i)
+        std::cout << "[Layer " << std::setfill('0') << std::setw(4) << i << "/" << g_st - 1 + g_num << "] "
+                  << (float)(t1 - g_t0) << " s elapsed" << (ok ? "" : " (failed)") << std::endl;
+    for (float *p : imgs) delete[] p;
+}
+
+// OSEM_thread (GPU.cpp:408-476): reconstruct the batch, hand the images to the output stage.
+void osem_thread(DeviceSlot *d, std::vector<float *> imgs, std::vector<float *> prjs, int startN, int endN)
+{
+    const int dN = endN - startN + 1;
+    const int rc = xct_osem_run(d->plan, dN, prjs.data(), imgs.data(), g_sub.data(), g_it);
+    if (rc != XCT_OK) {
+        std::cerr << "ERROR: " << xct_last_error() << " (" << rc << ")" << std::endl;
+        fail(rc);
+    }
+    join(d->output_th);
+    d->output_th = std::thread(output_thread, startN, endN, std::move(imgs), rc == XCT_OK);
+    for (float *p : prjs) delete[] p;
+}
+
+// OSEM_input_thread (GPU.cpp:483-510): read the batch, then chain the reconstruction.
+void osem_input_thread(DeviceSlot *d, int startN, int endN)
+{
+    std::vector<float *> prjs, imgs;
+    bool ok = true;
+    for (int i = startN; i <= endN; ++i) {
+        prjs.push_back(new float[(size_t)g_px * g_pa]);
+        imgs.push_back(new float[(size_t)g_ox * g_oy]);
+        ok = ok && read_data_input(g_d1, slice_name(g_f1, i), prjs.back(), (size_t)g_px * g_pa);
+        ok = ok && first_image(g_f4, imgs.back(), (size_t)g_ox * g_oy);
+    }
+    join(d->reconst_th);
+    if (!ok) {
+        fail(XCT_E_IO);
+        for (float *p : prjs) delete[] p;
+        for (float *p : imgs) delete[] p;
+        return;
+    }
+    d->reconst_th = std::thread(osem_thread, d, std::move(imgs), std::move(prjs), startN, endN);
+}
+
+}  // namespace
+
+// OSEM_ocl (GPU.cpp:562-663) on libxct: one context + plan per device, round-robin batches.
+int OSEM_gpu(const std::vector<int> &devices, const std::vector<float> &ang, int ss)
+{
+    if (devices.empty()) {
+        std::cerr << "ERROR: no usable CUDA device in the device list \"" << g_devList << "\"" << std::endl;
+        return XCT_E_INVALID;
+    }
+    g_sub.assign(ss, 0);
+    if (xct_subset_order(ss, g_sub.data()) != XCT_OK) {
+        std::cerr << "ERROR: " << xct_last_error() << std::endl;
+        return XCT_E_INVALID;
+    }
+    std::vector<std::unique_ptr<DeviceSlot>> slots;
+    for (int dev : devices) {
+        auto d = std::make_unique<DeviceSlot>();
+        d->device = dev;
+        d->dN = numParallel > 0 ? numParallel : 1;
+        if (xct_ctx_create(dev, &d->ctx) != XCT_OK) {
+            std::cerr << "ERROR: " << xct_last_error() << std::endl;
+            return XCT_E_UNSUPPORTED;
+        }
+        xct_geom g = {};
+        g.nx = g_nx;
+        g.ny = g_ny;
+        g.ox = g_ox;
+        g.oy = g_oy;
+        g.px = g_px;
+        g.pa = g_pa;
+        g.ss = ss;
+        g.it = g_it;
+        g.angles_deg = ang.data();
+        g.center_bin = -1.0f;
+        g.measured_fetch_mode = XCT_FETCH_EXACT;
+        g.subset_mode = XCT_SUBSETS_REF;
+        g.correction_mode = correctionMode;
+        g.max_batch = d->dN;
+        g.kernels = XCT_KERNELS_TILED;
+        if (xct_osem_plan_create(d->ctx, &g, &d->plan) != XCT_OK) {
+            std::cerr << "ERROR: " << xct_last_error() << std::endl;
+            xct_ctx_destroy(d->ctx);
+            return XCT_E_INVALID;
+        }
+        char name[256] = {0};
+        xct_device_name(dev, name, sizeof name);
+        std::cout << "Device No. " << dev + 1 << ": " << name << ", " << d->dN << " slices per call" << std::endl;
+        slots.push_back(std::move(d));
+    }
+    const int last = g_st + g_num - 1;
+    for (int N = g_st; N <= last;) {
+        for (auto &d : slots) {
+            join(d->input_th);
+            const int end = std::min(N + d->dN - 1, last);
+            d->input_th = std::thread(osem_input_thread, d.get(), N, end);
+            N = end + 1;
+            if (N > last) break;
+        }
+    }
+    for (auto &d : slots) join(d->input_th);
+    for (auto &d : slots) join(d->reconst_th);
+    for (auto &d : slots) join(d->output_th);
+    for (auto &d : slots) {
+        xct_osem_plan_destroy(d->plan);
+        xct_ctx_destroy(d->ctx);
+    }
+    return g_status.load();
+}
+
+// GPU() (GPU.cpp:23-97): the OS-EM-family modes of the reference.
+int GPU()
+{
+    if (g_ox != g_nx || g_oy != g_ny) {
+        std::cerr << "ERROR: an output size smaller than the reconstruction size is not supported" << std::endl;
+        return XCT_E_INVALID;
+    }
+    if (CSitBool) {
+        std::cerr << "ERROR: the compressed-sensing (FISTA) variant is not part of this build" << std::endl;
+        return XCT_E_UNSUPPORTED;
+    }
+    int ndev = 0;
+    if (xct_device_count(&ndev) != XCT_OK) {
+        std::cerr << "ERROR: " << xct_last_error() << std::endl;
+        return XCT_E_CUDA;
+    }
+    const std::vector<int> devices = parse_device_list(g_devList, ndev);
+    time(&g_t0);
+    switch (g_mode) {
+    case 2:
+        std::cout << "Processing by MART method" << std::endl << std::endl;
+        return OSEM_gpu(devices, g_ang, g_pa);  // OS-EM with ss = pa (GPU.cpp:51)
+    case 4:
+        std::cout << "Processing by MSIRT method" << std::endl << std::endl;
+        return OSEM_gpu(devices, g_ang, 1);
+    case 5:
+        std::cout << "Processing by ML-EM method" << std::endl << std::endl;
+        return OSEM_gpu(devices, g_ang, 1);
+    case 6:
+        std::cout << "Processing by OS-EM method" << std::endl << std::endl;
+        return OSEM_gpu(devices, g_ang, g_ss);
+    default:
+        std::cerr << "ERROR: reconstruction method " << g_mode
+                  << " is not part of this build (OS-EM family: 2, 4, 5, 6)" << std::endl;
+        return XCT_E_UNSUPPORTED;
+    }
+}

@@ -74,6 +74,7 @@ def lib():
             getattr(L, "xo_fista_bp" + sfx).argtypes = [p, p, p, p, gp, ctypes.c_int, r, r]
             getattr(L, "xo_bp_fbp" + sfx).argtypes = [p, p, gp, p]
             getattr(L, "xo_sino_correction" + sfx).argtypes = [p, p, fp, gp, ctypes.c_int]
+            getattr(L, "xo_adjoint" + sfx).argtypes = [p, p, gp, p]
             getattr(L, "xo_osem_run" + sfx).argtypes = [p, p, p, gp, ip, ctypes.c_int, ctypes.c_int]
         L.xo_trig_f32.argtypes = [fp, ctypes.c_int, fp]
         L.xo_trig_f64.argtypes = [fp, ctypes.c_int, dp]
@@ -190,6 +191,17 @@ def bp_fbp(fprj, angles_deg, nx, ny, cx=None, dtype=np.float32):
     cs = trig(angles_deg, dtype)
     out = np.empty((ny, nx), dtype=dtype)
     getattr(lib(), "xo_bp_fbp" + _sfx(dtype))(_p(fprj), _p(cs), ctypes.byref(g), _p(out))
+    return out
+
+
+def adjoint(sino, angles_deg, nx, ny, cx=None, dtype=np.float32):
+    """Exact adjoint A^T of projection() over all angles."""
+    sino = np.ascontiguousarray(sino, dtype=dtype)
+    pa, px = sino.shape
+    g = make_geom(nx, ny, px, pa, 1, cx, ORDER_CANONICAL)
+    cs = trig(angles_deg, dtype)
+    out = np.empty((ny, nx), dtype=dtype)
+    getattr(lib(), "xo_adjoint" + _sfx(dtype))(_p(sino), _p(cs), ctypes.byref(g), _p(out))
     return out
 
 

@@ -47,6 +47,7 @@ int xo_abi_version(void);
                         T alpha, T L);                                                                  \
     void xo_bp_fbp##S(const T *fprj, const T *cs, const xo_geom *g, T *dst);                               \
     void xo_sino_correction##S(const T *src, T *dst, const float *ang_deg, const xo_geom *g, int mode);    \
+    void xo_adjoint##S(const T *sino, const T *cs, const xo_geom *g, T *img);                               \
     void xo_osem_run##S(T *img, const T *meas, const T *cs, const xo_geom *g, const int *sub_order, int it, \
                         int cover);
 

@@ -136,6 +136,38 @@ void FN(xo_projection)(const REAL *img, const REAL *cs, const xo_geom *g, int su
         }
 }
 
+/* Exact adjoint A^T of xo_projection over all angles (no counterpart in the reference,
+ * whose backprojectors are pixel-driven nearest/linear rules): every sample of every ray
+ * scatters sino[th][X] with its bilinear weights (1-a)(1-b), a(1-b), (1-a)b, ab onto its
+ * 2x2 footprint (texels outside the image dropped).  Sequential, single thread. */
+void FN(xo_adjoint)(const REAL *sino, const REAL *cs, const xo_geom *g, REAL *img)
+{
+    const int D = g->depth, nx = g->nx, ny = g->ny;
+    const REAL hx = (REAL)nx * (REAL)0.5, hy = (REAL)ny * (REAL)0.5, hd = (REAL)D * (REAL)0.5;
+    memset(img, 0, sizeof(REAL) * (size_t)nx * ny);
+    for (int th = 0; th < g->pa; ++th) {
+        const REAL c = cs[2 * th], s = cs[2 * th + 1];
+        for (int X = 0; X < g->px; ++X) {
+            const REAL v = sino[(size_t)th * g->px + X];
+            if (v == (REAL)0) continue;
+            const REAL Xc = (REAL)X - (REAL)g->cx;
+            const REAL ax = XO_FMA(Xc, c, hx), ay = XO_FMA(Xc, -s, hy);
+            for (int Y = 0; Y < D; ++Y) {
+                const REAL Yc = (REAL)Y - hd;
+                const REAL x = XO_FMA(Yc, s, ax), y = XO_FMA(Yc, c, ay);
+                const REAL fi = XO_FLOOR(x), fj = XO_FLOOR(y);
+                const REAL a = x - fi, b = y - fj;
+                const int i = (int)fi, j = (int)fj;
+                const REAL w[4] = {((REAL)1 - a) * ((REAL)1 - b), a * ((REAL)1 - b), ((REAL)1 - a) * b, a * b};
+                const int ii[4] = {i, i + 1, i, i + 1}, jj[4] = {j, j, j + 1, j + 1};
+                for (int q = 0; q < 4; ++q)
+                    if (ii[q] >= 0 && jj[q] >= 0 && ii[q] < nx && jj[q] < ny)
+                        img[(size_t)jj[q] * nx + ii[q]] += w[q] * v;
+            }
+        }
+    }
+}
+
 /* OSEM1 (OSEM.cl:38-68): forward-project subset rows and write the measured/estimated
  * ratio r = (prj < 1e-4) ? m : m / prj with m = max(1e-6, y), NaN -> 1e-6. */
 void FN(xo_osem1)(const REAL *img, const REAL *meas, const REAL *cs, const xo_geom *g, int sub, int nrows,

@@ -1,0 +1,96 @@
+"""The C++ drop-in program xct_ct_reconstruction: the reference's .inp keys, file formats and
+slice naming (CPU), and an end-to-end reconstruction from files (GPU)."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def host_bin(xct_lib):
+    from xct import build
+    return build.build_host()
+
+
+# an .inp as the reference reads it: key lines, values on the next line (CRLF on some)
+INP_KEYS = [
+    ("#Open CL Platform & Device No", "1"),
+    ("#Number of Parallel processing per one device", "4"),
+    ("#測定ファイルディレクトリパス", "{d1}"),
+    ("#測定ファイル名", "s****.raw"),
+    ("#出力ファイルディレクトリパス", "{d2}"),
+    ("#出力ファイル名", "rec_****.img"),
+    ("#ログファイルパス", "{f3}"),
+    ("#レイヤー数", "3"),
+    ("#開始ナンバー", "7"),
+    ("#初期画像の使用 1:Yes 2: No", "2"),
+    ("#カメラピクセル数", "{px}"),
+    ("#投影数", "{pa}"),
+    ("#再構成画像サイズ", "{n}"),
+    ("#再構成法", "6"),
+    ("#反復回数", "{it}"),
+    ("#サブセット(OSEM)", "{ss}"),
+    ("#投影像補正 0:なし 1: x方向のみ 2:θ方向のみ 3:x,θ方向両方", "0"),
+]
+
+
+def write_inp(path, **kw):
+    with open(path, "wb") as f:
+        for i, (k, v) in enumerate(INP_KEYS):
+            eol = b"\r\n" if i % 3 == 0 else b"\n"
+            f.write(k.encode("utf-8") + eol + v.format(**kw).encode("utf-8") + eol)
+
+
+def test_inp_keys_parse_like_the_reference(host_bin, tmp_path):
+    p = tmp_path / "a.inp"
+    write_inp(p, d1="in dir", d2="out", f3="angles.log", px=96, pa=60, n=80, it=3, ss=5)
+    out = subprocess.run([host_bin, "--print-params", str(p)], capture_output=True, text=True, check=True)
+    prm = json.loads(out.stdout.strip().splitlines()[-1])
+    assert prm["devList"] == "1" and prm["numParallel"] == 4
+    assert prm["d1"] == "in dir" and prm["d2"] == "out" and prm["f3"] == "angles.log"
+    assert (prm["num"], prm["st"], prm["fst"]) == (3, 7, 2)
+    assert (prm["px"], prm["pa"], prm["nx"], prm["ny"], prm["ox"], prm["oy"]) == (96, 60, 80, 80, 80, 80)
+    assert (prm["mode"], prm["it"], prm["ss"], prm["correctionMode"]) == (6, 3, 5, 0)
+    # untouched keys keep the reference's defaults (main.cpp:12-47)
+    assert prm["zp"] == 4096 and prm["CSitBool"] is False and prm["f4"] == "1st.img"
+    # <base>####<tail> naming (GPU.cpp:27-34, :497)
+    assert prm["first_input"] == "s0007.raw" and prm["first_output"] == "rec_0007.img"
+
+
+@pytest.mark.parametrize("lst,n,want", [("1", 1, "0"), ("1,2-4", 8, "0,1,2,3"), ("2", 1, ""),
+                                        ("1-3,5", 6, "0,1,2,4"), ("3,1", 4, "0,2")])
+def test_device_list_syntax(host_bin, lst, n, want):
+    out = subprocess.run([host_bin, "--devlist", lst, str(n)], capture_output=True, text=True, check=True)
+    assert out.stdout.strip() == want
+
+
+@pytest.mark.gpu
+def test_end_to_end_reconstruction_from_files(host_bin, oracle_lib, tmp_path):
+    from xct import phantom as P
+    O = oracle_lib
+    n, px, pa, ss, it = 80, 96, 60, 5, 3
+    ang = P.uniform_angles(pa)
+    d1, d2 = tmp_path / "in", tmp_path / "out"
+    d1.mkdir()
+    with open(tmp_path / "angles.log", "w") as f:
+        for a in ang:
+            f.write("%.9g\t0.0\n" % a)  # first token per line (fileIO.cpp:11-23)
+    meas = {}
+    for z in range(7, 10):
+        img = P.rasterize_ellipses(P.ellipse_params(n, 5, z, axes=(3, 20)), n, n)
+        meas[z] = P.noisy_log_sinogram(O.projection(img, ang, px), 1e5, z)
+        meas[z].astype(np.float32).tofile(d1 / ("s%04d.raw" % z))
+    inp = tmp_path / "run.inp"
+    write_inp(inp, d1=str(d1), d2=str(d2), f3=str(tmp_path / "angles.log"), px=px, pa=pa, n=n, it=it, ss=ss)
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    x0 = np.ones((n, n), np.float32)
+    for z in range(7, 10):
+        got = np.fromfile(d2 / ("rec_%04d.img" % z), np.float32).reshape(n, n)
+        ref = O.osem_run(x0, meas[z], ang, ss, it, order=O.ORDER_LITERAL)
+        rel = np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)
+        assert rel <= 1e-4, (z, rel)

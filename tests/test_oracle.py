@@ -209,3 +209,16 @@ def test_sino_correction_bit_identical_to_reference_kernel(oracle_lib, mode):
     meas = np.random.default_rng(mode).uniform(0, 3, (pa, px)).astype(np.float32)
     ref = O.RefKernels(48, 40, px, pa, 4)
     assert np.array_equal(ref.sino_correction(meas, ang, mode), O.sino_correction(meas, ang, mode))
+
+
+def test_oracle_adjoint_dot_product_identity_f64(oracle_lib):
+    O = oracle_lib
+    rng = np.random.default_rng(12)
+    n, px, pa = 40, 52, 33
+    ang = np.sort(rng.uniform(0, 180, pa)).astype(np.float32)
+    x = rng.uniform(0, 1, (n, n))
+    y = rng.uniform(0, 1, (pa, px))
+    ax = O.projection(x, ang, px, dtype=np.float64)
+    aty = O.adjoint(y, ang, n, n, dtype=np.float64)
+    lhs, rhs = float(np.sum(ax * y)), float(np.sum(x * aty))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
