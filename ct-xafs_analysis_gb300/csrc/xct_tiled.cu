@@ -7,9 +7,11 @@
 //     It stages the tile ONCE per subset in shared memory as (t, t[x+1] - t) pairs, so
 //     the x-lerp of a bilinear sample is one FMA and its 2x2 footprint is two 64-bit
 //     loads, and serves every angle of its angle chunk from there;
-//   * a warp takes one angle and 32 consecutive rays; each lane finds the exact interval of
-//     sample indices Y whose base texel lies in the tile (the coordinates are monotone in
-//     Y), then sums those samples with packed f32x2 coordinate/floor/fraction arithmetic;
+//   * a warp takes one angle and 8 consecutive rays, 4 lanes per ray; the exact interval of
+//     sample indices Y whose base texel lies in the tile (the coordinates are monotone in Y)
+//     comes from four boundary searches, one per lane of the ray's group; the 4 lanes then
+//     take every 4th sample of the interval, with packed f32x2 coordinate/floor/fraction
+//     arithmetic, and their partial sums are combined with two shuffles;
 //   * per-tile partial ray sums go into a double-precision accumulator with one atomic per
 //     ray and tile.
 // A finalize kernel turns the accumulator into the OSEM1 ratio (or the raw projection)
@@ -30,11 +32,23 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+// forward projector: 12 warps per CTA so that 3 CTAs (3 x 69 KB of shared memory) give 36
+// resident warps per SM to hide the shared-memory load latency
+constexpr int kFwdThreads = 384;
+constexpr int kFwdWarps = kFwdThreads / 32;
 constexpr int kAngChunk = 128;  // angles per CTA (forward) / per staging pass (back)
 
-constexpr int kFwdT = 96;             // owned base texels per tile side
-constexpr int kFwdP = kFwdT + 1;      // element pitch (odd: spreads 64-bit banks)
+// A warp works on 8 consecutive rays of one angle with 4 lanes per ray, the 4 lanes taking
+// every 4th sample (lane k: samples ya+k, ya+k+4, ...).  A half-warp then reads a compact
+// 4x4 patch of footprints, and with an element pitch of 4 (mod 8) most such patches fall in
+// distinct 64-bit bank pairs; 8 neighbouring rays also have similar lengths inside a tile,
+// so few lanes idle.  (A CPU model of the access pattern: 0.232 shared wavefronts and 90 %
+// active lanes per sample, against 0.293 and 73 % for one lane per ray with an odd pitch.)
+constexpr int kFwdT = 92;             // owned base texels per tile side
+constexpr int kFwdP = kFwdT;          // element pitch: 92 = 4 (mod 8)
 constexpr int kFwdRows = kFwdT + 1;   // a base row r reads element rows r and r+1
+constexpr int kLanesPerRay = 4;
+constexpr int kRaysPerWarp = 32 / kLanesPerRay;
 constexpr size_t kFwdSmem = (size_t)kFwdP * kFwdRows * sizeof(float2) + kAngChunk * sizeof(float2);
 
 constexpr int kBpTX = 64, kBpTY = 32;  // backprojection tile (pixels)
@@ -113,8 +127,29 @@ __device__ __forceinline__ float lds_f1(unsigned addr)
 }
 
 // ----------------------------------------------------------------- forward projector
+// One bilinear sample at Yc (both halves of yc2): coordinates (fma(Yc,s,ax), fma(Yc,c,ay)),
+// floor as a round-down add of 1.5*2^23 (the low mantissa bits), fraction = coordinate -
+// floor, the footprint as two 64-bit loads of (t, t[x+1] - t), three FMA lerps.
+__device__ __forceinline__ float fwd_sample(f2x yc2, f2x sc, f2x axy, f2x MM, unsigned base2)
+{
+    const f2x xy = f2_fma(yc2, sc, axy);
+    const f2x tb = f2_add_rd(xy, MM);
+    const f2x fr = f2_sub(xy, f2_sub(tb, MM));
+    int ixb, iyb;
+    f2_unpack_bits(tb, ixb, iyb);
+    float fx, fy;
+    f2_unpack(fr, fx, fy);
+    const unsigned addr = (unsigned)iyb * (unsigned)(kFwdP * 8) + (unsigned)ixb * 8u + base2;
+    float t00, d0, t01, d1;
+    lds_f2(addr, t00, d0);
+    lds_f2_next_row(addr, t01, d1);
+    const float r0 = fmaf(fx, d0, t00);
+    const float r1 = fmaf(fx, d1, t01);
+    return fmaf(fy, r1 - r0, r0);
+}
+
 // grid: (ntx*nty tiles, angle chunks, dN).  acc: [dN][nrows][px] doubles.
-__global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__restrict__ img,
+__global__ void __launch_bounds__(kFwdThreads, 3) fwd_tiled_kernel(const float *__restrict__ img,
                                                              double *__restrict__ acc,
                                                              const float2 *__restrict__ trig, KGeom g, int sub,
                                                              int step, int nrows, int ntx)
@@ -131,7 +166,7 @@ __global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__rest
     const float *im = img + (size_t)z * g.nx * g.ny;
 
     // element (c, r) = (t(x0+c, y0+r), t(x0+c+1, y0+r) - t(x0+c, y0+r)), zero border
-    for (int i = threadIdx.x; i < kFwdT * kFwdRows; i += kThreads) {
+    for (int i = threadIdx.x; i < kFwdT * kFwdRows; i += kFwdThreads) {
         const int r = i / kFwdT, c = i - r * kFwdT;
         const int gx = x0 + c, gy = y0 + r;
         float t0 = 0.0f, t1 = 0.0f;
@@ -142,7 +177,7 @@ __global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__rest
         }
         tile[r * kFwdP + c] = make_float2(t0, t1 - t0);
     }
-    for (int k = threadIdx.x; k < kn; k += kThreads) scs[k] = trig[sub + (k0 + k) * step];
+    for (int k = threadIdx.x; k < kn; k += kFwdThreads) scs[k] = trig[sub + (k0 + k) * step];
     __syncthreads();
 
     // owned base-texel ranges (the union over tiles is [-1, n-1])
@@ -156,9 +191,15 @@ __global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__rest
     const unsigned bias = (unsigned)XCT_FLOOR_BIAS;
     const unsigned base2 = sbase - (((bias + (unsigned)y0) * (unsigned)kFwdP + bias + (unsigned)x0) * 8u);
     const f2x MM = f2_pack(kMagic, kMagic);
-    const f2x one2 = f2_pack(1.0f, 1.0f);
+    const f2x step2 = f2_pack((float)kLanesPerRay, (float)kLanesPerRay);
+    const int ray = lane / kLanesPerRay;  // ray within the warp's 8
+    const int ph = lane % kLanesPerRay;   // sample phase of this lane
+    const int grp = lane & ~(kLanesPerRay - 1);
+    // lane phase 0/1 bound the x coordinate, 2/3 the y coordinate (lower / upper Y limit)
+    const bool bound_x = ph < 2;
+    const bool upper = (ph & 1) != 0;
 
-    for (int k = warp; k < kn; k += kWarps) {
+    for (int k = warp; k < kn; k += kFwdWarps) {
         const float c = scs[k].x, s = scs[k].y;
         const float inv_s = 1.0f / s, inv_c = 1.0f / c;
         // rays that can reach the tile: project the (expanded) tile corners on the
@@ -175,43 +216,48 @@ __global__ void __launch_bounds__(kThreads) fwd_tiled_kernel(const float *__rest
         const int Xlo = max(0, (int)floorf(pmin) - 1);
         const int Xhi = min(g.px - 1, (int)ceilf(pmax) + 1);
         const f2x sc = f2_pack(s, c);
-        for (int base = Xlo; base <= Xhi; base += 32) {
-            const int X = base + lane;
-            int ya = 0, yb = 0;
-            float ax = 0.0f, ay = 0.0f;
-            if (X <= Xhi) {
-                const float Xc = (float)X - g.cx;
-                ax = fmaf(Xc, c, g.hx);
-                ay = fmaf(Xc, -s, g.hy);
-                int a0, a1, b0, b1;
-                coord_range(xlo, xhi, ax, s, inv_s, g.hd, D, a0, a1);
-                coord_range(ylo, yhi, ay, c, inv_c, g.hd, D, b0, b1);
-                ya = max(a0, b0);
-                yb = min(a1, b1);
+        for (int base = Xlo; base <= Xhi; base += kRaysPerWarp) {
+            const int X = base + ray;
+            const bool live = X <= Xhi;
+            const float Xc = (float)X - g.cx;
+            const float ax = fmaf(Xc, c, g.hx);
+            const float ay = fmaf(Xc, -s, g.hy);
+            // the four interval limits of this ray, one per lane of its group: the lower (even
+            // phase) or upper (odd phase) Y limit from the x (phase 0/1) or y (2/3) coordinate
+            int v = 0;
+            if (live) {
+                const float a = bound_x ? ax : ay, sl = bound_x ? s : c, isl = bound_x ? inv_s : inv_c;
+                const float lo = bound_x ? xlo : ylo, hi = bound_x ? xhi : yhi;
+                if (sl != 0.0f) {
+                    // sl > 0: [first(u >= lo), first(u >= hi)); sl < 0: [first(u < hi), first(u < lo))
+                    const float b = ((sl > 0.0f) != upper) ? lo : hi;
+                    v = first_true(b, a, sl, isl, g.hd, D);
+                } else {  // constant coordinate: all samples or none
+                    v = upper ? ((a >= lo && a < hi) ? D : 0) : 0;
+                }
             }
-            const int n = yb - ya;
-            const float yc0 = (float)ya - g.hd;
+            const int v0 = __shfl_sync(0xffffffffu, v, grp + 0), v1 = __shfl_sync(0xffffffffu, v, grp + 1);
+            const int v2 = __shfl_sync(0xffffffffu, v, grp + 2), v3 = __shfl_sync(0xffffffffu, v, grp + 3);
+            const int ya = max(v0, v2), yb = min(v1, v3);
+            const int n = yb - ya > ph ? (yb - ya - ph + kLanesPerRay - 1) / kLanesPerRay : 0;
+            const float yc0 = (float)(ya + ph) - g.hd;
             f2x yc2 = f2_pack(yc0, yc0);
             const f2x axy = f2_pack(ax, ay);
-            float sum = 0.0f;
-            for (int i = 0; i < n; ++i) {
-                const f2x xy = f2_fma(yc2, sc, axy);       // (fma(Yc,s,ax), fma(Yc,c,ay))
-                const f2x tb = f2_add_rd(xy, MM);          // floor in the low mantissa bits
-                const f2x fr = f2_sub(xy, f2_sub(tb, MM)); // (fx, fy) = (x, y) - floor
-                int ixb, iyb;
-                f2_unpack_bits(tb, ixb, iyb);
-                float fx, fy;
-                f2_unpack(fr, fx, fy);
-                const unsigned addr = (unsigned)iyb * (unsigned)(kFwdP * 8) + (unsigned)ixb * 8u + base2;
-                float t00, d0, t01, d1;
-                lds_f2(addr, t00, d0);
-                lds_f2_next_row(addr, t01, d1);
-                const float r0 = fmaf(fx, d0, t00);
-                const float r1 = fmaf(fx, d1, t01);
-                sum += fmaf(fy, r1 - r0, r0);
-                yc2 = f2_add(yc2, one2);
+            // two samples per iteration into two accumulators (independent load/FMA chains)
+            float sum = 0.0f, sum_b = 0.0f;
+            int i = 0;
+            for (; i + 1 < n; i += 2) {
+                const f2x yb2 = f2_add(yc2, step2);
+                sum += fwd_sample(yc2, sc, axy, MM, base2);
+                sum_b += fwd_sample(yb2, sc, axy, MM, base2);
+                yc2 = f2_add(yb2, step2);
             }
-            if (n > 0) atomicAdd(acc + ((size_t)z * nrows + k0 + k) * g.px + X, (double)sum);
+            if (i < n) sum += fwd_sample(yc2, sc, axy, MM, base2);
+            sum += sum_b;
+            // the ray's partial sum over this tile: the 4 phases, then one atomic
+            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+            sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+            if (ph == 0 && live && yb > ya) atomicAdd(acc + ((size_t)z * nrows + k0 + k) * g.px + X, (double)sum);
         }
     }
 }
@@ -441,7 +487,7 @@ int launch_fwd_tiled_main(const KGeom &g, const float2 *trig, const float *img, 
     int ntx;
     int rc = fwd_grid(g, nrows, dN, grid, ntx);
     if (rc) return rc;
-    fwd_tiled_kernel<<<grid, kThreads, kFwdSmem, st>>>(img, acc, trig, g, sub, step, nrows, ntx);
+    fwd_tiled_kernel<<<grid, kFwdThreads, kFwdSmem, st>>>(img, acc, trig, g, sub, step, nrows, ntx);
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;
