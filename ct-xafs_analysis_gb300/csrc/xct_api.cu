@@ -516,3 +516,6 @@ int xct_plan_last_ms(xct_plan *p, float *ms)
 }
 
 }  // extern "C"
+
+// geometry validation shared with the batched plans (xct_batch.cu)
+int xct_check_geom(const xct_geom *g) { return check_geom(g); }

@@ -1,0 +1,214 @@
+// xct_batch.cu -- OS-EM over many slices of different shapes in one graph of persistent
+// launches (CT-XAFS stacks: energies x slices, every slice its own width, bin count and
+// angle list).
+//
+// The reference reconstructs a batch of dN slices of ONE shape per OSEM_execution call
+// (GPU.cpp:125-240).  A batch plan instead holds n slices of any shapes that share the
+// subset count; every subset step is three persistent launches -- forward projection,
+// ratio, backprojection+update -- whose CTAs take (slice, tile) work units from a device
+// queue, so small slices fill the GPU together with large ones.  The whole subset/iteration
+// loop is captured once in a CUDA graph and replayed; the slices' buffer pointers live in a
+// device descriptor table written before each replay, so one plan serves any buffers of
+// the planned shapes.
+#include <math.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "xct_internal.h"
+
+struct xct_batch_plan {
+    xct_ctx *ctx = nullptr;
+    int n = 0, ss = 0, it = 0;
+    std::vector<int> sub;             // subset order (GPU.cpp:564-582)
+    std::vector<XctItemDev> host;     // descriptors (pointers filled per run)
+    XctItemDev *d_items = nullptr;
+    int *d_bases = nullptr;           // [3][n+1]
+    int *d_queues = nullptr;          // [it*ss][3]
+    float2 *d_trig = nullptr;
+    float *d_ratio = nullptr;
+    double *d_acc = nullptr;
+    int grids[3] = {0, 0, 0};
+    cudaStream_t cap = nullptr;       // capture stream
+    cudaGraphExec_t exec = nullptr;
+    size_t queue_bytes = 0;
+};
+
+static void batch_free(xct_batch_plan *p)
+{
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->cap) cudaStreamDestroy(p->cap);
+    cudaFree(p->d_items);
+    cudaFree(p->d_bases);
+    cudaFree(p->d_queues);
+    cudaFree(p->d_trig);
+    cudaFree(p->d_ratio);
+    cudaFree(p->d_acc);
+    delete p;
+}
+
+extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms, int it, xct_batch_plan **out)
+{
+    if (!ctx || !out || !geoms || n <= 0) return xct_fail(XCT_E_INVALID, "xct_batch_plan_create: bad arguments");
+    *out = nullptr;
+    if (it < 0) return xct_fail(XCT_E_INVALID, "xct_batch_plan_create: iterations must be >= 0");
+    const int ss = geoms[0].ss;
+    for (int i = 0; i < n; ++i) {
+        int rc = xct_check_geom(&geoms[i]);
+        if (rc) return rc;
+        if (geoms[i].ss != ss)
+            return xct_fail(XCT_E_INVALID, "xct_batch_plan_create: every slice of a batch needs the same subset count");
+        if (geoms[i].correction_mode != 0)
+            return xct_fail(XCT_E_UNSUPPORTED, "xct_batch_plan_create: sinogram correction is not available in batches");
+    }
+    XCT_CUDA_TRY(cudaSetDevice(ctx->device));
+    xct_batch_plan *p = new (std::nothrow) xct_batch_plan();
+    if (!p) return xct_fail(XCT_E_NOMEM, "xct_batch_plan_create: host allocation failed");
+    p->ctx = ctx;
+    p->n = n;
+    p->ss = ss;
+    p->it = it;
+    p->sub.resize(ss);
+    xct_subset_order_host(ss, p->sub.data());
+    auto fail = [&](cudaError_t e, const char *what) {
+        int r = xct_cuda_fail(e, what);
+        batch_free(p);
+        return r;
+    };
+    // sizes and unit tables
+    std::vector<int> bases(3 * (size_t)(n + 1), 0);
+    size_t n_trig = 0, n_ratio = 0, n_acc = 0;
+    p->host.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const xct_geom &g = geoms[i];
+        XctItemDev &d = p->host[i];
+        KGeom &k = d.g;
+        k.nx = g.nx;
+        k.ny = g.ny;
+        k.px = g.px;
+        k.pa = g.pa;
+        k.ss = g.ss;
+        k.depth = std::max(g.nx, g.ny);
+        k.hx = (float)g.nx * 0.5f;
+        k.hy = (float)g.ny * 0.5f;
+        k.hd = (float)k.depth * 0.5f;
+        k.cx = g.center_bin < 0.0f ? (float)g.px * 0.5f : g.center_bin;
+        k.fetch = g.measured_fetch_mode;
+        d.cover = g.subset_mode == XCT_SUBSETS_COVER;
+        int fu, fin, bu;
+        xct_batched_units(k, d.fwd_ntx, d.fwd_nty, fu, fin, d.bp_ntx, bu);
+        bases[0 * (n + 1) + i + 1] = bases[0 * (n + 1) + i] + fu;
+        bases[1 * (n + 1) + i + 1] = bases[1 * (n + 1) + i] + fin;
+        bases[2 * (n + 1) + i + 1] = bases[2 * (n + 1) + i] + bu;
+        n_trig += g.pa;
+        n_ratio += (size_t)g.pa * g.px;
+        n_acc += (size_t)((g.pa + g.ss - 1) / g.ss) * g.px;
+    }
+    cudaError_t e;
+    if ((e = cudaMalloc(&p->d_items, sizeof(XctItemDev) * n)) != cudaSuccess) return fail(e, "cudaMalloc items");
+    if ((e = cudaMalloc(&p->d_bases, sizeof(int) * bases.size())) != cudaSuccess) return fail(e, "cudaMalloc bases");
+    p->queue_bytes = sizeof(int) * 3 * (size_t)std::max(1, it * ss);
+    if ((e = cudaMalloc(&p->d_queues, p->queue_bytes)) != cudaSuccess) return fail(e, "cudaMalloc queues");
+    if ((e = cudaMalloc(&p->d_trig, sizeof(float2) * n_trig)) != cudaSuccess) return fail(e, "cudaMalloc trig");
+    if ((e = cudaMalloc(&p->d_ratio, sizeof(float) * n_ratio)) != cudaSuccess) return fail(e, "cudaMalloc ratio");
+    if ((e = cudaMalloc(&p->d_acc, sizeof(double) * n_acc)) != cudaSuccess) return fail(e, "cudaMalloc acc");
+    // ratio rows OSEM1 never writes read as 0 and stay 0; the accumulator starts at 0 and the
+    // finalize kernel clears what it reads
+    if ((e = cudaMemset(p->d_ratio, 0, sizeof(float) * n_ratio)) != cudaSuccess) return fail(e, "memset ratio");
+    if ((e = cudaMemset(p->d_acc, 0, sizeof(double) * n_acc)) != cudaSuccess) return fail(e, "memset acc");
+    size_t ot = 0, orat = 0, oacc = 0;
+    std::vector<float2> cs;
+    for (int i = 0; i < n; ++i) {
+        const xct_geom &g = geoms[i];
+        XctItemDev &d = p->host[i];
+        xct_trig_table(g.angles_deg, g.pa, cs);
+        if ((e = cudaMemcpy(p->d_trig + ot, cs.data(), sizeof(float2) * g.pa, cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "upload trig");
+        d.trig = p->d_trig + ot;
+        d.ratio = p->d_ratio + orat;
+        d.acc = p->d_acc + oacc;
+        d.sino = nullptr;
+        d.img = nullptr;
+        ot += g.pa;
+        orat += (size_t)g.pa * g.px;
+        oacc += (size_t)((g.pa + g.ss - 1) / g.ss) * g.px;
+    }
+    if ((e = cudaMemcpy(p->d_bases, bases.data(), sizeof(int) * bases.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e, "upload bases");
+    int rc = xct_batched_grids(ctx->device, ctx->sm_count, p->grids);
+    if (rc) {
+        batch_free(p);
+        return rc;
+    }
+    if ((e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+    *out = p;
+    return XCT_OK;
+}
+
+extern "C" int xct_batch_plan_destroy(xct_batch_plan *p)
+{
+    if (p) cudaSetDevice(p->ctx->device);
+    batch_free(p);
+    return XCT_OK;
+}
+
+// Capture the whole loop: clear the queue counters, then it x ss subset steps.
+static int capture(xct_batch_plan *p)
+{
+    cudaGraph_t graph = nullptr;
+    XCT_CUDA_TRY(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+    int rc = XCT_OK;
+    cudaError_t e = cudaMemsetAsync(p->d_queues, 0, p->queue_bytes, p->cap);
+    if (e != cudaSuccess) rc = xct_cuda_fail(e, "capture memset");
+    for (int i = 0; i < p->it && rc == XCT_OK; ++i)
+        for (int k = 0; k < p->ss && rc == XCT_OK; ++k)
+            rc = launch_osem_step_batched(p->d_items, p->d_bases, p->n, p->sub[k],
+                                          p->d_queues + 3 * (size_t)(i * p->ss + k), p->grids, p->cap);
+    e = cudaStreamEndCapture(p->cap, &graph);
+    if (rc == XCT_OK && e != cudaSuccess) rc = xct_cuda_fail(e, "cudaStreamEndCapture");
+    if (rc == XCT_OK) {
+        e = cudaGraphInstantiate(&p->exec, graph, 0);
+        if (e != cudaSuccess) rc = xct_cuda_fail(e, "cudaGraphInstantiate");
+    }
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+}
+
+extern "C" int xct_batch_run(xct_batch_plan *p, const float *const *d_sino, float *const *d_img, void *stream)
+{
+    if (!p || !d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_batch_run: null argument");
+    for (int i = 0; i < p->n; ++i)
+        if (!d_sino[i] || !d_img[i]) return xct_fail(XCT_E_INVALID, "xct_batch_run: null slice pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    if (!p->exec) {
+        int rc = capture(p);
+        if (rc) return rc;
+    }
+    for (int i = 0; i < p->n; ++i) {
+        p->host[i].sino = d_sino[i];
+        p->host[i].img = d_img[i];
+    }
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
+    XCT_CUDA_TRY(cudaMemcpyAsync(p->d_items, p->host.data(), sizeof(XctItemDev) * p->n, cudaMemcpyHostToDevice, st));
+    XCT_CUDA_TRY(cudaGraphLaunch(p->exec, st));
+    g_xct_launches.fetch_add((long long)3 * p->it * p->ss, std::memory_order_relaxed);
+    return XCT_OK;
+}
+
+extern "C" int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, const float *const *d_sino,
+                                    float *const *d_img, int it, void *stream)
+{
+    xct_batch_plan *p = nullptr;
+    int rc = xct_batch_plan_create(ctx, n, geoms, it, &p);
+    if (rc) return rc;
+    rc = xct_batch_run(p, d_sino, d_img, stream);
+    if (rc == XCT_OK) {
+        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+        if (e != cudaSuccess) rc = xct_cuda_fail(e, "xct_osem_run_batched: sync");
+    }
+    xct_batch_plan_destroy(p);
+    return rc;
+}

@@ -21,6 +21,18 @@ struct KGeom {
     int fetch;       // XCT_FETCH_*
 };
 
+// One slice of a batched launch (device-side descriptor).
+struct XctItemDev {
+    KGeom g;
+    const float *sino;   // measured sinogram [pa][px]
+    float *img;          // image [ny][nx], updated in place
+    float *ratio;        // ratio image [pa][px] (rows never written stay 0)
+    double *acc;         // ray-sum accumulator [ceil(pa/ss)][px] (kept zeroed between subsets)
+    const float2 *trig;  // (cos, sin) [pa]
+    int cover;           // XCT_SUBSETS_COVER
+    int fwd_ntx, fwd_nty, bp_ntx;
+};
+
 struct xct_ctx {
     int device;
     int sm_count;
@@ -88,6 +100,15 @@ int launch_fwd_finalize(const KGeom &g, const float *meas, float *out, double *a
 // Tiled OSEM2 backprojection + update, in place (same contract as the plain one).
 int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const float *ratio, int dN, int sub,
                            cudaStream_t st);
+// Batched launches (xct_tiled.cu): work units of one slice, persistent grid sizes, and one
+// subset step (forward, finalize, backprojection) over all slices; bases is [3][n+1]
+// prefix sums of the units of each kernel, queues 3 zeroed counters.
+void xct_batched_units(const KGeom &g, int &fwd_ntx, int &fwd_nty, int &fwd_units, int &fin_units, int &bp_ntx,
+                       int &bp_units);
+int xct_batched_grids(int device, int sm_count, int grids[3]);
+int launch_osem_step_batched(const XctItemDev *items, const int *bases, int n, int sub, int *queues,
+                             const int grids[3], cudaStream_t st);
+int xct_check_geom(const xct_geom *g);
 // Exact adjoint of the forward projector over all angles: img = A^T sino (overwrites img).
 int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, cudaStream_t st);
 // sinogramCorrection (reconstShare.cl:35-70), modes 1..4, src -> dst.

@@ -148,22 +148,17 @@ __device__ __forceinline__ float fwd_sample(f2x yc2, f2x sc, f2x axy, f2x MM, un
     return fmaf(fy, r1 - r0, r0);
 }
 
-// grid: (ntx*nty tiles, angle chunks, dN).  acc: [dN][nrows][px] doubles.
-__global__ void __launch_bounds__(kFwdThreads, 3) fwd_tiled_kernel(const float *__restrict__ img,
-                                                             double *__restrict__ acc,
-                                                             const float2 *__restrict__ trig, KGeom g, int sub,
-                                                             int step, int nrows, int ntx)
+// The work of one CTA: tile (bx, by) of one slice (image im, accumulator acc [nrows][px])
+// for the subset angles k0 .. k0+kAngChunk-1.  Starts and ends with all threads in step.
+__device__ __forceinline__ void fwd_tile(const KGeom &g, const float *__restrict__ im, double *__restrict__ acc,
+                                         const float2 *__restrict__ trig, int sub, int step, int nrows, int bx,
+                                         int by, int k0, unsigned char *smem_raw)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *tile = reinterpret_cast<float2 *>(smem_raw);
     float2 *scs = reinterpret_cast<float2 *>(smem_raw + (size_t)kFwdP * kFwdRows * sizeof(float2));
-
-    const int bx = blockIdx.x % ntx, by = blockIdx.x / ntx;
-    const int z = blockIdx.z;
-    const int k0 = blockIdx.y * kAngChunk;
     const int kn = min(kAngChunk, nrows - k0);
+    if (kn <= 0) return;
     const int x0 = -1 + bx * kFwdT, y0 = -1 + by * kFwdT;
-    const float *im = img + (size_t)z * g.nx * g.ny;
 
     // element (c, r) = (t(x0+c, y0+r), t(x0+c+1, y0+r) - t(x0+c, y0+r)), zero border
     for (int i = threadIdx.x; i < kFwdT * kFwdRows; i += kFwdThreads) {
@@ -257,9 +252,21 @@ __global__ void __launch_bounds__(kFwdThreads, 3) fwd_tiled_kernel(const float *
             // the ray's partial sum over this tile: the 4 phases, then one atomic
             sum += __shfl_xor_sync(0xffffffffu, sum, 1);
             sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-            if (ph == 0 && live && yb > ya) atomicAdd(acc + ((size_t)z * nrows + k0 + k) * g.px + X, (double)sum);
+            if (ph == 0 && live && yb > ya) atomicAdd(acc + (size_t)(k0 + k) * g.px + X, (double)sum);
         }
     }
+}
+
+// grid: (ntx*nty tiles, angle chunks, dN).  acc: [dN][nrows][px] doubles.
+__global__ void __launch_bounds__(kFwdThreads, 3) fwd_tiled_kernel(const float *__restrict__ img,
+                                                                   double *__restrict__ acc,
+                                                                   const float2 *__restrict__ trig, KGeom g, int sub,
+                                                                   int step, int nrows, int ntx)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int z = blockIdx.z;
+    fwd_tile(g, img + (size_t)z * g.nx * g.ny, acc + (size_t)z * nrows * g.px, trig, sub, step, nrows,
+             (int)blockIdx.x % ntx, (int)blockIdx.x / ntx, (int)blockIdx.y * kAngChunk, smem_raw);
 }
 
 // ------------------------------------------------------------------- exact adjoint
@@ -364,19 +371,23 @@ __global__ void fwd_finalize_kernel(double *__restrict__ acc, const float *__res
 }
 
 // ------------------------------------------------------------------- backprojector
-// grid: (ntx*nty tiles, 1, dN).  Angles th = sub + k*ss for k < nang (as OSEM2 loops).
-__global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ img,
-                                                            const float *__restrict__ ratio,
-                                                            const float2 *__restrict__ trig, KGeom g, int sub,
-                                                            int nang, int ntx, float ssf, float paf)
-{
-    __shared__ float win[kAngChunk * kBpW];
-    __shared__ float2 scs[kAngChunk];    // (c, s)
-    __shared__ int slo[kAngChunk];       // first staged bin of the angle's window
-    __shared__ unsigned soff[kAngChunk]; // byte address of window entry (bits - BIAS - lo)
+struct BpShared {
+    float win[kAngChunk * kBpW];
+    float2 scs[kAngChunk];     // (c, s)
+    int slo[kAngChunk];        // first staged bin of the angle's window
+    unsigned soff[kAngChunk];  // byte address of window entry (bits - BIAS - lo)
+};
 
-    const int bx = blockIdx.x % ntx, by = blockIdx.x / ntx;
-    const int z = blockIdx.z;
+// The work of one CTA: pixel tile (bx, by) of one slice (image img, ratio rt [pa][px]),
+// angles th = sub + k*ss for k < nang (as OSEM2 loops).  Starts/ends with threads in step.
+__device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img, const float *__restrict__ rt,
+                                        const float2 *__restrict__ trig, int sub, int nang, int bx, int by,
+                                        float ssf, float paf, BpShared &sh)
+{
+    float *win = sh.win;
+    float2 *scs = sh.scs;
+    int *slo = sh.slo;
+    unsigned *soff = sh.soff;
     const int X0 = bx * kBpTX, Y0 = by * kBpTY;
     const int X1 = min(X0 + kBpTX, g.nx) - 1, Y1 = min(Y0 + kBpTY, g.ny) - 1;
     const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;  // 8 threads x 8 pixels, 32 rows
@@ -397,7 +408,6 @@ __global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ 
     const f2x cxp = f2_pack(g.cx, g.cx);
     const f2x hp = f2_pack(0.5f, 0.5f);
     const f2x MM = f2_pack(kMagic, kMagic);
-    const float *rt = ratio + (size_t)z * g.pa * g.px;
     const unsigned wbase = (unsigned)__cvta_generic_to_shared(win);
 
     for (int k0 = 0; k0 < nang; k0 += kAngChunk) {
@@ -449,16 +459,171 @@ __global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ 
         }
     }
     if (Y <= Y1) {
-        float *row = img + ((size_t)z * g.ny + Y) * g.nx;
+        float *row = img + (size_t)Y * g.nx;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int X = X0 + tx * 8 + i;
             if (X <= X1) row[X] = xct_update(row[X], acc[i], ssf, paf);
         }
     }
+    __syncthreads();  // the shared arrays may be restaged by the caller's next tile
+}
+
+// grid: (ntx*nty tiles, 1, dN).
+__global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ img,
+                                                            const float *__restrict__ ratio,
+                                                            const float2 *__restrict__ trig, KGeom g, int sub,
+                                                            int nang, int ntx, float ssf, float paf)
+{
+    __shared__ BpShared sh;
+    const int z = blockIdx.z;
+    bp_tile(g, img + (size_t)z * g.nx * g.ny, ratio + (size_t)z * g.pa * g.px, trig, sub, nang,
+            (int)blockIdx.x % ntx, (int)blockIdx.x / ntx, ssf, paf, sh);
+}
+
+// ----------------------------------------------------------------- batched launches
+// One subset step of many slices of different shapes in one persistent launch per kernel:
+// CTAs take (slice, tile) work units from a device queue (an atomic counter) until the
+// units run out.  Units of slice i are [base[i], base[i+1]); they are independent within a
+// launch, so there is no waiting on other CTAs.
+__device__ __forceinline__ int queue_take(int *queue, int *s_unit)
+{
+    if (threadIdx.x == 0) *s_unit = atomicAdd(queue, 1);
+    __syncthreads();
+    const int u = *s_unit;
+    __syncthreads();
+    return u;
+}
+
+// Slice owning unit u: the last i with base[i] <= u (binary search, one thread).
+__device__ __forceinline__ int unit_item(const int *__restrict__ base, int n, int u, int *s_item)
+{
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (base[mid] <= u) lo = mid;
+            else hi = mid - 1;
+        }
+        *s_item = lo;
+    }
+    __syncthreads();
+    const int i = *s_item;
+    __syncthreads();
+    return i;
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 3) fwd_batched_kernel(const XctItemDev *__restrict__ items,
+                                                                     const int *__restrict__ base, int n, int sub,
+                                                                     int *queue)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_unit, s_item;
+    const int total = base[n];
+    for (;;) {
+        const int u = queue_take(queue, &s_unit);
+        if (u >= total) break;
+        const int i = unit_item(base, n, u, &s_item);
+        const XctItemDev &it = items[i];
+        const KGeom &g = it.g;
+        const int nrows = it.cover ? (g.pa - sub + g.ss - 1) / g.ss : g.pa / g.ss;
+        const int local = u - base[i];
+        const int tiles = it.fwd_ntx * it.fwd_nty;
+        const int t = local % tiles, ch = local / tiles;
+        fwd_tile(g, it.img, it.acc, it.trig, sub, g.ss, nrows, t % it.fwd_ntx, t / it.fwd_ntx, ch * kAngChunk,
+                 smem_raw);
+        __syncthreads();  // the tile in shared memory is restaged by the next unit
+    }
+}
+
+__global__ void fwd_finalize_batched_kernel(const XctItemDev *__restrict__ items, const int *__restrict__ base,
+                                            int n, int sub, int *queue)
+{
+    __shared__ int s_unit, s_item;
+    const int total = base[n];
+    for (;;) {
+        const int u = queue_take(queue, &s_unit);
+        if (u >= total) break;
+        const int i = unit_item(base, n, u, &s_item);
+        const XctItemDev &it = items[i];
+        const KGeom &g = it.g;
+        const int nrows = it.cover ? (g.pa - sub + g.ss - 1) / g.ss : g.pa / g.ss;
+        const int k = u - base[i];  // one unit per ratio row of the largest subset
+        if (k >= nrows) continue;
+        const int th = sub + k * g.ss;
+        for (int X = threadIdx.x; X < g.px; X += blockDim.x) {
+            double *a = it.acc + (size_t)k * g.px + X;
+            const float p = (float)*a;
+            *a = 0.0;
+            const float yv = xct_measured(it.sino, g.px, g.pa, X, th, g.fetch);
+            it.ratio[(size_t)th * g.px + X] = xct_ratio(yv, p);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) bp_batched_kernel(const XctItemDev *__restrict__ items,
+                                                              const int *__restrict__ base, int n, int sub,
+                                                              int *queue)
+{
+    __shared__ BpShared sh;
+    __shared__ int s_unit, s_item;
+    const int total = base[n];
+    for (;;) {
+        const int u = queue_take(queue, &s_unit);
+        if (u >= total) break;
+        const int i = unit_item(base, n, u, &s_item);
+        const XctItemDev &it = items[i];
+        const KGeom &g = it.g;
+        const int nang = (g.pa - sub + g.ss - 1) / g.ss;
+        const int t = u - base[i];
+        bp_tile(g, it.img, it.ratio, it.trig, sub, nang, t % it.bp_ntx, t / it.bp_ntx, (float)g.ss, (float)g.pa,
+                sh);
+    }
 }
 
 }  // namespace
+
+void xct_batched_units(const KGeom &g, int &fwd_ntx, int &fwd_nty, int &fwd_units, int &fin_units, int &bp_ntx,
+                       int &bp_units)
+{
+    fwd_ntx = (g.nx + 1 + kFwdT - 1) / kFwdT;
+    fwd_nty = (g.ny + 1 + kFwdT - 1) / kFwdT;
+    const int rows = (g.pa + g.ss - 1) / g.ss;  // the largest subset (cover mode)
+    fwd_units = fwd_ntx * fwd_nty * ((rows + kAngChunk - 1) / kAngChunk);
+    fin_units = rows;
+    bp_ntx = (g.nx + kBpTX - 1) / kBpTX;
+    bp_units = bp_ntx * ((g.ny + kBpTY - 1) / kBpTY);
+}
+
+int xct_batched_grids(int device, int sm_count, int grids[3])
+{
+    static bool attr_set[64] = {};
+    if (device >= 0 && device < 64 && !attr_set[device]) {
+        XCT_CUDA_TRY(cudaFuncSetAttribute(fwd_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kFwdSmem));
+        attr_set[device] = true;
+    }
+    int a = 0, b = 0, c = 0;
+    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fwd_batched_kernel, kFwdThreads, kFwdSmem));
+    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fwd_finalize_batched_kernel, 256, 0));
+    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, bp_batched_kernel, kThreads, 0));
+    grids[0] = sm_count * (a > 0 ? a : 1);
+    grids[1] = sm_count * (b > 0 ? b : 1);
+    grids[2] = sm_count * (c > 0 ? c : 1);
+    return XCT_OK;
+}
+
+int launch_osem_step_batched(const XctItemDev *items, const int *bases /*[3][n+1]*/, int n, int sub,
+                             int *queues /*[3]*/, const int grids[3], cudaStream_t st)
+{
+    fwd_batched_kernel<<<grids[0], kFwdThreads, kFwdSmem, st>>>(items, bases, n, sub, queues);
+    XCT_CUDA_TRY(cudaGetLastError());
+    fwd_finalize_batched_kernel<<<grids[1], 256, 0, st>>>(items, bases + (n + 1), n, sub, queues + 1);
+    XCT_CUDA_TRY(cudaGetLastError());
+    bp_batched_kernel<<<grids[2], kThreads, 0, st>>>(items, bases + 2 * (n + 1), n, sub, queues + 2);
+    XCT_CUDA_TRY(cudaGetLastError());
+    return XCT_OK;  // launches are counted when the captured graph is replayed
+}
 
 int fwd_tiled_rows_cap() { return kAngChunk; }
 

@@ -46,6 +46,7 @@ EXPORTS = (
     "xct_osem_run", "xct_osem_run_device", "xct_fwd", "xct_bp_ref", "xct_adj",
     "xct_plan_sync", "xct_plan_last_ms", "xct_launch_count", "xct_last_error", "xct_abi_version",
     "xct_osem_profile", "xct_fp32_peak", "xct_osem1", "xct_osem2", "xct_osem_run_static",
+    "xct_batch_plan_create", "xct_batch_run", "xct_batch_plan_destroy", "xct_osem_run_batched",
 )
 
 
@@ -100,6 +101,10 @@ def load():
     L.xct_osem1.argtypes = [vp, ip, ip, vp, vp, vp, vp]
     L.xct_osem2.argtypes = [vp, ip, ip, vp, vp, vp]
     L.xct_osem_run_static.argtypes = [ctypes.POINTER(Geom), ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, vp]
+    L.xct_batch_plan_create.argtypes = [vp, ip, ctypes.POINTER(Geom), ip, ctypes.POINTER(vp)]
+    L.xct_batch_run.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
+    L.xct_batch_plan_destroy.argtypes = [vp]
+    L.xct_osem_run_batched.argtypes = [vp, ip, ctypes.POINTER(Geom), ctypes.POINTER(vp), ctypes.POINTER(vp), ip, vp]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong
@@ -283,6 +288,48 @@ class OSEMPlan:
 
     def sync(self):
         _check(self._lib.xct_plan_sync(self.handle))
+
+
+def make_geom(nx, ny, px, angles_deg, ss, it, center_bin=None, fetch_mode=FETCH_EXACT, subset_mode=SUBSETS_REF,
+              correction_mode=0, max_batch=1, kernels=KERNELS_TILED):
+    """An xct_geom (keeps the angle array alive on the returned object as ._angles)."""
+    ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+    g = Geom(nx, ny, nx, ny, px, int(ang.size), ss, it, ang.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+             -1.0 if center_bin is None else float(center_bin), fetch_mode, subset_mode, correction_mode,
+             max_batch, kernels)
+    g._angles = ang
+    return g
+
+
+class BatchPlan:
+    """OS-EM over slices of different shapes (same subset count) in one CUDA graph of
+    persistent launches (xct_batch_plan_create / xct_batch_run)."""
+
+    def __init__(self, ctx, geoms, it):
+        self._lib = load()
+        self.ctx = ctx
+        self.geoms = list(geoms)
+        arr = (Geom * len(self.geoms))(*self.geoms)
+        h = ctypes.c_void_p()
+        _check(self._lib.xct_batch_plan_create(ctx.handle, len(self.geoms), arr, it, ctypes.byref(h)))
+        self.handle = h
+
+    def run(self, sinos, imgs, stream=None):
+        n = len(self.geoms)
+        s = (ctypes.c_void_p * n)(*[_ptr(t) for t in sinos])
+        i = (ctypes.c_void_p * n)(*[_ptr(t) for t in imgs])
+        _check(self._lib.xct_batch_run(self.handle, s, i, _stream(stream)))
+
+    def close(self):
+        if self.handle:
+            self._lib.xct_batch_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------- reference-named mirrors

@@ -123,3 +123,35 @@ def xanes_mixture(n_energy=64, seed=3, e_range=(7080.0, 7180.0)):
     e = np.linspace(e_range[0], e_range[1], n_energy)
     s = [xanes_spectrum(e, wl_amp=rng.uniform(0.2, 1.5), wl_sigma=rng.uniform(2.0, 5.0)) for _ in range(2)]
     return e, s[0], s[1]
+
+
+def ctxafs_item_specs(n, seed=3, widths=(512, 1024, 1536, 2048), angles=(360, 720, 900, 1200), max_drop=0.10):
+    """n slice shapes of a CT-XAFS stack: width w (bins = w) from `widths`, a projection count
+    from `angles` over 180 deg with 0..max_drop of the angles dropped at random (seeded).
+    Returns a list of (w, angle array in degrees)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        w = int(rng.choice(widths))
+        pa = int(rng.choice(angles))
+        drop = int(rng.integers(0, int(max_drop * pa) + 1))
+        keep = np.sort(rng.choice(pa, pa - drop, replace=False))
+        out.append((w, (keep * (180.0 / pa)).astype(np.float32)))
+    return out
+
+
+def xanes_slice(w, energy_index, seed, spectra, mu_scale=0.02, torch_device=None):
+    """One slice of a CT-XAFS volume at one energy: inside a few ellipses, each voxel is the
+    mixture f*S1(E) + (1-f)*S2(E) with a seeded per-voxel fraction f (smoothed noise), times
+    mu_scale per pixel."""
+    e, s1, s2 = spectra
+    rng = np.random.default_rng(seed)
+    support = rasterize_ellipses(ellipse_params(w, 4, seed, axes=(0.1 * w, 0.35 * w), mu=(1.0, 1.0)), w, w) > 0
+    f = rng.uniform(0.0, 1.0, (w // 16 + 1, w // 16 + 1))
+    f = np.kron(f, np.ones((16, 16)))[:w, :w]  # piecewise-constant per 16x16 voxel block
+    mu = support * (f * s1[energy_index] + (1.0 - f) * s2[energy_index]) * mu_scale
+    mu = mu.astype(np.float32)
+    if torch_device is not None:
+        import torch
+        return torch.from_numpy(mu).to(torch_device)
+    return mu

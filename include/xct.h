@@ -91,6 +91,24 @@ int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *c
 int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                         void *stream);
 
+/* ---- batches of slices of different shapes (CT-XAFS stacks) -------------------------
+ * The reference reconstructs dN slices of ONE shape per OSEM_execution call
+ * (GPU.cpp:125-240, image2d_array layers).  A batch plan takes n slices of any shapes
+ * (each its own xct_geom: size, bins, angle list, centre, modes) that share the subset
+ * count; every subset step is three persistent launches whose CTAs take (slice, tile) work
+ * units from a device queue, and the whole subset/iteration loop is one CUDA graph,
+ * captured on the first xct_batch_run and replayed after.  d_sino[i] / d_img[i] are slice
+ * i's device sinogram [pa_i][px_i] and image [ny_i][nx_i] (initial in, result out); they may
+ * change from run to run.  Runs of one plan must not overlap (they share its buffers).
+ * Sinogram correction is not available in batches.  xct_osem_run_batched = create, run,
+ * synchronise the stream, destroy. */
+typedef struct xct_batch_plan xct_batch_plan;
+int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms, int it, xct_batch_plan **out);
+int xct_batch_run(xct_batch_plan *plan, const float *const *d_sino, float *const *d_img, void *stream);
+int xct_batch_plan_destroy(xct_batch_plan *plan);
+int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, const float *const *d_sino,
+                         float *const *d_img, int it, void *stream);
+
 /* ---- OS-EM without any allocation ----------------------------------------------------
  * No counterpart in the reference: the reference allocates its image objects on every call.
  *
