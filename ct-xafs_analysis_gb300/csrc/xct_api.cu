@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <new>
 
 #include "xct_internal.h"
@@ -142,6 +143,7 @@ static void plan_free(xct_plan *p)
     cudaFree(p->d_corr_ang);
     cudaFree(p->d_corr_bin);
     cudaFree(p->d_acc);
+    cudaFree(p->d_min_keys);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -158,6 +160,8 @@ static int check_geom(const xct_geom *g)
                         "geometry: output ROI smaller than the reconstruction (ox < nx) is not supported; the "
                         "reference's own ROI path updates a different region than it reads back (GPU.cpp:152-170)");
     if (g->ss > g->pa) return xct_fail(XCT_E_INVALID, "geometry: more subsets than angles");
+    if (!(g->center_bin < 2.0f * (float)g->px))
+        return xct_fail(XCT_E_INVALID, "geometry: center_bin must be finite and below 2*px (< 0 selects px/2)");
     if (!g->angles_deg) return xct_fail(XCT_E_INVALID, "geometry: angles_deg is null");
     if (g->nx > 16384 || g->ny > 16384 || g->px > 65536 || g->pa > 65536)
         return xct_fail(XCT_E_INVALID, "geometry: size beyond the supported maximum (16384 px image, 65536 bins)");
@@ -218,6 +222,7 @@ int xct_osem_plan_create(xct_ctx *ctx, const xct_geom *geom, xct_plan **out)
     if ((e = cudaMalloc(&p->d_sino, sizeof(float) * nb * nprj)) != cudaSuccess) return fail(e, "cudaMalloc sino");
     if ((e = cudaMalloc(&p->d_img, sizeof(float) * nb * nimg)) != cudaSuccess) return fail(e, "cudaMalloc img");
     if ((e = cudaMalloc(&p->d_ratio, sizeof(float) * nb * nprj)) != cudaSuccess) return fail(e, "cudaMalloc ratio");
+    if ((e = cudaMalloc(&p->d_min_keys, sizeof(int) * nb)) != cudaSuccess) return fail(e, "cudaMalloc min keys");
     if ((e = cudaMemsetAsync(p->d_ratio, 0, sizeof(float) * nb * nprj, p->stream)) != cudaSuccess)
         return fail(e, "memset ratio");
     if (geom->kernels == XCT_KERNELS_TILED) {
@@ -285,11 +290,11 @@ static inline int subset_rows(const xct_plan *p, int sub)
 // backprojection update is done in place, which is equivalent because each pixel's new
 // value depends only on its own old value and the ratio image.
 static int osem_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it,
-                     cudaStream_t st)
+                     cudaStream_t st, bool correct = true)
 {
     const KGeom &g = p->kg;
     const float *meas = d_sino;
-    if (p->g.correction_mode > 0) {
+    if (correct && p->g.correction_mode > 0) {
         int rc = launch_sino_correction(g, d_sino, p->d_corr, p->d_corr_ang, p->d_corr_bin, p->g.correction_mode, dN,
                                         st);
         if (rc) return rc;
@@ -498,6 +503,138 @@ int xct_osem_profile(xct_plan *p, int dN, const float *d_sino, float *d_img, con
     }
     cleanup();
     return rc;
+}
+
+// ---------------------------------------------------------------------------- FBP
+// FBP_execution (GPU.cpp:665-819) on dN slices already on the device: the plan's sinogram
+// correction when it has one (GPU.cpp:711-723, applied into the correction buffer), the
+// ramp filter into the ratio buffer, backProjectionFBP into d_img.  The ratio buffer is
+// cleared afterwards: OS-EM relies on the rows it never writes being 0.
+static int fbp_device(xct_plan *p, int dN, int zp, const float *d_sino, float *d_img, bool with_min,
+                      const float **meas_out, cudaStream_t st)
+{
+    const KGeom &g = p->kg;
+    const float *meas = d_sino;
+    if (p->g.correction_mode > 0) {
+        int rc = launch_sino_correction(g, d_sino, p->d_corr, p->d_corr_ang, p->d_corr_bin, p->g.correction_mode, dN,
+                                        st);
+        if (rc) return rc;
+        meas = p->d_corr;
+    }
+    int rc = launch_fbp_filter(g, meas, p->d_ratio, dN, zp, st);
+    if (rc) return rc;
+    rc = launch_fbp_bp(g, p->d_trig, p->d_ratio, d_img, dN, with_min ? p->d_min_keys : nullptr, st);
+    if (rc) return rc;
+    XCT_CUDA_TRY(cudaMemsetAsync(p->d_ratio, 0, sizeof(float) * dN * (size_t)g.pa * g.px, st));
+    if (meas_out) *meas_out = meas;
+    return XCT_OK;
+}
+
+int xct_fbp_filter(xct_plan *p, int dN, int zp, const float *d_sino, float *d_fprj, void *stream)
+{
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if (!d_sino || !d_fprj) return xct_fail(XCT_E_INVALID, "xct_fbp_filter: null device pointer");
+    if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return launch_fbp_filter(p->kg, d_sino, d_fprj, dN, zp, (cudaStream_t)stream);
+}
+
+int xct_fbp_backproject(xct_plan *p, int dN, const float *d_fprj, float *d_img, void *stream)
+{
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if (!d_fprj || !d_img) return xct_fail(XCT_E_INVALID, "xct_fbp_backproject: null device pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return launch_fbp_bp(p->kg, p->d_trig, d_fprj, d_img, dN, nullptr, (cudaStream_t)stream);
+}
+
+int xct_fbp_run_device(xct_plan *p, int dN, int zp, const float *d_sino, float *d_img, void *stream)
+{
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_fbp_run_device: null device pointer");
+    if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return fbp_device(p, dN, zp, d_sino, d_img, false, nullptr, (cudaStream_t)stream);
+}
+
+// hybrid_thread (GPU.cpp:1458-1600): FBP_execution with the sinogram correction, the
+// base-up of FBPcorrection = 1 (slice minimum, then baseUp with baseupOrder), then
+// OSEM_execution on the corrected sinogram without correcting it again.
+static int hybrid_device(xct_plan *p, int dN, int zp, int order, const float *d_sino, float *d_img, const int *sub,
+                         int it, cudaStream_t st)
+{
+    const float *meas = nullptr;
+    int rc = fbp_device(p, dN, zp, d_sino, d_img, true, &meas, st);
+    if (rc) return rc;
+    rc = launch_base_up(p->kg, d_img, dN, order, p->d_min_keys, p->ctx->sm_count, st);
+    if (rc) return rc;
+    return osem_loop(p, dN, meas, d_img, sub ? sub : p->sub_default.data(), it, st, false);
+}
+
+int xct_hybrid_run_device(xct_plan *p, int dN, int zp, int baseup_order, const float *d_sino, float *d_img,
+                          const int *sub, int it, void *stream)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_hybrid_run_device: null device pointer");
+    if (baseup_order < 0 || baseup_order > 64) return xct_fail(XCT_E_INVALID, "xct_hybrid_run_device: order 0..64");
+    if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return hybrid_device(p, dN, zp, baseup_order, d_sino, d_img, sub, it, (cudaStream_t)stream);
+}
+
+// Host-buffer forms (FBP_thread GPU.cpp:822-893, hybrid_thread): copies in, run, copies out.
+static int host_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, bool upload_img,
+                    const std::function<int(cudaStream_t)> &run)
+{
+    if (!sino_host || !img_host) return xct_fail(XCT_E_INVALID, "null host array");
+    for (int i = 0; i < dN; ++i)
+        if (!sino_host[i] || !img_host[i]) return xct_fail(XCT_E_INVALID, "null slice pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    const size_t nimg = (size_t)p->g.nx * p->g.ny, nprj = (size_t)p->g.px * p->g.pa;
+    cudaStream_t st = p->stream;
+    for (int i = 0; i < dN; ++i) {
+        XCT_CUDA_TRY(cudaMemcpyAsync(p->d_sino + i * nprj, sino_host[i], sizeof(float) * nprj,
+                                     cudaMemcpyHostToDevice, st));
+        if (upload_img)
+            XCT_CUDA_TRY(cudaMemcpyAsync(p->d_img + i * nimg, img_host[i], sizeof(float) * nimg,
+                                         cudaMemcpyHostToDevice, st));
+    }
+    XCT_CUDA_TRY(cudaEventRecord(p->ev0, st));
+    int rc = run(st);
+    if (rc) return rc;
+    XCT_CUDA_TRY(cudaEventRecord(p->ev1, st));
+    for (int i = 0; i < dN; ++i)
+        XCT_CUDA_TRY(
+            cudaMemcpyAsync(img_host[i], p->d_img + i * nimg, sizeof(float) * nimg, cudaMemcpyDeviceToHost, st));
+    XCT_CUDA_TRY(cudaStreamSynchronize(st));
+    XCT_CUDA_TRY(cudaEventElapsedTime(&p->last_ms, p->ev0, p->ev1));
+    return XCT_OK;
+}
+
+int xct_fbp_run(xct_plan *p, int dN, int zp, const float *const *sino_host, float *const *img_host)
+{
+    int rc = check_run(p, dN, nullptr, 0);
+    if (rc) return rc;
+    if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    return host_run(p, dN, sino_host, img_host, false,
+                    [&](cudaStream_t st) { return fbp_device(p, dN, zp, p->d_sino, p->d_img, false, nullptr, st); });
+}
+
+int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *const *sino_host,
+                   float *const *img_host, const int *sub, int it)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (baseup_order < 0 || baseup_order > 64) return xct_fail(XCT_E_INVALID, "xct_hybrid_run: order 0..64");
+    if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
+        return hybrid_device(p, dN, zp, baseup_order, p->d_sino, p->d_img, sub, it, st);
+    });
 }
 
 int xct_plan_sync(xct_plan *p)

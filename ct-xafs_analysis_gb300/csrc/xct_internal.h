@@ -54,6 +54,7 @@ struct xct_plan {
     float *d_corr_ang = nullptr; // [pa] x 2 per-angle correction factors
     float *d_corr_bin = nullptr; // [px] per-bin correction factors
     double *d_acc = nullptr;     // tiled forward: ray-sum accumulator [max_batch][acc_rows][px]
+    int *d_min_keys = nullptr;   // [max_batch] per-slice image minimum (FBP + OS-EM hybrid)
     int acc_rows = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -111,6 +112,18 @@ int launch_osem_step_batched(const XctItemDev *items, const int *bases, int n, i
 int xct_check_geom(const xct_geom *g);
 // Exact adjoint of the forward projector over all angles: img = A^T sino (overwrites img).
 int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, cudaStream_t st);
+// FBP (xct_fbp.cu).  zp: the zero-padded transform length (0 -> smallest power of two
+// >= 2 px); checked and resolved by xct_fbp_check_zp.
+int xct_fbp_check_zp(int px, int &zp);
+// Ramp filter of dN sinograms [pa][px] -> [pa][px] (FBP.cl:34-160).
+int launch_fbp_filter(const KGeom &g, const float *sino, float *out, int dN, int zp, cudaStream_t st);
+// backProjectionFBP (FBP.cl:164-188) of dN filtered sinograms; min_keys (optional, [dN])
+// receives each slice's minimum as an ordered integer key.
+int launch_fbp_bp(const KGeom &g, const float2 *trig, const float *fprj, float *img, int dN, int *min_keys,
+                  cudaStream_t st);
+// baseUp (reconstShare.cl:87-109) with the slice minima of launch_fbp_bp, in place.
+int launch_base_up(const KGeom &g, float *img, int dN, int order, const int *min_keys, int sm_count,
+                   cudaStream_t st);
 // sinogramCorrection (reconstShare.cl:35-70), modes 1..4, src -> dst.
 int launch_sino_correction(const KGeom &g, const float *src, float *dst, const float *ang_fac, const float *bin_fac,
                            int mode, int dN, cudaStream_t st);

@@ -47,6 +47,8 @@ EXPORTS = (
     "xct_plan_sync", "xct_plan_last_ms", "xct_launch_count", "xct_last_error", "xct_abi_version",
     "xct_osem_profile", "xct_fp32_peak", "xct_osem1", "xct_osem2", "xct_osem_run_static",
     "xct_batch_plan_create", "xct_batch_run", "xct_batch_plan_destroy", "xct_osem_run_batched",
+    "xct_fbp_filter", "xct_fbp_backproject", "xct_fbp_run_device", "xct_hybrid_run_device", "xct_fbp_run",
+    "xct_hybrid_run",
 )
 
 
@@ -105,6 +107,13 @@ def load():
     L.xct_batch_run.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
     L.xct_batch_plan_destroy.argtypes = [vp]
     L.xct_osem_run_batched.argtypes = [vp, ip, ctypes.POINTER(Geom), ctypes.POINTER(vp), ctypes.POINTER(vp), ip, vp]
+    L.xct_fbp_filter.argtypes = [vp, ip, ip, vp, vp, vp]
+    L.xct_fbp_backproject.argtypes = [vp, ip, vp, vp, vp]
+    L.xct_fbp_run_device.argtypes = [vp, ip, ip, vp, vp, vp]
+    L.xct_hybrid_run_device.argtypes = [vp, ip, ip, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, vp]
+    L.xct_fbp_run.argtypes = [vp, ip, ip, ctypes.POINTER(fp), ctypes.POINTER(fp)]
+    L.xct_hybrid_run.argtypes = [vp, ip, ip, ip, ctypes.POINTER(fp), ctypes.POINTER(fp),
+                                 ctypes.POINTER(ctypes.c_int), ip]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong
@@ -241,6 +250,27 @@ class OSEMPlan:
         _check(self._lib.xct_osem_run(self.handle, dN, s_arr, i_arr, self._sub(sub), it))
         return imgs
 
+    def _host_arrays(self, sinos, imgs):
+        fp = ctypes.POINTER(ctypes.c_float)
+        for a in list(sinos) + list(imgs):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                raise XCTError(XCT_E_INVALID, "host arrays must be C-contiguous float32 numpy arrays")
+        dN = len(sinos)
+        return (fp * dN)(*[s.ctypes.data_as(fp) for s in sinos]), (fp * dN)(*[i.ctypes.data_as(fp) for i in imgs])
+
+    def fbp_run(self, sinos, imgs, zp=0):
+        """FBP (FBP_thread) on host arrays; reconstructions written into ``imgs``."""
+        s_arr, i_arr = self._host_arrays(sinos, imgs)
+        _check(self._lib.xct_fbp_run(self.handle, len(sinos), zp, s_arr, i_arr))
+        return imgs
+
+    def hybrid_run(self, sinos, imgs, zp=0, baseup_order=4, sub=None, it=-1):
+        """FBP + base-up + OS-EM (hybrid_thread) on host arrays."""
+        s_arr, i_arr = self._host_arrays(sinos, imgs)
+        _check(self._lib.xct_hybrid_run(self.handle, len(sinos), zp, baseup_order, s_arr, i_arr, self._sub(sub),
+                                        it))
+        return imgs
+
     def last_ms(self):
         v = ctypes.c_float()
         _check(self._lib.xct_plan_last_ms(self.handle, ctypes.byref(v)))
@@ -274,6 +304,27 @@ class OSEMPlan:
     def adj(self, d_sino, d_img, dN=None, stream=None):
         dN = d_img.shape[0] if dN is None else dN
         _check(self._lib.xct_adj(self.handle, dN, _ptr(d_sino), _ptr(d_img), _stream(stream)))
+
+    def fbp_filter(self, d_sino, d_fprj, zp=0, dN=None, stream=None):
+        """Ramp-filtered sinograms (FBP.cl:34-160) into d_fprj."""
+        dN = d_sino.shape[0] if dN is None else dN
+        _check(self._lib.xct_fbp_filter(self.handle, dN, zp, _ptr(d_sino), _ptr(d_fprj), _stream(stream)))
+
+    def fbp_backproject(self, d_fprj, d_img, dN=None, stream=None):
+        """backProjectionFBP (FBP.cl:164-188) of filtered sinograms into d_img."""
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_fbp_backproject(self.handle, dN, _ptr(d_fprj), _ptr(d_img), _stream(stream)))
+
+    def fbp(self, d_sino, d_img, zp=0, dN=None, stream=None):
+        """FBP_execution: (correction), filter, backprojection."""
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_fbp_run_device(self.handle, dN, zp, _ptr(d_sino), _ptr(d_img), _stream(stream)))
+
+    def hybrid(self, d_sino, d_img, zp=0, baseup_order=4, dN=None, sub=None, it=-1, stream=None):
+        """FBP + base-up + OS-EM of hybrid_thread on device tensors."""
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_hybrid_run_device(self.handle, dN, zp, baseup_order, _ptr(d_sino), _ptr(d_img),
+                                               self._sub(sub), it, _stream(stream)))
 
     def profile(self, d_sino, d_img, dN=None, sub=None, it=-1, stream=None):
         """Run OS-EM with CUDA events around every launch; returns a dict of summed device
@@ -343,6 +394,18 @@ def OSEM_execution(plan, sub, reconst_img, prj_img, dN, it, prjCorrection=True, 
     if not prjCorrection and plan is not None and getattr(plan, "_correction", 0):
         raise XCTError(XCT_E_INVALID, "plan was built with a sinogram correction mode")
     plan.run_device(prj_img, reconst_img, dN=dN, sub=sub, it=it, stream=stream)
+    return 0
+
+
+def FBP_execution(plan, reconst_img, prj_img, dN, prjCorrection=True, zp=0, stream=None):
+    """Mirror of ``int FBP_execution(queue, kernels, angle_buffer, Image2DArray reconst_img,
+    Image2DArray prj_img, int dN, bool prjCorrection, unsigned int iter)``
+    (CT_reconstruction.hpp, GPU.cpp:665-819) on device tensors; the transform length is zp
+    (the reference passes log2 of it as ``iter``).  The sinogram correction is the plan's.
+    Returns 0."""
+    if not prjCorrection and plan is not None and getattr(plan, "_correction", 0):
+        raise XCTError(XCT_E_INVALID, "plan was built with a sinogram correction mode")
+    plan.fbp(prj_img, reconst_img, zp=zp, dN=dN, stream=stream)
     return 0
 
 

@@ -158,6 +158,35 @@ int xct_fwd(xct_plan *plan, int dN, const float *d_img, float *d_sino, void *str
 int xct_bp_ref(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
 int xct_adj(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
 
+/* ---- filtered backprojection and the FBP + OS-EM hybrid (methods 7 and 8 of GPU(),
+ * GPU.cpp:80-90) ---------------------------------------------------------------------
+ * zp is the zero-padded transform length (g_zp, main.cpp:36; default 4096): a power of two
+ * with px <= zp <= 16384 and zp >= 64; 0 selects the smallest power of two >= 2*px.
+ * xct_fbp_filter      : the ramp filter chain of FBP_execution (GPU.cpp:745-806 over
+ *                       FBP.cl:34-160): d_fprj [dN][pa][px] = filtered d_sino.
+ * xct_fbp_backproject : backProjectionFBP (FBP.cl:164-188): d_img [dN][ny][nx] =
+ *                       (1/(2 pa)) sum over all angles of the linearly interpolated
+ *                       d_fprj, 0 outside the circle r < nx/2.
+ * xct_fbp_run_device  : FBP_execution (GPU.cpp:665-819): the plan's sinogram correction
+ *                       (if any), the filter, the backprojection.  Uses the plan's ratio
+ *                       buffer as scratch (calls on one plan must not overlap).
+ * xct_hybrid_run_device : hybrid_thread (GPU.cpp:1458-1600): FBP as above, then the base-up
+ *                       of its FBPcorrection = 1 branch (slice minimum a of findMinimumX/Y,
+ *                       then baseUp, reconstShare.cl:87-177, with order baseup_order 0..64;
+ *                       baseupOrder, main.cpp:44, default 4), then `it` OS-EM iterations on
+ *                       the corrected sinogram (it < 0: the plan's; sub NULL: plan order).
+ * xct_fbp_run / xct_hybrid_run : the same from host buffers (FBP_thread, GPU.cpp:822-893):
+ *                       sinograms in, images out (the images' initial contents are not
+ *                       read: the backprojection writes every pixel).  Blocking. */
+int xct_fbp_filter(xct_plan *plan, int dN, int zp, const float *d_sino, float *d_fprj, void *stream);
+int xct_fbp_backproject(xct_plan *plan, int dN, const float *d_fprj, float *d_img, void *stream);
+int xct_fbp_run_device(xct_plan *plan, int dN, int zp, const float *d_sino, float *d_img, void *stream);
+int xct_hybrid_run_device(xct_plan *plan, int dN, int zp, int baseup_order, const float *d_sino, float *d_img,
+                          const int *sub, int it, void *stream);
+int xct_fbp_run(xct_plan *plan, int dN, int zp, const float *const *sino_host, float *const *img_host);
+int xct_hybrid_run(xct_plan *plan, int dN, int zp, int baseup_order, const float *const *sino_host,
+                   float *const *img_host, const int *sub, int it);
+
 /* Tracing: xct_osem_run_device with CUDA events around every launch.  The reference
  * enables CL_QUEUE_PROFILING_ENABLE but never reads the events
  * (share source/OCL_platform_device_class.cpp:175-178).  ms[0..3] = summed device time of

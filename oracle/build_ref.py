@@ -3,11 +3,14 @@
 TEST INFRASTRUCTURE ONLY.  The reference (NozomuIshiguro/CT-XAFS_analysis) has no tests
 and no CPU build; its kernels are OpenCL C JIT-compiled at run time with the problem shape
 as -D macros (CT_reconstruction/GPU.cpp:537-550).  This recipe compiles
-CT_reconstruction/OSEM.cl and CT_reconstruction/reconstShare.cl, where they lie in the
-reference checkout, with g++ against oracle/ref_shim/cl_shim.hpp (an OpenCL-C environment
-written for this project).  The only change to the kernel text is mechanical and happens
-in the build output: OpenCL vector literals ``(float4)(a,b,c,d)`` become constructor calls
-``float4(a,b,c,d)`` (C++ would parse the former as a comma expression).  The generated
+CT_reconstruction/FBP.cl, CT_reconstruction/OSEM.cl and CT_reconstruction/reconstShare.cl,
+where they lie in the reference checkout, with g++ against oracle/ref_shim/cl_shim.hpp (an
+OpenCL-C environment written for this project).  The only changes to the kernel text are
+mechanical and happen in the build output: OpenCL vector literals ``(float4)(a,b,c,d)``
+become constructor calls ``float4(a,b,c,d)`` (C++ would parse the former as a comma
+expression), the two-component swizzles ``v.xx`` / ``v.yy`` / ``v.yx`` become member calls
+``v.xx()`` etc., and the bare address-space qualifier ``global`` becomes ``__global``.  The
+FBP program is built with -D ZP_SIZE as the reference builds it (GPU.cpp:947-954).  The generated
 translation unit and the shared objects go to oracle/_ref/ (git-ignored), one library per
 problem shape, exactly as the reference JIT-builds one program per shape.
 
@@ -22,8 +25,10 @@ import hashlib
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_ROOT = os.environ.get("XCT_REFERENCE_ROOT", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
-KERNELS = ("CT_reconstruction/OSEM.cl", "CT_reconstruction/reconstShare.cl")
-_VEC = re.compile(r"\((float|int)([234])\)\s*\(")
+KERNELS = ("CT_reconstruction/FBP.cl", "CT_reconstruction/OSEM.cl", "CT_reconstruction/reconstShare.cl")
+_VEC = re.compile(r"\((float|int|uint)([234])\)\s*\(")
+_SWZ = re.compile(r"\.(xx|yy|yx)\b")
+_GLOBAL = re.compile(r"(?<![_\w])global(?=\s)")
 
 
 def available():
@@ -32,11 +37,22 @@ def available():
 
 def _rewrite(text):
     text = text.lstrip("﻿")
-    return _VEC.sub(lambda m: "%s%s(" % (m.group(1), m.group(2)), text)
+    text = _VEC.sub(lambda m: "%s%s(" % (m.group(1), m.group(2)), text)
+    text = _SWZ.sub(lambda m: ".%s()" % m.group(1), text)
+    return _GLOBAL.sub("__global", text)
 
 
-def build(nx, ny, px, pa, ss, force=False):
+def default_zp(px):
+    """Smallest power of two >= 2*px (4096 for 2048 bins, the reference's default g_zp)."""
+    zp = 1
+    while zp < 2 * px:
+        zp *= 2
+    return zp
+
+
+def build(nx, ny, px, pa, ss, zp=None, force=False):
     """Compile the reference kernels for one shape; return the .so path."""
+    zp = default_zp(px) if zp is None else int(zp)
     if not available():
         raise FileNotFoundError("reference kernel sources not found under %s" % REF_ROOT)
     os.makedirs(OUT, exist_ok=True)
@@ -48,7 +64,7 @@ def build(nx, ny, px, pa, ss, force=False):
     parts.append("}  // namespace clk")
     parts.append('#include "%s"' % os.path.join(HERE, "ref_shim", "ref_driver.inc"))
     src = "\n".join(parts) + "\n"
-    tag = "%dx%d_%dx%d_s%d" % (nx, ny, px, pa, ss)
+    tag = "%dx%d_%dx%d_s%d_zp%d" % (nx, ny, px, pa, ss, zp)
     h = hashlib.sha1(src.encode())
     for dep in ("cl_shim.hpp", "ref_driver.inc"):
         with open(os.path.join(HERE, "ref_shim", dep), "rb") as f:
@@ -63,7 +79,7 @@ def build(nx, ny, px, pa, ss, force=False):
     defs = [
         "-DIMAGESIZE_X=%d" % nx, "-DIMAGESIZE_Y=%d" % ny, "-DIMAGESIZE_M=%d" % (nx * ny),
         "-DDEPTHSIZE=%d" % max(nx, ny), "-DPRJ_IMAGESIZE=%d" % px, "-DPRJ_ANGLESIZE=%d" % pa,
-        "-DPRJ_IMAGESIZE_M=%d" % (px * pa), "-DSS=%d" % ss, "-DLAMBDA_FISTA=0.0001",
+        "-DPRJ_IMAGESIZE_M=%d" % (px * pa), "-DSS=%d" % ss, "-DLAMBDA_FISTA=0.0001", "-DZP_SIZE=%d" % zp,
     ]
     cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-shared", "-fPIC",
            "-w", "-o", so, cpp] + defs

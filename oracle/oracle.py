@@ -76,6 +76,9 @@ def lib():
             getattr(L, "xo_sino_correction" + sfx).argtypes = [p, p, fp, gp, ctypes.c_int]
             getattr(L, "xo_adjoint" + sfx).argtypes = [p, p, gp, p]
             getattr(L, "xo_osem_run" + sfx).argtypes = [p, p, p, gp, ip, ctypes.c_int, ctypes.c_int]
+        L.xo_fbp_filter_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp]
+        L.xo_fbp_filter_f64.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+        L.xo_base_up_f32.argtypes = [fp, ctypes.c_longlong, ctypes.c_int, fp]
         L.xo_trig_f32.argtypes = [fp, ctypes.c_int, fp]
         L.xo_trig_f64.argtypes = [fp, ctypes.c_int, dp]
         L.xo_subset_order.argtypes = [ctypes.c_int, ip]
@@ -194,6 +197,40 @@ def bp_fbp(fprj, angles_deg, nx, ny, cx=None, dtype=np.float32):
     return out
 
 
+def default_zp(px):
+    """Smallest power of two >= 2*px (4096 for 2048 bins, the reference's default g_zp)."""
+    zp = 1
+    while zp < 2 * px:
+        zp *= 2
+    return zp
+
+
+def fbp_filter(prj, zp=None, dtype=np.float32):
+    """Ramp-filtered sinogram of FBP_execution (rows [n][px]); float32 follows FBP.cl
+    literally, float64 is the exact-twiddle double transform."""
+    prj = np.ascontiguousarray(prj, dtype=dtype)
+    shape = prj.shape
+    px = shape[-1]
+    rows = int(np.prod(shape[:-1]))
+    zp = default_zp(px) if zp is None else int(zp)
+    out = np.empty_like(prj)
+    getattr(lib(), "xo_fbp_filter" + _sfx(dtype))(_p(prj), px, rows, zp, _p(out))
+    return out
+
+
+def fbp(meas, angles_deg, nx, ny, zp=None, cx=None):
+    """FBP_execution without sinogram correction: filter, then backProjectionFBP."""
+    return bp_fbp(fbp_filter(meas, zp), angles_deg, nx, ny, cx)
+
+
+def base_up(img, order):
+    """Hybrid base-up of one slice; returns (image, slice minimum)."""
+    out = np.array(img, dtype=np.float32, copy=True, order="C")
+    m = ctypes.c_float(0.0)
+    lib().xo_base_up_f32(_p(out), out.size, order, ctypes.byref(m))
+    return out, m.value
+
+
 def adjoint(sino, angles_deg, nx, ny, cx=None, dtype=np.float32):
     """Exact adjoint A^T of projection() over all angles."""
     sino = np.ascontiguousarray(sino, dtype=dtype)
@@ -235,16 +272,46 @@ def osem_run(img0, meas, angles_deg, ss, it, sub_order=None, cx=None, order=ORDE
 class RefKernels:
     """The reference's OSEM.cl/reconstShare.cl compiled for one shape (see build_ref.py)."""
 
-    def __init__(self, nx, ny, px, pa, ss):
+    def __init__(self, nx, ny, px, pa, ss, zp=None):
         import build_ref  # noqa: local module beside this file
         self.shape = (nx, ny, px, pa, ss)
-        self.lib = ctypes.CDLL(build_ref.build(nx, ny, px, pa, ss))
+        self.lib = ctypes.CDLL(build_ref.build(nx, ny, px, pa, ss, zp))
+        self.zp = self.lib.ref_zp_size()
         fp = ctypes.POINTER(ctypes.c_float)
         ip = ctypes.POINTER(ctypes.c_int)
         self.lib.ref_osem_execution.argtypes = [fp, fp, fp, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         self.lib.ref_projection.argtypes = [fp, fp, ctypes.c_int, fp]
         self.lib.ref_backprojection.argtypes = [fp, fp, ctypes.c_int, fp]
         self.lib.ref_sino_correction.argtypes = [fp, fp, ctypes.c_int, fp]
+        self.lib.ref_fbp.argtypes = [fp, fp, ctypes.c_int, fp, fp]
+        self.lib.ref_bp_fbp.argtypes = [fp, fp, ctypes.c_int, fp]
+        self.lib.ref_base_up.argtypes = [fp, ctypes.c_int, ctypes.c_int, fp]
+
+    def fbp(self, prjs, angles_deg):
+        """FBP_execution: returns (filtered sinograms, images), one per layer."""
+        nx, ny, px, pa, ss = self.shape
+        prjs = np.ascontiguousarray(prjs, dtype=np.float32)
+        dN = prjs.shape[0] if prjs.ndim == 3 else 1
+        fprj = np.zeros((dN, pa, px), dtype=np.float32)
+        img = np.zeros((dN, ny, nx), dtype=np.float32)
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        self.lib.ref_fbp(_p(prjs), _p(ang), dN, _p(fprj), _p(img))
+        return fprj.reshape(prjs.shape), img.reshape((ny, nx) if prjs.ndim == 2 else (dN, ny, nx))
+
+    def bp_fbp(self, fprj, angles_deg):
+        nx, ny, px, pa, ss = self.shape
+        out = np.zeros((ny, nx), dtype=np.float32)
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        self.lib.ref_bp_fbp(_p(np.ascontiguousarray(fprj, dtype=np.float32)), _p(ang), 1, _p(out))
+        return out
+
+    def base_up(self, imgs, order):
+        """Returns (images after base-up, per-layer minimum)."""
+        imgs = np.array(imgs, dtype=np.float32, copy=True, order="C")
+        dN = imgs.shape[0] if imgs.ndim == 3 else 1
+        mins = np.zeros(dN, dtype=np.float32)
+        self.lib.ref_base_up(_p(imgs), dN, order, _p(mins))
+        return imgs, mins
 
     def osem_execution(self, imgs, prjs, angles_deg, sub_order, it, fetch_mode=0):
         imgs = np.array(imgs, dtype=np.float32, copy=True, order="C")

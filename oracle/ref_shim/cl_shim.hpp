@@ -13,6 +13,7 @@
 #include <math.h>
 #include <stddef.h>
 #include <stdint.h>
+#include <string.h>
 
 #define __kernel
 #define kernel
@@ -26,7 +27,8 @@
 
 namespace clk {
 
-// ---- vector types (only what the kernels use: construction and .x/.y/.z/.w) ----
+// ---- vector types (only what the kernels use: construction, .x/.y/.z/.w, the float2
+// arithmetic and swizzles of FBP.cl, as_float2/as_uint2 bit casts) ----
 struct float4 {
     float x, y, z, w;
     float4() : x(0), y(0), z(0), w(0) {}
@@ -41,7 +43,40 @@ struct float2 {
     float x, y;
     float2() : x(0), y(0) {}
     float2(float a, float b) : x(a), y(b) {}
+    // swizzles: the build rewrites v.xx / v.yy / v.yx into these calls
+    float2 xx() const { return float2(x, x); }
+    float2 yy() const { return float2(y, y); }
+    float2 yx() const { return float2(y, x); }
+    float2 &operator*=(float s) { x *= s; y *= s; return *this; }
+    float2 &operator/=(float s) { x /= s; y /= s; return *this; }
+    float2 &operator+=(float2 o) { x += o.x; y += o.y; return *this; }
 };
+inline float2 operator+(float2 a, float2 b) { return float2(a.x + b.x, a.y + b.y); }
+inline float2 operator-(float2 a, float2 b) { return float2(a.x - b.x, a.y - b.y); }
+inline float2 operator*(float2 a, float2 b) { return float2(a.x * b.x, a.y * b.y); }
+inline float2 operator*(float s, float2 b) { return float2(s * b.x, s * b.y); }
+inline float2 operator-=(float2 &a, float2 b) { a = a - b; return a; }
+typedef unsigned int uint;
+struct uint2 {
+    uint x, y;
+    uint2() : x(0), y(0) {}
+    uint2(uint a, uint b) : x(a), y(b) {}
+};
+inline uint2 operator^(uint2 a, uint2 b) { return uint2(a.x ^ b.x, a.y ^ b.y); }
+inline uint2 as_uint2(float2 v)
+{
+    uint2 r;
+    memcpy(&r.x, &v.x, 4);
+    memcpy(&r.y, &v.y, 4);
+    return r;
+}
+inline float2 as_float2(uint2 v)
+{
+    float2 r;
+    memcpy(&r.x, &v.x, 4);
+    memcpy(&r.y, &v.y, 4);
+    return r;
+}
 struct int2 {
     int x, y;
     int2() : x(0), y(0) {}
@@ -136,6 +171,7 @@ inline float cos(float x) { return (float)::cos((double)x); }
 inline float sin(float x) { return (float)::sin((double)x); }
 inline double cos(double x) { return ::cos(x); }
 inline double sin(double x) { return ::sin(x); }
+inline float2 cos(float2 v) { return float2(cos(v.x), cos(v.y)); }
 inline float asin(float x) { return (float)::asin((double)x); }
 inline float exp(float x) { return (float)::exp((double)x); }
 inline float sqrt(float x) { return ::sqrtf(x); }

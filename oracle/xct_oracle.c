@@ -13,6 +13,9 @@
  *     (reconstShare.cl:213-275), AART1 (AART.cl:38-70), FISTAbackProjection
  *     (FISTA.cl:211-246), backProjectionFBP (FBP.cl:164-188)           -> xct_oracle_body.h
  *   - the subset/iteration loop of OSEM_execution (GPU.cpp:125-240)    -> xo_osem_run_*
+ *   - the FBP ramp filter chain of FBP_execution (GPU.cpp:745-806 over FBP.cl:34-160)
+ *                                                                       -> xo_fbp_filter_*
+ *   - the hybrid base-up (GPU.cpp:1538-1566, reconstShare.cl:87-177)   -> xo_base_up_f32
  *
  * Parity pin: the reference ships no tests, fixtures or golden vectors, and its OpenCL
  * runtime is not available, so the pin is oracle/_ref: the reference's own OSEM.cl and
@@ -107,3 +110,188 @@ int xo_subset_order(int ss, int *sub)
 }
 
 int xo_abi_version(void) { return XO_ABI_VERSION; }
+
+/* ---------------------------------------------------------------- FBP ramp filter
+ * FBP_execution (GPU.cpp:745-806) runs, per sinogram row th:
+ *   spinFactor  W[m] = (cos(d*m), cos(d*m + PI/2)) with d = 2*PI/ZP_SIZE stored to a float
+ *               (FBP.cl:34-40): d*m is a float product, d*m + PI_2 a double sum stored to
+ *               the float2 component, cos the float cos of that float;
+ *   zeroPadding bin X goes to Xswap = (X - px/2) mod zp, imaginary part 0 (FBP.cl:44-57);
+ *   bitReverse  xc2[rev(X)] = xc1[X], rev over log2(zp) bits (FBP.cl:60-79);
+ *   butterfly   passes i = 1..log2(zp), radix-2 decimation in time with twiddle W[l],
+ *               l = (zp >> i) * (X & (2^(i-1) - 1)) (FBP.cl:83-120);
+ *   filtering   xc[k] *= (k < zp/2 ? k : zp - k) * h, h = PI/zp stored to a float
+ *               (FBP.cl:125-134);
+ *   the inverse transform: bitReverse + butterflies with flag 0x80000000, which flips the
+ *               sign of W.y (FBP.cl:111), then normalization xc /= zp (FBP.cl:138-145);
+ *   outputImage fprj[X] = xc[Xswap].x (FBP.cl:149-160). */
+#define XO_PI_2 1.57079632679489661923
+
+static unsigned xo_bitrev(unsigned x, int bits)
+{
+    unsigned r = 0;
+    for (int b = 0; b < 32; ++b)
+        if (x & (1u << b)) r |= 1u << (31 - b);
+    return bits > 0 ? r >> (32 - bits) : 0u;
+}
+
+static int xo_log2(int n)
+{
+    int b = 0;
+    while ((1 << b) < n) ++b;
+    return b;
+}
+
+typedef struct { float x, y; } xo_c32;
+typedef struct { double x, y; } xo_c64;
+
+/* one radix-2 pass (FBP.cl:83-120) over xc[zp]; neg_wy: the inverse transform's flag */
+static void xo_butterfly_f32(xo_c32 *xc, const xo_c32 *W, int zp, int it, int neg_wy)
+{
+    const unsigned size = 1u << (it - 1), dist = 1u << it, num = (unsigned)zp >> it;
+    for (unsigned X = 0; X < (unsigned)zp / 2; ++X) {
+        const unsigned base = (X >> (it - 1)) * dist, off = X & (size - 1);
+        const unsigned a = base + off, b = a + size, l = num * off;
+        const xo_c32 xa = xc[a], xb = xc[b];
+        xo_c32 wab = W[l];
+        if (neg_wy) wab.y = -wab.y;
+        const xo_c32 wayx = {-wab.y, wab.x}, wbyx = {wab.y, -wab.x};
+        xo_c32 ra, rb;
+        ra.x = (xa.x + xb.x * wab.x) + xb.y * wayx.x;
+        ra.y = (xa.y + xb.x * wab.y) + xb.y * wayx.y;
+        rb.x = (xa.x - xb.x * wab.x) + xb.y * wbyx.x;
+        rb.y = (xa.y - xb.x * wab.y) + xb.y * wbyx.y;
+        xc[a] = ra;
+        xc[b] = rb;
+    }
+}
+
+void xo_fbp_filter_f32(const float *prj, int px, int nrows, int zp, float *out)
+{
+    const int bits = xo_log2(zp);
+    xo_c32 *W = (xo_c32 *)malloc(sizeof(xo_c32) * (size_t)zp);
+    const float d = (float)(2.0 * XO_PI / zp);
+    for (int m = 0; m < zp; ++m) {
+        const float dm = d * (float)m;
+        const float q = (float)((double)dm + XO_PI_2);
+        W[m].x = (float)cos((double)dm);
+        W[m].y = (float)cos((double)q);
+    }
+    const float h = (float)(XO_PI / zp);
+#pragma omp parallel
+    {
+        xo_c32 *x1 = (xo_c32 *)malloc(sizeof(xo_c32) * (size_t)zp);
+        xo_c32 *x2 = (xo_c32 *)malloc(sizeof(xo_c32) * (size_t)zp);
+#pragma omp for schedule(static)
+        for (int th = 0; th < nrows; ++th) {
+            memset(x1, 0, sizeof(xo_c32) * (size_t)zp);
+            for (int X = 0; X < px; ++X) {
+                const int xs = (X - px / 2 + zp / 2 < zp / 2) ? X - px / 2 + zp : X - px / 2;
+                x1[xs].x = prj[(size_t)th * px + X];
+                x1[xs].y = 0.0f;
+            }
+            for (int X = 0; X < zp; ++X) x2[xo_bitrev((unsigned)X, bits)] = x1[X];
+            for (int i = 1; i <= bits; ++i) xo_butterfly_f32(x2, W, zp, i, 0);
+            for (int k = 0; k < zp; ++k) {
+                const float f = (k < zp / 2) ? (float)k * h : (float)(zp - k) * h;
+                x2[k].x *= f;
+                x2[k].y *= f;
+            }
+            for (int X = 0; X < zp; ++X) x1[xo_bitrev((unsigned)X, bits)] = x2[X];
+            for (int i = 1; i <= bits; ++i) xo_butterfly_f32(x1, W, zp, i, 1);
+            for (int k = 0; k < zp; ++k) {
+                x1[k].x /= (float)zp;
+                x1[k].y /= (float)zp;
+            }
+            for (int X = 0; X < px; ++X) {
+                const int xs = (X - px / 2 + zp / 2 < zp / 2) ? X - px / 2 + zp : X - px / 2;
+                out[(size_t)th * px + X] = x1[xs].x;
+            }
+        }
+        free(x1);
+        free(x2);
+    }
+    free(W);
+}
+
+/* The same chain in double with W[m] = exp(-2 pi i m / zp) taken exactly. */
+void xo_fbp_filter_f64(const double *prj, int px, int nrows, int zp, double *out)
+{
+    const int bits = xo_log2(zp);
+    xo_c64 *W = (xo_c64 *)malloc(sizeof(xo_c64) * (size_t)zp);
+    for (int m = 0; m < zp; ++m) {
+        W[m].x = cos(2.0 * XO_PI * m / zp);
+        W[m].y = -sin(2.0 * XO_PI * m / zp);
+    }
+#pragma omp parallel
+    {
+        xo_c64 *x1 = (xo_c64 *)malloc(sizeof(xo_c64) * (size_t)zp);
+        xo_c64 *x2 = (xo_c64 *)malloc(sizeof(xo_c64) * (size_t)zp);
+#pragma omp for schedule(static)
+        for (int th = 0; th < nrows; ++th) {
+            memset(x1, 0, sizeof(xo_c64) * (size_t)zp);
+            for (int X = 0; X < px; ++X) {
+                const int xs = (X - px / 2 + zp / 2 < zp / 2) ? X - px / 2 + zp : X - px / 2;
+                x1[xs].x = prj[(size_t)th * px + X];
+            }
+            for (int X = 0; X < zp; ++X) x2[xo_bitrev((unsigned)X, bits)] = x1[X];
+            for (int pass = 0; pass < 2; ++pass) {
+                xo_c64 *xc = pass == 0 ? x2 : x1;
+                const double sgn = pass == 0 ? 1.0 : -1.0;
+                for (int it = 1; it <= bits; ++it) {
+                    const unsigned size = 1u << (it - 1), dist = 1u << it, num = (unsigned)zp >> it;
+                    for (unsigned X = 0; X < (unsigned)zp / 2; ++X) {
+                        const unsigned a = (X >> (it - 1)) * dist + (X & (size - 1)), b = a + size;
+                        const double wx = W[num * (X & (size - 1))].x, wy = sgn * W[num * (X & (size - 1))].y;
+                        const double tx = xc[b].x * wx - xc[b].y * wy, ty = xc[b].x * wy + xc[b].y * wx;
+                        const xo_c64 xa = xc[a];
+                        xc[a].x = xa.x + tx;
+                        xc[a].y = xa.y + ty;
+                        xc[b].x = xa.x - tx;
+                        xc[b].y = xa.y - ty;
+                    }
+                }
+                if (pass == 0) {
+                    for (int k = 0; k < zp; ++k) {
+                        const double f = (k < zp / 2 ? k : zp - k) * (XO_PI / zp);
+                        x2[k].x *= f;
+                        x2[k].y *= f;
+                    }
+                    for (int X = 0; X < zp; ++X) x1[xo_bitrev((unsigned)X, bits)] = x2[X];
+                }
+            }
+            for (int X = 0; X < px; ++X) {
+                const int xs = (X - px / 2 + zp / 2 < zp / 2) ? X - px / 2 + zp : X - px / 2;
+                out[(size_t)th * px + X] = x1[xs].x / zp;
+            }
+        }
+        free(x1);
+        free(x2);
+    }
+    free(W);
+}
+
+/* Hybrid base-up (hybrid_thread, GPU.cpp:1538-1566, FBPcorrection = 1): a = the slice
+ * minimum (findMinimumX/Y, reconstShare.cl:111-177), then per pixel (baseUp,
+ * reconstShare.cl:87-109) b1 = (v - a)/a (0 when a == 0), g = sum_{i=1..order}
+ * (-1)^(i+1) b1^i / i accumulated in float, v -= a * exp(g) with the float exp of g
+ * (taken correctly rounded). */
+void xo_base_up_f32(float *img, long long n, int order, float *min_out)
+{
+    float a = INFINITY;
+    for (long long i = 0; i < n; ++i) a = fminf(a, img[i]);
+    if (min_out) *min_out = a;
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n; ++i) {
+        const float v = img[i];
+        float g = 0.0f;
+        const float b1 = (a != 0.0f) ? (v - a) / a : 0.0f;
+        float b2 = 1.0f, flag = -1.0f;
+        for (int k = 1; k <= order; ++k) {
+            b2 *= b1;
+            flag *= -1.0f;
+            g += flag * b2 / (float)k;
+        }
+        img[i] = v - a * (float)exp((double)g);
+    }
+}

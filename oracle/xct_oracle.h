@@ -35,6 +35,15 @@ void xo_trig_f64(const float *ang_deg, int pa, double *cs);
 int xo_subset_order(int ss, int *sub);
 int xo_abi_version(void);
 
+/* FBP ramp filter of nrows sinogram rows [nrows][px] -> [nrows][px], zero padding zp
+ * (a power of two >= px).  _f32 follows FBP.cl's float evaluation literally; _f64 is the
+ * same transform in double with exact twiddles (the accuracy yardstick). */
+void xo_fbp_filter_f32(const float *prj, int px, int nrows, int zp, float *out);
+void xo_fbp_filter_f64(const double *prj, int px, int nrows, int zp, double *out);
+/* hybrid base-up on n pixels of one slice (reconstShare.cl:87-109 with the slice minimum);
+ * returns the minimum in *min_out when not NULL. */
+void xo_base_up_f32(float *img, long long n, int order, float *min_out);
+
 #define XO_DECL(T, S)                                                                                   \
     void xo_projection##S(const T *img, const T *cs, const xo_geom *g, int sub, int ss, int nrows, T *prj); \
     void xo_osem1##S(const T *img, const T *meas, const T *cs, const xo_geom *g, int sub, int nrows,      \

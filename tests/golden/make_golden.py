@@ -16,6 +16,11 @@ Fixtures (np.savez_compressed):
                  backProjection kernels on their own.
   odd_48x40.npz  48x40 image, 56 bins, 36 angles, 4 subsets (power of two: bit-reversed
                  order) x 3 iterations: non-square image, px != nx.
+  fbp_64.npz     FBP (FBP.cl) of a 64x64 slice, 90 angles, 64 bins, zero padding 128: the
+                 filtered sinogram, the image, the base-up image (order 4) and the hybrid
+                 (FBP + base-up + 10 subsets x 2 iterations of OS-EM).
+  fbp_odd.npz    the same for a 48x40 image, 57 bins, 37 angles (odd: the GPU filter pairs
+                 rows across the end of a slice), zero padding 256, 1 subset x 2 iterations.
 """
 import os
 import sys
@@ -65,8 +70,41 @@ def case(name, nx, ny, px, pa, ss, it, n_ell, seed, i0, noise_seed):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
 
 
+def fbp_case(name, nx, ny, px, pa, zp, ss, it, order, n_ell, seed, i0, noise_seed):
+    m = max(nx, ny)
+    img = P.rasterize_ellipses(P.ellipse_params(m, n_ell, seed, axes=(3, m / 4)), m, m)
+    img = np.ascontiguousarray(img[(m - ny) // 2:(m - ny) // 2 + ny, (m - nx) // 2:(m - nx) // 2 + nx])
+    ang = P.uniform_angles(pa)
+    meas = P.noisy_log_sinogram(O.projection(img, ang, px, order=LIT), i0, noise_seed)
+    fprj = O.fbp_filter(meas, zp)
+    fbp = O.bp_fbp(fprj, ang, nx, ny)
+    based, amin = O.base_up(fbp, order)
+    sub = O.subset_order(ss)
+    hybrid = O.osem_run(based, meas, ang, ss, it, sub_order=sub, order=LIT)
+    arrays = dict(phantom=img, angles=ang, meas=meas, fprj=fprj, fbp=fbp, base_up=based,
+                  minimum=np.array([amin], np.float32), sub=sub, hybrid=hybrid,
+                  fprj_f64=O.fbp_filter(meas.astype(np.float64), zp, dtype=np.float64),
+                  shape=np.array([nx, ny, px, pa, ss, it, zp, order], np.int32))
+    if O.ref_available():
+        ref = O.RefKernels(nx, ny, px, pa, ss, zp)
+        r_fprj, r_img = ref.fbp(meas, ang)
+        assert np.array_equal(r_fprj, fprj), name + ": filtered sinogram differs from FBP.cl"
+        assert np.array_equal(r_img, fbp), name + ": FBP image differs from FBP.cl"
+        r_based, r_min = ref.base_up(r_img, order)
+        assert np.array_equal(r_based, based) and r_min[0] == amin, name + ": base-up differs"
+        r_hyb = ref.osem_execution(r_based[None], meas[None], ang, sub, it)[0]
+        assert np.array_equal(r_hyb, hybrid), name + ": hybrid OS-EM differs"
+        arrays["pinned_by_reference_kernels"] = np.array([1], np.int32)
+        print(name, "pinned: bit-identical to the reference kernels")
+    else:
+        arrays["pinned_by_reference_kernels"] = np.array([0], np.int32)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+
+
 if __name__ == "__main__":
     O.build()
     case("small_64", 64, 64, 64, 90, 10, 2, 10, 1, 1e5, 11)
     case("odd_48x40", 48, 40, 56, 36, 4, 3, 6, 5, 1e5, 12)
     case("cfg1_256", 256, 256, 256, 180, 10, 5, 10, 1, 1e5, 11)
+    fbp_case("fbp_64", 64, 64, 64, 90, 128, 10, 2, 4, 8, 3, 1e5, 13)
+    fbp_case("fbp_odd", 48, 40, 57, 37, 256, 1, 2, 4, 6, 7, 1e5, 14)
