@@ -144,6 +144,9 @@ static void plan_free(xct_plan *p)
     cudaFree(p->d_corr_bin);
     cudaFree(p->d_acc);
     cudaFree(p->d_min_keys);
+    cudaFree(p->d_red);
+    cudaFree(p->d_rc_prm);
+    cudaFree(p->d_fi);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -223,6 +226,11 @@ int xct_osem_plan_create(xct_ctx *ctx, const xct_geom *geom, xct_plan **out)
     if ((e = cudaMalloc(&p->d_img, sizeof(float) * nb * nimg)) != cudaSuccess) return fail(e, "cudaMalloc img");
     if ((e = cudaMalloc(&p->d_ratio, sizeof(float) * nb * nprj)) != cudaSuccess) return fail(e, "cudaMalloc ratio");
     if ((e = cudaMalloc(&p->d_min_keys, sizeof(int) * nb)) != cudaSuccess) return fail(e, "cudaMalloc min keys");
+    if ((e = cudaMalloc(&p->d_red, sizeof(double) * 2 * nb)) != cudaSuccess) return fail(e, "cudaMalloc red");
+    if ((e = cudaMemsetAsync(p->d_red, 0, sizeof(double) * 2 * nb, p->stream)) != cudaSuccess)
+        return fail(e, "memset red");
+    if ((e = cudaMalloc(&p->d_rc_prm, sizeof(float) * 16 * nb)) != cudaSuccess) return fail(e, "cudaMalloc prm");
+    if ((e = cudaMalloc(&p->d_fi, sizeof(float) * nb)) != cudaSuccess) return fail(e, "cudaMalloc findex");
     if ((e = cudaMemsetAsync(p->d_ratio, 0, sizeof(float) * nb * nprj, p->stream)) != cudaSuccess)
         return fail(e, "memset ratio");
     if (geom->kernels == XCT_KERNELS_TILED) {
@@ -635,6 +643,98 @@ int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *c
     return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
         return hybrid_device(p, dN, zp, baseup_order, p->d_sino, p->d_img, sub, it, st);
     });
+}
+
+// ------------------------------------------------------------ rotation-centre search
+static int check_shifts(int n, float start, float step)
+{
+    if (n <= 0) return xct_fail(XCT_E_INVALID, "rotation-centre search: n must be > 0");
+    if (!(fabsf(start) < 1.0e6f) || !(fabsf(step) < 1.0e6f) || !(fabsf(start) + fabsf(step) * (float)n < 1.0e6f))
+        return xct_fail(XCT_E_INVALID, "rotation-centre search: shifts must be finite and below 1e6 bins");
+    return XCT_OK;
+}
+
+int xct_rot_center_shift(xct_plan *p, int n, float shift_start, float shift_step, const float *d_sino,
+                         float *d_shifted, void *stream)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "plan is null");
+    int rc = check_shifts(n, shift_start, shift_step);
+    if (rc) return rc;
+    if (!d_sino || !d_shifted) return xct_fail(XCT_E_INVALID, "xct_rot_center_shift: null device pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return launch_rot_shift(d_sino, d_shifted, p->g.px, p->g.pa, n, 0, shift_start, shift_step, p->ctx->sm_count,
+                            (cudaStream_t)stream);
+}
+
+// Focus indices of images [off, off + c) of a shift sequence into d_findex (device).
+static int focus_chunk(xct_plan *p, const float *d_imgs, int off, int c, float start, float step, float ang_ini,
+                       float ang_fin, float *d_findex, cudaStream_t st)
+{
+    std::vector<float> prm(16 * (size_t)c);
+    for (int i = 0; i < c; ++i)
+        xct_mask_params(p->g.nx, p->g.ny, xct_shift_value(start, step, off + i), ang_ini, ang_fin, &prm[16 * i]);
+    XCT_CUDA_TRY(cudaMemcpyAsync(p->d_rc_prm, prm.data(), sizeof(float) * prm.size(), cudaMemcpyHostToDevice, st));
+    return launch_focus_index(d_imgs, p->g.nx, p->g.ny, c, p->d_rc_prm, p->d_red, d_findex, st);
+}
+
+int xct_focus_index(xct_plan *p, int n, int shift_offset, float shift_start, float shift_step, float ang_ini_deg,
+                    float ang_fin_deg, const float *d_imgs, float *d_findex, void *stream)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "plan is null");
+    int rc = check_shifts(n + std::max(shift_offset, 0), shift_start, shift_step);
+    if (rc) return rc;
+    if (shift_offset < 0) return xct_fail(XCT_E_INVALID, "xct_focus_index: shift_offset must be >= 0");
+    if (!d_imgs || !d_findex) return xct_fail(XCT_E_INVALID, "xct_focus_index: null device pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t nimg = (size_t)p->g.nx * p->g.ny;
+    for (int off = 0; off < n; off += p->g.max_batch) {
+        const int c = std::min(p->g.max_batch, n - off);
+        rc = focus_chunk(p, d_imgs + off * nimg, shift_offset + off, c, shift_start, shift_step, ang_ini_deg,
+                         ang_fin_deg, d_findex + off, st);
+        if (rc) return rc;
+    }
+    return XCT_OK;
+}
+
+// rotationCenterSearch (rotationCenterSearch_ocl.cpp:419-540) from the resliced sinogram on:
+// per batch of max_batch shifts, rotCenterShift, a uniform initial image (g_ini), one OS-EM
+// iteration with the plan's subsets and sinogram correction (OSEM_execution(..., 1, true),
+// :307), and the focus index; the estimate is the first shift with the smallest index
+// (:505-513).
+int xct_rot_center_search(xct_plan *p, int n, float shift_start, float shift_step, float ang_ini_deg,
+                          float ang_fin_deg, float init_value, const float *d_sino, float *d_imgs, float *findex,
+                          int *best, void *stream)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "plan is null");
+    int rc = check_shifts(n, shift_start, shift_step);
+    if (rc) return rc;
+    if (!d_sino || !d_imgs || !findex || !best) return xct_fail(XCT_E_INVALID, "xct_rot_center_search: null argument");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t nimg = (size_t)p->g.nx * p->g.ny;
+    for (int off = 0; off < n; off += p->g.max_batch) {
+        const int c = std::min(p->g.max_batch, n - off);
+        float *imgs = d_imgs + off * nimg;
+        if ((rc = launch_rot_shift(d_sino, p->d_sino, p->g.px, p->g.pa, c, off, shift_start, shift_step,
+                                   p->ctx->sm_count, st)))
+            return rc;
+        if ((rc = launch_fill(imgs, (long long)c * nimg, init_value, p->ctx->sm_count, st))) return rc;
+        if ((rc = osem_loop(p, c, p->d_sino, imgs, p->sub_default.data(), 1, st))) return rc;
+        if ((rc = focus_chunk(p, imgs, off, c, shift_start, shift_step, ang_ini_deg, ang_fin_deg, p->d_fi, st)))
+            return rc;
+        XCT_CUDA_TRY(cudaMemcpyAsync(findex + off, p->d_fi, sizeof(float) * c, cudaMemcpyDeviceToHost, st));
+    }
+    XCT_CUDA_TRY(cudaStreamSynchronize(st));
+    float m = 3.402823466e38f;
+    int b = 0;
+    for (int i = 0; i < n; ++i)
+        if (m > findex[i]) {
+            m = findex[i];
+            b = i;
+        }
+    *best = b;
+    return XCT_OK;
 }
 
 int xct_plan_sync(xct_plan *p)

@@ -55,6 +55,9 @@ struct xct_plan {
     float *d_corr_bin = nullptr; // [px] per-bin correction factors
     double *d_acc = nullptr;     // tiled forward: ray-sum accumulator [max_batch][acc_rows][px]
     int *d_min_keys = nullptr;   // [max_batch] per-slice image minimum (FBP + OS-EM hybrid)
+    double *d_red = nullptr;     // [2*max_batch] focus-index sums (rotation-centre search)
+    float *d_rc_prm = nullptr;   // [max_batch][16] mask constants per shift
+    float *d_fi = nullptr;       // [max_batch] focus indices
     int acc_rows = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -124,6 +127,14 @@ int launch_fbp_bp(const KGeom &g, const float2 *trig, const float *fprj, float *
 // baseUp (reconstShare.cl:87-109) with the slice minima of launch_fbp_bp, in place.
 int launch_base_up(const KGeom &g, float *img, int dN, int order, const int *min_keys, int sm_count,
                    cudaStream_t st);
+// Rotation-centre search (xct_rcs.cu).
+void xct_mask_params(int W, int H, float shift, float ang_min, float ang_max, float *prm16);
+float xct_shift_value(float start, float step, int i);
+int launch_rot_shift(const float *prj, float *out, int px, int pa, int n, int i0, float start, float step,
+                     int sm_count, cudaStream_t st);
+int launch_fill(float *p, long long n, float v, int sm_count, cudaStream_t st);
+int launch_focus_index(const float *imgs, int nx, int ny, int n, const float *d_prm, double *red, float *findex,
+                       cudaStream_t st);
 // sinogramCorrection (reconstShare.cl:35-70), modes 1..4, src -> dst.
 int launch_sino_correction(const KGeom &g, const float *src, float *dst, const float *ang_fac, const float *bin_fac,
                            int mode, int dN, cudaStream_t st);

@@ -7,7 +7,9 @@
 // :99-123) -- fed round-robin with batches [N, N+dN-1] by the dispatcher of OSEM_ocl
 // (:562-663).  The OpenCL context/queue/program/image objects are replaced by one libxct
 // context and plan per device; the reconstruction thread calls xct_osem_run, which does the
-// host<->device copies and the whole subset/iteration loop on the device.
+// host<->device copies and the whole subset/iteration loop on the device.  The FBP (FBP_ocl,
+// GPU.cpp:997-1090) and FBP + OS-EM hybrid (hybrid_ocl, :1605-1700) drivers have the same
+// pipeline shape; their reconstruction step is xct_fbp_run / xct_hybrid_run.
 #include <sys/stat.h>
 #include <time.h>
 
@@ -29,6 +31,8 @@ struct DeviceSlot {
     std::thread input_th, reconst_th, output_th;
 };
 
+enum Method { METHOD_OSEM, METHOD_FBP, METHOD_HYBRID };
+Method g_method = METHOD_OSEM;
 std::vector<int> g_sub;           // subset order (GPU.cpp:564-582)
 std::atomic<int> g_status{0};     // first failure (the reference exits on the spot)
 time_t g_t0 = 0;
@@ -59,11 +63,16 @@ void output_thread(int startN, int endN, std::vector<float *> imgs, bool ok)
     for (float *p : imgs) delete[] p;
 }
 
-// OSEM_thread (GPU.cpp:408-476): reconstruct the batch, hand the images to the output stage.
+// OSEM_thread (GPU.cpp:408-476) / FBP_thread (:822-893) / hybrid_thread (:1458-1600):
+// reconstruct the batch, hand the images to the output stage.
 void osem_thread(DeviceSlot *d, std::vector<float *> imgs, std::vector<float *> prjs, int startN, int endN)
 {
     const int dN = endN - startN + 1;
-    const int rc = xct_osem_run(d->plan, dN, prjs.data(), imgs.data(), g_sub.data(), g_it);
+    int rc;
+    if (g_method == METHOD_FBP) rc = xct_fbp_run(d->plan, dN, g_zp, prjs.data(), imgs.data());
+    else if (g_method == METHOD_HYBRID)
+        rc = xct_hybrid_run(d->plan, dN, g_zp, baseupOrder, prjs.data(), imgs.data(), g_sub.data(), g_it);
+    else rc = xct_osem_run(d->plan, dN, prjs.data(), imgs.data(), g_sub.data(), g_it);
     if (rc != XCT_OK) {
         std::cerr << "ERROR: " << xct_last_error() << " (" << rc << ")" << std::endl;
         fail(rc);
@@ -82,7 +91,8 @@ void osem_input_thread(DeviceSlot *d, int startN, int endN)
         prjs.push_back(new float[(size_t)g_px * g_pa]);
         imgs.push_back(new float[(size_t)g_ox * g_oy]);
         ok = ok && read_data_input(g_d1, slice_name(g_f1, i), prjs.back(), (size_t)g_px * g_pa);
-        ok = ok && first_image(g_f4, imgs.back(), (size_t)g_ox * g_oy);
+        // FBP and the hybrid overwrite every pixel: no initial image to read
+        if (g_method == METHOD_OSEM) ok = ok && first_image(g_f4, imgs.back(), (size_t)g_ox * g_oy);
     }
     join(d->reconst_th);
     if (!ok) {
@@ -96,9 +106,13 @@ void osem_input_thread(DeviceSlot *d, int startN, int endN)
 
 }  // namespace
 
-// OSEM_ocl (GPU.cpp:562-663) on libxct: one context + plan per device, round-robin batches.
-int OSEM_gpu(const std::vector<int> &devices, const std::vector<float> &ang, int ss)
+namespace {
+
+// OSEM_ocl (GPU.cpp:562-663) on libxct: one context + plan per device, round-robin batches
+// (FBP_ocl and hybrid_ocl dispatch the same way).
+int run_pipeline(const std::vector<int> &devices, const std::vector<float> &ang, int ss, Method method)
 {
+    g_method = method;
     if (devices.empty()) {
         std::cerr << "ERROR: no usable CUDA device in the device list \"" << g_devList << "\"" << std::endl;
         return XCT_E_INVALID;
@@ -163,6 +177,13 @@ int OSEM_gpu(const std::vector<int> &devices, const std::vector<float> &ang, int
     return g_status.load();
 }
 
+}  // namespace
+
+int OSEM_gpu(const std::vector<int> &devices, const std::vector<float> &ang, int ss)
+{
+    return run_pipeline(devices, ang, ss, METHOD_OSEM);
+}
+
 // GPU() (GPU.cpp:23-97): the OS-EM-family modes of the reference.
 int GPU()
 {
@@ -194,9 +215,15 @@ int GPU()
     case 6:
         std::cout << "Processing by OS-EM method" << std::endl << std::endl;
         return OSEM_gpu(devices, g_ang, g_ss);
+    case 7:
+        std::cout << "Processing by FBP method" << std::endl << std::endl;
+        return run_pipeline(devices, g_ang, 1, METHOD_FBP);
+    case 8:
+        std::cout << "Processing by FBP+OS-EM hybrid method" << std::endl << std::endl;
+        return run_pipeline(devices, g_ang, g_ss, METHOD_HYBRID);
     default:
         std::cerr << "ERROR: reconstruction method " << g_mode
-                  << " is not part of this build (OS-EM family: 2, 4, 5, 6)" << std::endl;
+                  << " is not part of this build (OS-EM family 2, 4, 5, 6; FBP 7; hybrid 8)" << std::endl;
         return XCT_E_UNSUPPORTED;
     }
 }

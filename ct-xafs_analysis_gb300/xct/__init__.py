@@ -48,7 +48,7 @@ EXPORTS = (
     "xct_osem_profile", "xct_fp32_peak", "xct_osem1", "xct_osem2", "xct_osem_run_static",
     "xct_batch_plan_create", "xct_batch_run", "xct_batch_plan_destroy", "xct_osem_run_batched",
     "xct_fbp_filter", "xct_fbp_backproject", "xct_fbp_run_device", "xct_hybrid_run_device", "xct_fbp_run",
-    "xct_hybrid_run",
+    "xct_hybrid_run", "xct_rot_center_shift", "xct_focus_index", "xct_rot_center_search",
 )
 
 
@@ -114,6 +114,11 @@ def load():
     L.xct_fbp_run.argtypes = [vp, ip, ip, ctypes.POINTER(fp), ctypes.POINTER(fp)]
     L.xct_hybrid_run.argtypes = [vp, ip, ip, ip, ctypes.POINTER(fp), ctypes.POINTER(fp),
                                  ctypes.POINTER(ctypes.c_int), ip]
+    c_f = ctypes.c_float
+    L.xct_rot_center_shift.argtypes = [vp, ip, c_f, c_f, vp, vp, vp]
+    L.xct_focus_index.argtypes = [vp, ip, ip, c_f, c_f, c_f, c_f, vp, vp, vp]
+    L.xct_rot_center_search.argtypes = [vp, ip, c_f, c_f, c_f, c_f, c_f, vp, vp, fp, ctypes.POINTER(ctypes.c_int),
+                                        vp]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong
@@ -325,6 +330,34 @@ class OSEMPlan:
         dN = d_img.shape[0] if dN is None else dN
         _check(self._lib.xct_hybrid_run_device(self.handle, dN, zp, baseup_order, _ptr(d_sino), _ptr(d_img),
                                                self._sub(sub), it, _stream(stream)))
+
+    # ---- rotation-centre search ---------------------------------------------------------
+    def rot_center_shift(self, d_sino, d_shifted, start, step, n=None, stream=None):
+        """rotCenterShift of one sinogram [pa][px] for shifts start + step*i -> [n][pa][px]."""
+        n = d_shifted.shape[0] if n is None else n
+        _check(self._lib.xct_rot_center_shift(self.handle, n, start, step, _ptr(d_sino), _ptr(d_shifted),
+                                              _stream(stream)))
+
+    def focus_index(self, d_imgs, d_findex, start, step, ang_ini, ang_fin, offset=0, n=None, stream=None):
+        """setMask + imgFocusIndex of images [n][ny][nx] -> d_findex [n] (device)."""
+        n = d_imgs.shape[0] if n is None else n
+        _check(self._lib.xct_focus_index(self.handle, n, offset, start, step, ang_ini, ang_fin, _ptr(d_imgs),
+                                         _ptr(d_findex), _stream(stream)))
+
+    def rot_center_search(self, d_sino, d_imgs, start, step, ang_ini=None, ang_fin=None, init_value=1.0, n=None,
+                          stream=None):
+        """The whole search; returns (focus indices [n] (numpy), index of the best shift).
+        ang_ini/ang_fin default to the plan's first and last angle."""
+        n = d_imgs.shape[0] if n is None else n
+        ang_ini = float(self.angles[0]) if ang_ini is None else ang_ini
+        ang_fin = float(self.angles[-1]) if ang_fin is None else ang_fin
+        fi = np.zeros(n, np.float32)
+        best = ctypes.c_int(-1)
+        _check(self._lib.xct_rot_center_search(self.handle, n, start, step, ang_ini, ang_fin, init_value,
+                                               _ptr(d_sino), _ptr(d_imgs),
+                                               fi.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(best),
+                                               _stream(stream)))
+        return fi, best.value
 
     def profile(self, d_sino, d_img, dN=None, sub=None, it=-1, stream=None):
         """Run OS-EM with CUDA events around every launch; returns a dict of summed device

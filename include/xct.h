@@ -187,6 +187,34 @@ int xct_fbp_run(xct_plan *plan, int dN, int zp, const float *const *sino_host, f
 int xct_hybrid_run(xct_plan *plan, int dN, int zp, int baseup_order, const float *const *sino_host,
                    float *const *img_host, const int *sub, int it);
 
+/* ---- rotation-centre search (RotationCenterSearch/rotationCenterSearch_ocl.cpp) ------
+ * Shifts are s_i = shift_start + shift_step * i (float, :140), i < n; a positive shift
+ * samples the sinogram at X + s (the rotation centre moves to px/2 + s).
+ * xct_rot_center_shift : rotCenterShift (rotCenterSearch.cl:37-49) of one sinogram
+ *                        d_sino [pa][px] for every shift -> d_shifted [n][pa][px].
+ * xct_focus_index      : setMask + imgFocusIndex (rotCenterSearch.cl:51-97, 167-232) of
+ *                        images d_imgs [n][ny][nx] reconstructed for shifts
+ *                        shift_offset .. shift_offset + n - 1 -> d_findex [n] (device):
+ *                        sqrt(sum of the relative squared 8-neighbour differences / pixels)
+ *                        over the pixels whose 3x3 neighbourhood lies in the shift's mask;
+ *                        ang_ini_deg / ang_fin_deg are the first and last projection angles.
+ *                        The mask and the sums use the plan's nx, ny (the reference builds
+ *                        these kernels without size options: 2048 x 2048).
+ * xct_rot_center_search: rotationCenterSearch from the resliced sinogram on (:419-540): per
+ *                        shift, the shifted sinogram, an image filled with init_value
+ *                        (g_ini), ONE OS-EM iteration with the plan's subsets and sinogram
+ *                        correction (:307), the focus index.  d_imgs [n][ny][nx] receives the
+ *                        reconstructions, findex (HOST, [n]) the indices, *best the first
+ *                        shift index with the smallest one (:505-513).  Batches of max_batch
+ *                        shifts; uses the plan's staging and ratio buffers.  Blocking. */
+int xct_rot_center_shift(xct_plan *plan, int n, float shift_start, float shift_step, const float *d_sino,
+                         float *d_shifted, void *stream);
+int xct_focus_index(xct_plan *plan, int n, int shift_offset, float shift_start, float shift_step, float ang_ini_deg,
+                    float ang_fin_deg, const float *d_imgs, float *d_findex, void *stream);
+int xct_rot_center_search(xct_plan *plan, int n, float shift_start, float shift_step, float ang_ini_deg,
+                          float ang_fin_deg, float init_value, const float *d_sino, float *d_imgs, float *findex,
+                          int *best, void *stream);
+
 /* Tracing: xct_osem_run_device with CUDA events around every launch.  The reference
  * enables CL_QUEUE_PROFILING_ENABLE but never reads the events
  * (share source/OCL_platform_device_class.cpp:175-178).  ms[0..3] = summed device time of

@@ -91,3 +91,42 @@ if __name__ == "__main__":
     import sys
     shape = [int(v) for v in sys.argv[1:6]] if len(sys.argv) >= 6 else [64, 64, 64, 90, 10]
     print(build(*shape))
+
+
+RCS_KERNEL = "RotationCenterSearch/rotCenterSearch.cl"
+
+
+def rcs_available():
+    return os.path.isfile(os.path.join(REF_ROOT, RCS_KERNEL))
+
+
+def build_rcs(width, height, force=False):
+    """Compile RotationCenterSearch/rotCenterSearch.cl for one image size (the -D size
+    macros the reference leaves at their 2048 defaults); return the .so path."""
+    if not rcs_available():
+        raise FileNotFoundError("reference kernel sources not found under %s" % REF_ROOT)
+    os.makedirs(OUT, exist_ok=True)
+    parts = ['#include "%s"' % os.path.join(HERE, "ref_shim", "cl_shim.hpp"), "namespace clk {"]
+    with open(os.path.join(REF_ROOT, RCS_KERNEL), encoding="utf-8") as f:
+        parts.append("// ---- %s (vector literals rewritten) ----" % RCS_KERNEL)
+        parts.append(_rewrite(f.read()))
+    parts.append("}  // namespace clk")
+    parts.append('#include "%s"' % os.path.join(HERE, "ref_shim", "rcs_driver.inc"))
+    src = "\n".join(parts) + "\n"
+    tag = "%dx%d" % (width, height)
+    h = hashlib.sha1(src.encode())
+    for dep in ("cl_shim.hpp", "rcs_driver.inc"):
+        with open(os.path.join(HERE, "ref_shim", dep), "rb") as f:
+            h.update(f.read())
+    digest = h.hexdigest()[:10]
+    cpp = os.path.join(OUT, "rcs_kernels_%s.cpp" % tag)
+    so = os.path.join(OUT, "librcs_%s_%s.so" % (tag, digest))
+    if os.path.exists(so) and not force:
+        return so
+    with open(cpp, "w") as f:
+        f.write(src)
+    defs = ["-DIMAGESIZE_X=%d" % width, "-DIMAGESIZE_Y=%d" % height, "-DIMAGESIZE_M=%d" % (width * height)]
+    cmd = ["g++", "-std=c++17", "-O2", "-pthread", "-ffp-contract=off", "-Wno-narrowing", "-shared", "-fPIC",
+           "-w", "-o", so, cpp] + defs
+    subprocess.run(cmd, check=True)
+    return so

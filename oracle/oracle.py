@@ -79,6 +79,12 @@ def lib():
         L.xo_fbp_filter_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp]
         L.xo_fbp_filter_f64.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
         L.xo_base_up_f32.argtypes = [fp, ctypes.c_longlong, ctypes.c_int, fp]
+        L.xo_rot_center_shift_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp]
+        L.xo_mask_params_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_float, fp]
+        L.xo_set_mask_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, fp]
+        L.xo_focus_index.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.xo_focus_index.restype = ctypes.c_double
         L.xo_trig_f32.argtypes = [fp, ctypes.c_int, fp]
         L.xo_trig_f64.argtypes = [fp, ctypes.c_int, dp]
         L.xo_subset_order.argtypes = [ctypes.c_int, ip]
@@ -231,6 +237,43 @@ def base_up(img, order):
     return out, m.value
 
 
+def shift_values(start, step, n):
+    """The shifts start + step*i of rotationCenterSearch_ocl.cpp:140, in float."""
+    return [float(np.float32(np.float32(start) + np.float32(step) * np.float32(i))) for i in range(n)]
+
+
+def rot_center_shift(prj, shift):
+    """rotCenterShift (rotCenterSearch.cl:37-49) of one sinogram [pa][px]."""
+    prj = np.ascontiguousarray(prj, dtype=np.float32)
+    pa, px = prj.shape
+    out = np.empty_like(prj)
+    lib().xo_rot_center_shift_f32(_p(prj), px, pa, shift, _p(out))
+    return out
+
+
+def mask_params(W, H, shift, ang_min, ang_max):
+    prm = np.zeros(13, np.float32)
+    lib().xo_mask_params_f32(W, H, shift, ang_min, ang_max, _p(prm))
+    return prm
+
+
+def set_mask(W, H, shift, ang_min, ang_max, w_visit=None):
+    """setMask (rotCenterSearch.cl:51-97) for one shift: a [H][W] 0/1 mask."""
+    prm = mask_params(W, H, shift, ang_min, ang_max)
+    out = np.zeros((H, W), np.float32)
+    lib().xo_set_mask_f32(W, H, W if w_visit is None else w_visit, _p(prm), _p(out))
+    return out
+
+
+def focus_index(img, mask, L=0):
+    """imgFocusIndex (rotCenterSearch.cl:167-232): literal float order of a work-group of L
+    items, or (L = 0) double sums over every pixel."""
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    mask = np.ascontiguousarray(mask, dtype=np.float32)
+    H, W = img.shape
+    return lib().xo_focus_index(_p(img), _p(mask), W, H, int(L))
+
+
 def adjoint(sino, angles_deg, nx, ny, cx=None, dtype=np.float32):
     """Exact adjoint A^T of projection() over all angles."""
     sino = np.ascontiguousarray(sino, dtype=dtype)
@@ -342,6 +385,41 @@ class RefKernels:
         ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
         self.lib.ref_backprojection(_p(np.ascontiguousarray(prj, dtype=np.float32)), _p(ang), sub, _p(out))
         return out
+
+
+class RefRotCenter:
+    """The reference's rotCenterSearch.cl compiled for one image size (build_ref.build_rcs)."""
+
+    def __init__(self, width, height):
+        import build_ref  # noqa: local module beside this file
+        self.shape = (width, height)
+        self.lib = ctypes.CDLL(build_ref.build_rcs(width, height))
+        fp = ctypes.POINTER(ctypes.c_float)
+        c_i, c_f = ctypes.c_int, ctypes.c_float
+        self.lib.rcs_rot_center_shift.argtypes = [fp, c_i, c_i, c_i, c_f, c_f, fp]
+        self.lib.rcs_focus_index.argtypes = [fp, c_i, c_i, c_i, c_f, c_f, c_f, c_f, fp, fp]
+
+    def rot_center_shift(self, prj, n, start, step):
+        prj = np.ascontiguousarray(prj, dtype=np.float32)
+        pa, px = prj.shape
+        out = np.zeros((n, pa, px), np.float32)
+        self.lib.rcs_rot_center_shift(_p(prj), px, pa, n, start, step, _p(out))
+        return out
+
+    def focus_index(self, imgs, L, start, step, ang_ini, ang_fin, offsetN=0):
+        """Returns (masks [n][H][W], findex [n])."""
+        imgs = np.ascontiguousarray(imgs, dtype=np.float32)
+        n = imgs.shape[0]
+        W, H = self.shape
+        masks = np.zeros((n, H, W), np.float32)
+        fi = np.zeros(n, np.float32)
+        self.lib.rcs_focus_index(_p(imgs), n, L, offsetN, start, step, ang_ini, ang_fin, _p(masks), _p(fi))
+        return masks, fi
+
+
+def rcs_available():
+    import build_ref
+    return build_ref.rcs_available()
 
 
 def ref_available():

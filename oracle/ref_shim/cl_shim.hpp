@@ -55,7 +55,11 @@ inline float2 operator+(float2 a, float2 b) { return float2(a.x + b.x, a.y + b.y
 inline float2 operator-(float2 a, float2 b) { return float2(a.x - b.x, a.y - b.y); }
 inline float2 operator*(float2 a, float2 b) { return float2(a.x * b.x, a.y * b.y); }
 inline float2 operator*(float s, float2 b) { return float2(s * b.x, s * b.y); }
-inline float2 operator-=(float2 &a, float2 b) { a = a - b; return a; }
+inline float2 &operator-=(float2 &a, float2 b)
+{
+    a = float2(a.x - b.x, a.y - b.y);
+    return a;
+}
 typedef unsigned int uint;
 struct uint2 {
     uint x, y;
@@ -161,10 +165,18 @@ inline void write_imagef(image2d_t im, int2 c, float4 v)
 extern thread_local size_t g_gid[3];
 extern thread_local size_t g_lid[3];
 extern thread_local size_t g_lsz[3];
+extern thread_local size_t g_grp[3];
+// Drivers that run a work-group as one host thread per work-item install a real barrier
+// here; kernels driven one work-item at a time have none and need none.
+extern thread_local void (*g_barrier_fn)(void);
 inline size_t get_global_id(int d) { return g_gid[d]; }
 inline size_t get_local_id(int d) { return g_lid[d]; }
 inline size_t get_local_size(int d) { return g_lsz[d]; }
-inline void barrier(int) {}
+inline size_t get_group_id(int d) { return g_grp[d]; }
+inline void barrier(int)
+{
+    if (g_barrier_fn) g_barrier_fn();
+}
 
 // ---- math builtins (float overloads as in OpenCL C) ----
 inline float cos(float x) { return (float)::cos((double)x); }
@@ -172,6 +184,7 @@ inline float sin(float x) { return (float)::sin((double)x); }
 inline double cos(double x) { return ::cos(x); }
 inline double sin(double x) { return ::sin(x); }
 inline float2 cos(float2 v) { return float2(cos(v.x), cos(v.y)); }
+inline float dot(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
 inline float asin(float x) { return (float)::asin((double)x); }
 inline float exp(float x) { return (float)::exp((double)x); }
 inline float sqrt(float x) { return ::sqrtf(x); }

@@ -16,6 +16,9 @@
  *   - the FBP ramp filter chain of FBP_execution (GPU.cpp:745-806 over FBP.cl:34-160)
  *                                                                       -> xo_fbp_filter_*
  *   - the hybrid base-up (GPU.cpp:1538-1566, reconstShare.cl:87-177)   -> xo_base_up_f32
+ *   - the rotation-centre search's rotCenterShift, setMask and imgFocusIndex
+ *     (RotationCenterSearch/rotCenterSearch.cl:37-232)                  -> xo_rot_center_*,
+ *                                                    xo_mask_*, xo_set_mask_f32, xo_focus_index
  *
  * Parity pin: the reference ships no tests, fixtures or golden vectors, and its OpenCL
  * runtime is not available, so the pin is oracle/_ref: the reference's own OSEM.cl and
@@ -294,4 +297,137 @@ void xo_base_up_f32(float *img, long long n, int order, float *min_out)
         }
         img[i] = v - a * (float)exp((double)g);
     }
+}
+
+
+/* ------------------------------------------------------------- rotation-centre search
+ * rotCenterShift (rotCenterSearch.cl:37-49): out[th][X] = the linear sampler at
+ * ((X + shift) + 0.5, th + 0.5) of the sinogram, zero beyond its edges:
+ * u = ((float)X + shift) + 0.5; i = floor(u - 0.5); a = (u - 0.5) - i;
+ * (1 - a) t[i] + a t[i+1]. */
+void xo_rot_center_shift_f32(const float *prj, int px, int pa, float shift, float *out)
+{
+#pragma omp parallel for schedule(static)
+    for (int th = 0; th < pa; ++th)
+        for (int X = 0; X < px; ++X) {
+            const float u = ((float)X + shift) + 0.5f;
+            const float uu = u - 0.5f;
+            const float fi = floorf(uu);
+            const float a = uu - fi;
+            const int i = (int)fi;
+            const float t0 = (i >= 0 && i < px) ? prj[(size_t)th * px + i] : 0.0f;
+            const float t1 = (i + 1 >= 0 && i + 1 < px) ? prj[(size_t)th * px + i + 1] : 0.0f;
+            out[(size_t)th * px + X] = (1.0f - a) * t0 + a * t1;
+        }
+}
+
+/* setMask's constants (rotCenterSearch.cl:58-72): a = ang*PI/180 and ang*PI/180 - PI/2 in
+ * double stored to float; p_cnt = (W/2, H/2) in integers; rp = min(W/2 + shift, W/2),
+ * rm = max(-W/2 + shift, -W/2); p1 = rp cos(a_max), p2 = rp cos(a_min), p3 = rm cos(a_max),
+ * p4 = rm cos(a_min) (float cos of the float components); p_div = p1.x if rp^2 < rm^2
+ * else p3.x. */
+void xo_mask_params_f32(int W, int H, float shift, float ang_min, float ang_max, float *prm)
+{
+    const float amin_x = (float)((double)ang_min * XO_PI / 180), amin_y = (float)((double)ang_min * XO_PI / 180 - XO_PI_2);
+    const float amax_x = (float)((double)ang_max * XO_PI / 180), amax_y = (float)((double)ang_max * XO_PI / 180 - XO_PI_2);
+    const float rp = fminf((float)(W / 2) + shift, (float)(W / 2));
+    const float rm = fmaxf((float)(-W / 2) + shift, (float)(-W / 2));
+    const float p1x = rp * (float)cos((double)amax_x), p1y = rp * (float)cos((double)amax_y);
+    const float p2x = rp * (float)cos((double)amin_x), p2y = rp * (float)cos((double)amin_y);
+    const float p3x = rm * (float)cos((double)amax_x), p3y = rm * (float)cos((double)amax_y);
+    const float p4x = rm * (float)cos((double)amin_x), p4y = rm * (float)cos((double)amin_y);
+    prm[0] = rp;
+    prm[1] = rm;
+    prm[2] = p1x;
+    prm[3] = p1y;
+    prm[4] = p2x;
+    prm[5] = p2y;
+    prm[6] = p3x;
+    prm[7] = p3y;
+    prm[8] = p4x;
+    prm[9] = p4y;
+    prm[10] = (rp * rp < rm * rm) ? p1x : p3x;
+    prm[11] = (float)(W / 2);
+    prm[12] = (float)(H / 2);
+}
+
+/* setMask's per-pixel test (rotCenterSearch.cl:79-95); dot(a, b) = a.x*b.x + a.y*b.y. */
+static int xo_mask_at(const float *prm, int x, int y)
+{
+    const float X = (float)x - prm[11], Y = (float)y - prm[12];
+    const float rp = prm[0], rm = prm[1], pd = prm[10];
+    const int b1 = X * prm[2] + Y * prm[3] <= rp * rp;
+    const int b2 = X * prm[4] + Y * prm[5] <= rp * rp;
+    const int b3 = X * prm[6] + Y * prm[7] <= rm * rm;
+    const int b4 = X * prm[8] + Y * prm[9] <= rm * rm;
+    const float d2 = X * X + Y * Y;
+    const int b5 = d2 <= rp * rp && X > pd;
+    const int b6 = d2 <= rm * rm && X <= pd;
+    return b1 && b2 && b3 && b4 && (b5 || b6);
+}
+
+void xo_set_mask_f32(int W, int H, int w_visit, const float *prm, float *mask)
+{
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) mask[(size_t)y * W + x] = (x < w_visit && xo_mask_at(prm, x, y)) ? 1.0f : 0.0f;
+}
+
+static float xo_tex2(const float *im, int W, int H, int x, int y)
+{
+    return (x >= 0 && y >= 0 && x < W && y < H) ? im[(size_t)y * W + x] : 0.0f;
+}
+
+/* imgFocusIndex's per-pixel terms (rotCenterSearch.cl:178-224): the product of the nine
+ * masks of the 3x3 neighbourhood, and the squared differences to the neighbours u, d, r, l,
+ * ur, dr, ul, dl (u = y+1, r = x+1) summed in that order, divided by a*a, where the
+ * product is 1. */
+static void xo_focus_terms(const float *img, const float *mask, int W, int H, int x, int y, float *sq, float *mt)
+{
+    static const int dx[8] = {0, 0, 1, -1, 1, 1, -1, -1}, dy[8] = {1, -1, 0, 0, 1, -1, 1, -1};
+    float m = xo_tex2(mask, W, H, x, y);
+    for (int k = 0; k < 8; ++k) m *= xo_tex2(mask, W, H, x + dx[k], y + dy[k]);
+    const float a = xo_tex2(img, W, H, x, y);
+    float s = 0.0f;
+    for (int k = 0; k < 8; ++k) {
+        const float d = xo_tex2(img, W, H, x + dx[k], y + dy[k]) - a;
+        s += (m == 1.0f) ? d * d : 0.0f;
+    }
+    s /= (m == 1.0f) ? a * a : 1.0f;
+    *sq = s;
+    *mt = m;
+}
+
+double xo_focus_index(const float *img, const float *mask, int W, int H, int L)
+{
+    if (L <= 0) {
+        double s = 0.0, m = 0.0;
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                float a, b;
+                xo_focus_terms(img, mask, W, H, x, y, &a, &b);
+                s += a;
+                m += b;
+            }
+        return sqrt(s / m);
+    }
+    /* work-item lid sums pixels x = lid + i*L (i < W/L) row by row in float; then the
+     * local-memory tree: loc[id] += loc[id + s] for s = L/2, L/4, ..., 1 */
+    float *ls = (float *)calloc((size_t)L, sizeof(float)), *lm = (float *)calloc((size_t)L, sizeof(float));
+    for (int lid = 0; lid < L; ++lid)
+        for (int y = 0; y < H; ++y)
+            for (int i = 0; i < W / L; ++i) {
+                float a, b;
+                xo_focus_terms(img, mask, W, H, lid + i * L, y, &a, &b);
+                ls[lid] += a;
+                lm[lid] += b;
+            }
+    for (int st = L / 2; st > 0; st >>= 1)
+        for (int id = 0; id < st; ++id) {
+            ls[id] += ls[id + st];
+            lm[id] += lm[id + st];
+        }
+    const float r = sqrtf(ls[0] / lm[0]);
+    free(ls);
+    free(lm);
+    return r;
 }

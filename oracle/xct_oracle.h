@@ -44,6 +44,16 @@ void xo_fbp_filter_f64(const double *prj, int px, int nrows, int zp, double *out
  * returns the minimum in *min_out when not NULL. */
 void xo_base_up_f32(float *img, long long n, int order, float *min_out);
 
+/* Rotation-centre search (RotationCenterSearch/rotCenterSearch.cl).  Images are [H][W]. */
+void xo_rot_center_shift_f32(const float *prj, int px, int pa, float shift, float *out);
+/* setMask's per-shift constants: rp, rm, p1..p4 (x, y), p_div, p_cnt (x, y) -> prm[13] */
+void xo_mask_params_f32(int W, int H, float shift, float ang_min, float ang_max, float *prm);
+/* setMask over columns x < w_visit (others 0) */
+void xo_set_mask_f32(int W, int H, int w_visit, const float *prm, float *mask);
+/* imgFocusIndex: per-pixel (sq_delta, mask_tot) summed in the reference's order for a
+ * work-group of L items (literal, float) or in double over every pixel (L = 0). */
+double xo_focus_index(const float *img, const float *mask, int W, int H, int L);
+
 #define XO_DECL(T, S)                                                                                   \
     void xo_projection##S(const T *img, const T *cs, const xo_geom *g, int sub, int ss, int nrows, T *prj); \
     void xo_osem1##S(const T *img, const T *meas, const T *cs, const xo_geom *g, int sub, int nrows,      \

@@ -21,6 +21,10 @@ Fixtures (np.savez_compressed):
                  (FBP + base-up + 10 subsets x 2 iterations of OS-EM).
   fbp_odd.npz    the same for a 48x40 image, 57 bins, 37 angles (odd: the GPU filter pairs
                  rows across the end of a slice), zero padding 256, 1 subset x 2 iterations.
+  rcs_64.npz     rotation-centre search (RotationCenterSearch/) on a 64x64 slice whose
+                 sinogram (64 bins, 90 angles) is centred 1.0 bin right of px/2: 9 shifts
+                 from -2.0 in steps of 0.5, one OS-EM iteration of 10 subsets from 1.0 each,
+                 masks and focus indices (work-group of 64 items, and in double).
 """
 import os
 import sys
@@ -101,6 +105,38 @@ def fbp_case(name, nx, ny, px, pa, zp, ss, it, order, n_ell, seed, i0, noise_see
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
 
 
+def rcs_case(name, n_img, px, pa, ss, n, start, step, offset, seed, i0, noise_seed, L):
+    img = P.rasterize_ellipses(P.ellipse_params(n_img, 6, seed, axes=(3, n_img / 4)), n_img, n_img)
+    ang = P.uniform_angles(pa)
+    sino = P.noisy_log_sinogram(O.projection(img, ang, px, cx=px / 2 + offset, order=LIT), i0, noise_seed)
+    shifts = O.shift_values(start, step, n)
+    shifted = np.stack([O.rot_center_shift(sino, s) for s in shifts])
+    sub = O.subset_order(ss)
+    x0 = np.ones((n_img, n_img), np.float32)
+    imgs = np.stack([O.osem_run(x0, shifted[i], ang, ss, 1, sub_order=sub, order=LIT) for i in range(n)])
+    masks = np.stack([O.set_mask(n_img, n_img, s, float(ang[0]), float(ang[-1])) for s in shifts])
+    f_lit = np.array([O.focus_index(imgs[i], masks[i], L) for i in range(n)], np.float32)
+    f_dbl = np.array([O.focus_index(imgs[i], masks[i], 0) for i in range(n)], np.float64)
+    arrays = dict(phantom=img, angles=ang, sino=sino, shifted=shifted, sub=sub, imgs=imgs, masks=masks,
+                  findex=f_lit, findex_f64=f_dbl,
+                  shape=np.array([n_img, px, pa, ss, n, L], np.int32),
+                  shift=np.array([start, step, offset], np.float32))
+    if O.ref_available() and O.rcs_available():
+        R = O.RefRotCenter(n_img, n_img)
+        assert np.array_equal(R.rot_center_shift(sino, n, start, step), shifted), name + ": rotCenterShift differs"
+        r_masks, r_fi = R.focus_index(imgs, L, start, step, float(ang[0]), float(ang[-1]))
+        assert np.array_equal(r_masks, masks), name + ": setMask differs"
+        assert np.array_equal(r_fi, f_lit), name + ": imgFocusIndex differs"
+        ref = O.RefKernels(n_img, n_img, px, pa, ss)
+        r_imgs = ref.osem_execution(np.repeat(x0[None], n, 0), shifted, ang, sub, 1)
+        assert np.array_equal(r_imgs, imgs), name + ": OS-EM differs"
+        arrays["pinned_by_reference_kernels"] = np.array([1], np.int32)
+        print(name, "pinned: bit-identical to the reference kernels")
+    else:
+        arrays["pinned_by_reference_kernels"] = np.array([0], np.int32)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+
+
 if __name__ == "__main__":
     O.build()
     case("small_64", 64, 64, 64, 90, 10, 2, 10, 1, 1e5, 11)
@@ -108,3 +144,4 @@ if __name__ == "__main__":
     case("cfg1_256", 256, 256, 256, 180, 10, 5, 10, 1, 1e5, 11)
     fbp_case("fbp_64", 64, 64, 64, 90, 128, 10, 2, 4, 8, 3, 1e5, 13)
     fbp_case("fbp_odd", 48, 40, 57, 37, 256, 1, 2, 4, 6, 7, 1e5, 14)
+    rcs_case("rcs_64", 64, 64, 90, 10, 9, -2.0, 0.5, 1.0, 5, 1e5, 15, 64)

@@ -31,16 +31,17 @@ INP_KEYS = [
     ("#カメラピクセル数", "{px}"),
     ("#投影数", "{pa}"),
     ("#再構成画像サイズ", "{n}"),
-    ("#再構成法", "6"),
+    ("#再構成法", "{method}"),
     ("#反復回数", "{it}"),
     ("#サブセット(OSEM)", "{ss}"),
     ("#投影像補正 0:なし 1: x方向のみ 2:θ方向のみ 3:x,θ方向両方", "0"),
 ]
 
 
-def write_inp(path, **kw):
+def write_inp(path, extra=(), **kw):
+    kw.setdefault("method", 6)
     with open(path, "wb") as f:
-        for i, (k, v) in enumerate(INP_KEYS):
+        for i, (k, v) in enumerate(list(INP_KEYS) + list(extra)):
             eol = b"\r\n" if i % 3 == 0 else b"\n"
             f.write(k.encode("utf-8") + eol + v.format(**kw).encode("utf-8") + eol)
 
@@ -94,3 +95,37 @@ def test_end_to_end_reconstruction_from_files(host_bin, oracle_lib, tmp_path):
         ref = O.osem_run(x0, meas[z], ang, ss, it, order=O.ORDER_LITERAL)
         rel = np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)
         assert rel <= 1e-4, (z, rel)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", [7, 8])
+def test_fbp_and_hybrid_methods_from_files(host_bin, oracle_lib, tmp_path, method):
+    """Methods 7 (FBP) and 8 (FBP + OS-EM hybrid) of GPU() (GPU.cpp:80-90) with the .inp's
+    zero padding and base-up order keys."""
+    from xct import phantom as P
+    O = oracle_lib
+    n, px, pa, ss, it, zp, order = 64, 72, 45, 3, 2, 256, 3
+    ang = P.uniform_angles(pa)
+    d1, d2 = tmp_path / "in", tmp_path / "out"
+    d1.mkdir()
+    with open(tmp_path / "angles.log", "w") as f:
+        for a in ang:
+            f.write("%.9g\n" % a)
+    meas = {}
+    for z in range(7, 10):
+        img = P.rasterize_ellipses(P.ellipse_params(n, 5, z, axes=(3, 16)), n, n)
+        meas[z] = P.noisy_log_sinogram(O.projection(img, ang, px), 1e5, z)
+        meas[z].astype(np.float32).tofile(d1 / ("s%04d.raw" % z))
+    inp = tmp_path / "run.inp"
+    write_inp(inp, extra=[("#ゼロパディングサイズ(FBP)", str(zp)), ("#Base up 減少速度次数 (Hybrid)", str(order))],
+              d1=str(d1), d2=str(d2), f3=str(tmp_path / "angles.log"), px=px, pa=pa, n=n, it=it, ss=ss,
+              method=method)
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for z in range(7, 10):
+        got = np.fromfile(d2 / ("rec_%04d.img" % z), np.float32).reshape(n, n)
+        ref = O.fbp(meas[z], ang, n, n, zp)
+        if method == 8:
+            ref = O.osem_run(O.base_up(ref, order)[0], meas[z], ang, ss, it, order=O.ORDER_LITERAL)
+        rel = np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)
+        assert rel <= (2e-5 if method == 7 else 1e-4), (z, rel)

@@ -296,3 +296,67 @@ def test_fbp_oracle_bit_identical_to_reference_kernels(oracle_lib, shape):
         for z in range(2):
             ob, om = O.base_up(r_img[z], order)
             assert np.array_equal(rb[z], ob) and rm[z] == om
+
+
+# ------------------------------------------------------------- rotation-centre search
+def test_rcs_oracle_reproduces_golden(oracle_lib):
+    """rotCenterShift, setMask, imgFocusIndex (literal work-group order and double sums) and
+    the one-iteration OS-EM of the search, bit-exact against the pinned fixture."""
+    O = oracle_lib
+    f = _load("rcs_64")
+    n_img, px, pa, ss, n, L = [int(v) for v in f["shape"]]
+    start, step, _ = [float(v) for v in f["shift"]]
+    shifts = O.shift_values(start, step, n)
+    x0 = np.ones((n_img, n_img), np.float32)
+    for i, s in enumerate(shifts):
+        sh = O.rot_center_shift(f["sino"], s)
+        assert np.array_equal(sh, f["shifted"][i])
+        img = O.osem_run(x0, sh, f["angles"], ss, 1, sub_order=f["sub"], order=O.ORDER_LITERAL)
+        assert np.array_equal(img, f["imgs"][i])
+        m = O.set_mask(n_img, n_img, s, float(f["angles"][0]), float(f["angles"][-1]))
+        assert np.array_equal(m, f["masks"][i])
+        assert np.float32(O.focus_index(img, m, L)) == f["findex"][i]
+        assert O.focus_index(img, m, 0) == f["findex_f64"][i]
+    # the float work-group order and the double sums agree to ~1e-7
+    assert np.abs(f["findex"] / f["findex_f64"] - 1).max() < 1e-5
+
+
+def test_rcs_mask_known_answers(oracle_lib):
+    """setMask with shift 0 over 0..180 deg keeps the disc of radius W/2 (minus the
+    half-plane test's boundary); a positive shift shrinks the right edge (rp = W/2) and
+    not the left (rm = -W/2 + s)."""
+    O = oracle_lib
+    W = 64
+    m0 = O.set_mask(W, W, 0.0, 0.0, 179.0)
+    yy, xx = np.mgrid[0:W, 0:W].astype(np.float64) - W // 2
+    disc = (xx * xx + yy * yy) <= (W // 2) ** 2
+    assert m0.sum() > 0.9 * disc.sum() and not np.any(m0[~disc])
+    m4 = O.set_mask(W, W, 4.0, 0.0, 179.0)
+    assert m4.sum() < m0.sum() and not np.any(m4[~disc])
+
+
+@pytest.mark.parametrize("shape", [(64, 72, 60, 32, 2), (48, 48, 40, 16, 0)])
+def test_rcs_oracle_bit_identical_to_reference_kernels(oracle_lib, shape):
+    """oracle/_ref's rotCenterSearch.cl build against the oracle: other sizes, work-group
+    sizes and a shift offset (offsetN).  Only where the reference checkout exists."""
+    O = oracle_lib
+    if not (O.ref_available() and O.rcs_available()):
+        pytest.skip("reference checkout not present")
+    from xct import phantom as P
+    n_img, px, pa, L, off = shape
+    img = P.rasterize_ellipses(P.ellipse_params(n_img, 5, 4, axes=(2, n_img / 4)), n_img, n_img)
+    ang = P.uniform_angles(pa)
+    sino = P.noisy_log_sinogram(O.projection(img, ang, px, cx=px / 2 - 1.5), 1e5, 2)
+    n, start, step = 5, -1.25, 0.75
+    R = O.RefRotCenter(n_img, n_img)
+    shifted = R.rot_center_shift(sino, n + off, start, step)
+    sv = O.shift_values(start, step, n + off)
+    for i in range(n + off):
+        assert np.array_equal(shifted[i], O.rot_center_shift(sino, sv[i]))
+    x0 = np.ones((n_img, n_img), np.float32)
+    imgs = np.stack([O.osem_run(x0, shifted[off + i], ang, 4, 1) for i in range(n)])
+    masks, fi = R.focus_index(imgs, L, start, step, float(ang[0]), float(ang[-1]), offsetN=off)
+    for i in range(n):
+        m = O.set_mask(n_img, n_img, sv[off + i], float(ang[0]), float(ang[-1]))
+        assert np.array_equal(masks[i], m)
+        assert np.float32(O.focus_index(imgs[i], m, L)) == fi[i]
