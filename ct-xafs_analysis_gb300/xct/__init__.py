@@ -49,6 +49,7 @@ EXPORTS = (
     "xct_batch_plan_create", "xct_batch_run", "xct_batch_plan_destroy", "xct_osem_run_batched",
     "xct_fbp_filter", "xct_fbp_backproject", "xct_fbp_run_device", "xct_hybrid_run_device", "xct_fbp_run",
     "xct_hybrid_run", "xct_rot_center_shift", "xct_focus_index", "xct_rot_center_search",
+    "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_denoise_sinogram",
 )
 
 
@@ -119,6 +120,10 @@ def load():
     L.xct_focus_index.argtypes = [vp, ip, ip, c_f, c_f, c_f, c_f, vp, vp, vp]
     L.xct_rot_center_search.argtypes = [vp, ip, c_f, c_f, c_f, c_f, c_f, vp, vp, fp, ctypes.POINTER(ctypes.c_int),
                                         vp]
+    L.xct_reslice_plan_create.argtypes = [vp, ip, ip, ip, fp, fp, c_f, ip, ctypes.POINTER(vp)]
+    L.xct_reslice.argtypes = [vp, ip, ip, vp, vp, vp]
+    L.xct_reslice_plan_destroy.argtypes = [vp]
+    L.xct_denoise_sinogram.argtypes = [ip, ip, ip, c_f, vp, vp, vp]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong
@@ -414,6 +419,49 @@ class BatchPlan:
             self.close()
         except Exception:
             pass
+
+
+class ReslicePlan:
+    """Projection stack -> sinograms on the device (Reslice/reslice_ocl.cpp reslice())."""
+
+    def __init__(self, ctx, width, height, n_angles, xshift=None, yshift=None, baseup=0.0, correction=0):
+        self._lib = load()
+        self.ctx = ctx
+        self.width, self.height, self.n_angles = width, height, n_angles
+        fp = ctypes.POINTER(ctypes.c_float)
+        xs = None if xshift is None else np.ascontiguousarray(xshift, dtype=np.float32)
+        ys = None if yshift is None else np.ascontiguousarray(yshift, dtype=np.float32)
+        for a in (xs, ys):
+            if a is not None and a.size != n_angles:
+                raise XCTError(XCT_E_INVALID, "shift arrays must have n_angles entries")
+        h = ctypes.c_void_p()
+        _check(self._lib.xct_reslice_plan_create(ctx.handle, width, height, n_angles,
+                                                 None if xs is None else xs.ctypes.data_as(fp),
+                                                 None if ys is None else ys.ctypes.data_as(fp),
+                                                 baseup, correction, ctypes.byref(h)))
+        self.handle = h
+
+    def reslice(self, d_proj, d_sino, first_angle=0, n=None, stream=None):
+        """d_proj [n][height][width] (angles first_angle..) -> rows of d_sino [height][n_angles][width]."""
+        n = d_proj.shape[0] if n is None else n
+        _check(self._lib.xct_reslice(self.handle, first_angle, n, _ptr(d_proj), _ptr(d_sino), _stream(stream)))
+
+    def close(self):
+        if self.handle:
+            self._lib.xct_reslice_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def denoise_sinogram(d_src, d_dst, threshold, stream=None):
+    """denoiseSinogram (Reslice/reslice.cl:223-248) on sinograms [rows][angles][width]."""
+    rows, na, w = d_src.shape
+    _check(load().xct_denoise_sinogram(w, na, rows, threshold, _ptr(d_src), _ptr(d_dst), _stream(stream)))
 
 
 # ---------------------------------------------------------------- reference-named mirrors

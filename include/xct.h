@@ -215,6 +215,28 @@ int xct_rot_center_search(xct_plan *plan, int n, float shift_start, float shift_
                           float ang_fin_deg, float init_value, const float *d_sino, float *d_imgs, float *findex,
                           int *best, void *stream);
 
+/* ---- reslice: projection stack -> sinograms on the device (Reslice/reslice_ocl.cpp) ----
+ * A reslice plan holds the per-angle shifts and constants of reslice() (:153-208):
+ * xshift/yshift [n_angles] (host, copied; NULL = 0; the y shift is the z-drift correction
+ * of Z_Correction, :89-150), baseup (added to every value) and correction (0/1: multiply by
+ * cos(asin(2|X - W/2|/W)), reslice.cl:65-67).
+ * xct_reslice : reslice (reslice.cl:52-71) of projections d_proj [n][height][width] for angles
+ *               first_angle .. first_angle + n - 1 into d_sino [height][n_angles][width]:
+ *               d_sino[Y][th][X] = bilinear(projection th at (X + xshift[th], Y + yshift[th]),
+ *               zero outside) + baseup.  Row Y of d_sino is slice Y's sinogram [n_angles][width],
+ *               so d_sino + Y0*n_angles*width is a ready dN-slice input of the OS-EM/FBP calls.
+ * xct_denoise_sinogram : denoiseSinogram (reslice.cl:223-248) on n_rows sinograms
+ *               [n_angles][width]: a value that is a one-angle spike beyond +-threshold against
+ *               both angle neighbours (clamped at the ends) becomes their mean.  d_src and
+ *               d_dst must not overlap.  Runs on the current device. */
+typedef struct xct_reslice_plan xct_reslice_plan;
+int xct_reslice_plan_create(xct_ctx *ctx, int width, int height, int n_angles, const float *xshift,
+                            const float *yshift, float baseup, int correction, xct_reslice_plan **out);
+int xct_reslice(xct_reslice_plan *plan, int first_angle, int n, const float *d_proj, float *d_sino, void *stream);
+int xct_reslice_plan_destroy(xct_reslice_plan *plan);
+int xct_denoise_sinogram(int width, int n_angles, int n_rows, float threshold, const float *d_src, float *d_dst,
+                         void *stream);
+
 /* Tracing: xct_osem_run_device with CUDA events around every launch.  The reference
  * enables CL_QUEUE_PROFILING_ENABLE but never reads the events
  * (share source/OCL_platform_device_class.cpp:175-178).  ms[0..3] = summed device time of

@@ -130,3 +130,43 @@ def build_rcs(width, height, force=False):
            "-w", "-o", so, cpp] + defs
     subprocess.run(cmd, check=True)
     return so
+
+
+RESLICE_KERNEL = "Reslice/reslice.cl"
+
+
+def reslice_available():
+    return os.path.isfile(os.path.join(REF_ROOT, RESLICE_KERNEL))
+
+
+def build_reslice(width, height, n_angles, force=False):
+    """Compile Reslice/reslice.cl for one (width, height, angles) with the -D options of
+    reslice_programBuild (Reslice/reslice_ocl.cpp:429-435); return the .so path."""
+    if not reslice_available():
+        raise FileNotFoundError("reference kernel sources not found under %s" % REF_ROOT)
+    os.makedirs(OUT, exist_ok=True)
+    parts = ['#include "%s"' % os.path.join(HERE, "ref_shim", "cl_shim.hpp"), "namespace clk {"]
+    with open(os.path.join(REF_ROOT, RESLICE_KERNEL), encoding="utf-8") as f:
+        parts.append("// ---- %s (vector literals rewritten) ----" % RESLICE_KERNEL)
+        parts.append(_rewrite(f.read()))
+    parts.append("}  // namespace clk")
+    parts.append('#include "%s"' % os.path.join(HERE, "ref_shim", "reslice_driver.inc"))
+    src = "\n".join(parts) + "\n"
+    tag = "%dx%d_a%d" % (width, height, n_angles)
+    h = hashlib.sha1(src.encode())
+    for dep in ("cl_shim.hpp", "reslice_driver.inc"):
+        with open(os.path.join(HERE, "ref_shim", dep), "rb") as f:
+            h.update(f.read())
+    digest = h.hexdigest()[:10]
+    cpp = os.path.join(OUT, "reslice_kernels_%s.cpp" % tag)
+    so = os.path.join(OUT, "libreslice_%s_%s.so" % (tag, digest))
+    if os.path.exists(so) and not force:
+        return so
+    with open(cpp, "w") as f:
+        f.write(src)
+    defs = ["-DPRJ_ANGLESIZE=%d" % n_angles, "-DNUM_TRIAL=20", "-DLAMBDA=0.001f", "-DIMAGESIZE_X=%d" % width,
+            "-DIMAGESIZE_Y=%d" % height, "-DIMAGESIZE_M=%d" % (width * height)]
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-Wno-narrowing", "-shared", "-fPIC",
+           "-w", "-o", so, cpp] + defs
+    subprocess.run(cmd, check=True)
+    return so

@@ -85,6 +85,9 @@ def lib():
         L.xo_set_mask_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, fp]
         L.xo_focus_index.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.xo_focus_index.restype = ctypes.c_double
+        L.xo_reslice_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, fp, ctypes.c_float,
+                                     ctypes.c_int, fp]
+        L.xo_denoise_sinogram_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp]
         L.xo_trig_f32.argtypes = [fp, ctypes.c_int, fp]
         L.xo_trig_f64.argtypes = [fp, ctypes.c_int, dp]
         L.xo_subset_order.argtypes = [ctypes.c_int, ip]
@@ -274,6 +277,27 @@ def focus_index(img, mask, L=0):
     return lib().xo_focus_index(_p(img), _p(mask), W, H, int(L))
 
 
+def reslice(mt, xshift=None, yshift=None, baseup=0.0, correction=0):
+    """reslice (Reslice/reslice.cl:52-71): projections [A][H][W] -> sinograms [H][A][W]."""
+    mt = np.ascontiguousarray(mt, dtype=np.float32)
+    A, H, W = mt.shape
+    xs = None if xshift is None else np.ascontiguousarray(xshift, dtype=np.float32)
+    ys = None if yshift is None else np.ascontiguousarray(yshift, dtype=np.float32)
+    out = np.empty((H, A, W), np.float32)
+    lib().xo_reslice_f32(_p(mt), W, H, A, None if xs is None else _p(xs), None if ys is None else _p(ys),
+                         baseup, correction, _p(out))
+    return out
+
+
+def denoise_sinogram(sino, threshold):
+    """denoiseSinogram (Reslice/reslice.cl:223-248) on sinograms [H][A][W]."""
+    sino = np.ascontiguousarray(sino, dtype=np.float32)
+    H, A, W = sino.shape
+    out = np.empty_like(sino)
+    lib().xo_denoise_sinogram_f32(_p(sino), W, A, H, threshold, _p(out))
+    return out
+
+
 def adjoint(sino, angles_deg, nx, ny, cx=None, dtype=np.float32):
     """Exact adjoint A^T of projection() over all angles."""
     sino = np.ascontiguousarray(sino, dtype=dtype)
@@ -415,6 +439,37 @@ class RefRotCenter:
         fi = np.zeros(n, np.float32)
         self.lib.rcs_focus_index(_p(imgs), n, L, offsetN, start, step, ang_ini, ang_fin, _p(masks), _p(fi))
         return masks, fi
+
+
+class RefReslice:
+    """The reference's reslice.cl compiled for one (width, height, angles) (build_reslice)."""
+
+    def __init__(self, width, height, n_angles):
+        import build_ref  # noqa: local module beside this file
+        self.shape = (width, height, n_angles)
+        self.lib = ctypes.CDLL(build_ref.build_reslice(width, height, n_angles))
+        fp = ctypes.POINTER(ctypes.c_float)
+        self.lib.ref_reslice.argtypes = [fp, fp, fp, ctypes.c_float, ctypes.c_int, fp]
+        self.lib.ref_denoise.argtypes = [fp, ctypes.c_float, fp]
+
+    def reslice(self, mt, xshift=None, yshift=None, baseup=0.0, correction=0):
+        W, H, A = self.shape
+        xs = np.zeros(A, np.float32) if xshift is None else np.ascontiguousarray(xshift, dtype=np.float32)
+        ys = np.zeros(A, np.float32) if yshift is None else np.ascontiguousarray(yshift, dtype=np.float32)
+        out = np.zeros((H, A, W), np.float32)
+        self.lib.ref_reslice(_p(np.ascontiguousarray(mt, dtype=np.float32)), _p(xs), _p(ys), baseup, correction,
+                             _p(out))
+        return out
+
+    def denoise(self, sino, threshold):
+        out = np.zeros_like(sino, dtype=np.float32)
+        self.lib.ref_denoise(_p(np.ascontiguousarray(sino, dtype=np.float32)), threshold, _p(out))
+        return out
+
+
+def reslice_available():
+    import build_ref
+    return build_ref.reslice_available()
 
 
 def rcs_available():

@@ -7,7 +7,8 @@
 // (section 8, "Image Addressing and Filtering"): unnormalised coordinates,
 // CLK_ADDRESS_CLAMP with the CL_R border colour (.x == 0), linear filtering with
 // i0 = floor(u - 0.5) and a = frac(u - 0.5), nearest filtering with i = floor(u), array
-// layer = clamp(rint(z)).  cos/sin of a float are taken correctly rounded
+// layer = clamp(rint(z)), CLK_ADDRESS_CLAMP_TO_EDGE clamping texel indices to the edge.
+// cos/sin of a float are taken correctly rounded
 // ((float)cos((double)x)); the specification allows up to 4 ulp.
 #pragma once
 #include <math.h>
@@ -119,6 +120,17 @@ inline float texel_(const image2d_array_t &im, int i, int j, int k)
     if (i < 0 || j < 0 || i >= im.w || j >= im.h) return 0.0f;  // CLK_ADDRESS_CLAMP border
     return im.data[((size_t)k * im.h + j) * im.w + i];
 }
+// CLK_ADDRESS_CLAMP_TO_EDGE: out-of-range texels take the nearest edge texel
+inline float texel_edge_(const image2d_array_t &im, int i, int j, int k)
+{
+    i = i < 0 ? 0 : (i >= im.w ? im.w - 1 : i);
+    j = j < 0 ? 0 : (j >= im.h ? im.h - 1 : j);
+    return im.data[((size_t)k * im.h + j) * im.w + i];
+}
+inline float texel_mode_(const image2d_array_t &im, int smp, int i, int j, int k)
+{
+    return (smp & CLK_ADDRESS_CLAMP_TO_EDGE) ? texel_edge_(im, i, j, k) : texel_(im, i, j, k);
+}
 inline int layer_(const image2d_array_t &im, float z)
 {
     int k = (int)rintf(z);
@@ -132,11 +144,12 @@ inline float4 read_imagef(image2d_array_t im, sampler_t smp, float4 c)
         const float fi = floorf(u), fj = floorf(v);
         const float a = u - fi, b = v - fj;
         const int i = (int)fi, j = (int)fj;
-        const float t = (1.0f - a) * (1.0f - b) * texel_(im, i, j, k) + a * (1.0f - b) * texel_(im, i + 1, j, k) +
-                        (1.0f - a) * b * texel_(im, i, j + 1, k) + a * b * texel_(im, i + 1, j + 1, k);
+        const float t = (1.0f - a) * (1.0f - b) * texel_mode_(im, smp, i, j, k) +
+                        a * (1.0f - b) * texel_mode_(im, smp, i + 1, j, k) +
+                        (1.0f - a) * b * texel_mode_(im, smp, i, j + 1, k) + a * b * texel_mode_(im, smp, i + 1, j + 1, k);
         return float4(t, 0.0f, 0.0f, 1.0f);
     }
-    return float4(texel_(im, (int)floorf(c.x), (int)floorf(c.y), k), 0.0f, 0.0f, 1.0f);
+    return float4(texel_mode_(im, smp, (int)floorf(c.x), (int)floorf(c.y), k), 0.0f, 0.0f, 1.0f);
 }
 inline float4 read_imagef(image2d_array_t im, sampler_t smp, int4 c)
 {
@@ -173,6 +186,9 @@ inline size_t get_global_id(int d) { return g_gid[d]; }
 inline size_t get_local_id(int d) { return g_lid[d]; }
 inline size_t get_local_size(int d) { return g_lsz[d]; }
 inline size_t get_group_id(int d) { return g_grp[d]; }
+extern thread_local size_t g_gsz[3];   // global size (set by drivers whose kernels ask)
+inline size_t get_global_size(int d) { return g_gsz[d]; }
+inline size_t get_num_groups(int d) { return g_gsz[d] / (g_lsz[d] ? g_lsz[d] : 1); }
 inline void barrier(int)
 {
     if (g_barrier_fn) g_barrier_fn();

@@ -19,6 +19,8 @@
  *   - the rotation-centre search's rotCenterShift, setMask and imgFocusIndex
  *     (RotationCenterSearch/rotCenterSearch.cl:37-232)                  -> xo_rot_center_*,
  *                                                    xo_mask_*, xo_set_mask_f32, xo_focus_index
+ *   - reslice and denoiseSinogram (Reslice/reslice.cl:52-71, 223-248) -> xo_reslice_f32,
+ *                                                    xo_denoise_sinogram_f32
  *
  * Parity pin: the reference ships no tests, fixtures or golden vectors, and its OpenCL
  * runtime is not available, so the pin is oracle/_ref: the reference's own OSEM.cl and
@@ -430,4 +432,57 @@ double xo_focus_index(const float *img, const float *mask, int W, int H, int L)
     free(ls);
     free(lm);
     return r;
+}
+
+
+/* ------------------------------------------------------------------------ reslice
+ * reslice (reslice.cl:52-71): prj[Y][th][X] = the linear sampler (zero border) of
+ * projection th at ((X + xs[th]) + 0.5, (Y + ys[th]) + 0.5), plus baseup; with
+ * correction, times cos(asin(theta)), theta = 2|X - W/2.0|/W (float cos/asin, taken
+ * correctly rounded).  The sampler's sum is evaluated as written in the OpenCL 1.2
+ * filtering formula: (1-a)(1-b) T00 + a(1-b) T10 + (1-a) b T01 + a b T11. */
+void xo_reslice_f32(const float *mt, int W, int H, int A, const float *xs, const float *ys, float baseup,
+                    int correction, float *prj)
+{
+#pragma omp parallel for schedule(static)
+    for (int Y = 0; Y < H; ++Y)
+        for (int th = 0; th < A; ++th) {
+            const float *im = mt + (size_t)th * H * W;
+            const float sx = xs ? xs[th] : 0.0f, sy = ys ? ys[th] : 0.0f;
+            for (int X = 0; X < W; ++X) {
+                const float uu = (((float)X + sx) + 0.5f) - 0.5f, vv = (((float)Y + sy) + 0.5f) - 0.5f;
+                const float fi = floorf(uu), fj = floorf(vv);
+                const float a = uu - fi, b = vv - fj;
+                const int i = (int)fi, j = (int)fj;
+                float t = (1.0f - a) * (1.0f - b) * xo_tex2(im, W, H, i, j) + a * (1.0f - b) * xo_tex2(im, W, H, i + 1, j) +
+                          (1.0f - a) * b * xo_tex2(im, W, H, i, j + 1) + a * b * xo_tex2(im, W, H, i + 1, j + 1);
+                t += baseup;
+                if (correction == 1) {
+                    const float theta = 2.0f * fabsf((float)X - (float)W / 2.0f) / (float)W;
+                    t *= (float)cos((double)(float)asin((double)theta));
+                }
+                prj[((size_t)Y * A + th) * W + X] = t;
+            }
+        }
+}
+
+/* denoiseSinogram (reslice.cl:223-248): f1 = s[th], f2 = s[th+1], f3 = s[th-1] with the
+ * angle index clamped to the edge; where the row is a one-angle spike (f2 - f1 and f1 - f3
+ * both beyond the threshold, with opposite signs) it becomes (f2 + f3)/2. */
+void xo_denoise_sinogram_f32(const float *src, int W, int A, int H, float threshold, float *dst)
+{
+#pragma omp parallel for schedule(static)
+    for (int Y = 0; Y < H; ++Y)
+        for (int th = 0; th < A; ++th) {
+            const float *r1 = src + ((size_t)Y * A + th) * W;
+            const float *r2 = src + ((size_t)Y * A + (th + 1 < A ? th + 1 : A - 1)) * W;
+            const float *r3 = src + ((size_t)Y * A + (th > 0 ? th - 1 : 0)) * W;
+            for (int X = 0; X < W; ++X) {
+                const float f1 = r1[X], f2 = r2[X], f3 = r3[X];
+                const float d1 = f2 - f1, d2 = f1 - f3;
+                const float c = (f2 + f3) / 2.0f;
+                dst[((size_t)Y * A + th) * W + X] =
+                    ((d1 > threshold && d2 < -threshold) || (d1 < -threshold && d2 > threshold)) ? c : f1;
+            }
+        }
 }

@@ -54,6 +54,13 @@ void xo_set_mask_f32(int W, int H, int w_visit, const float *prm, float *mask);
  * work-group of L items (literal, float) or in double over every pixel (L = 0). */
 double xo_focus_index(const float *img, const float *mask, int W, int H, int L);
 
+/* Reslice (Reslice/reslice.cl): projections mt [A][H][W] -> sinograms prj [H][A][W] with
+ * per-angle shifts (xs, ys may be NULL: 0), baseup and the optional cosine correction;
+ * denoiseSinogram on sinograms [H][A][W]. */
+void xo_reslice_f32(const float *mt, int W, int H, int A, const float *xs, const float *ys, float baseup,
+                    int correction, float *prj);
+void xo_denoise_sinogram_f32(const float *src, int W, int A, int H, float threshold, float *dst);
+
 #define XO_DECL(T, S)                                                                                   \
     void xo_projection##S(const T *img, const T *cs, const xo_geom *g, int sub, int ss, int nrows, T *prj); \
     void xo_osem1##S(const T *img, const T *meas, const T *cs, const xo_geom *g, int sub, int nrows,      \

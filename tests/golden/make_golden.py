@@ -25,6 +25,10 @@ Fixtures (np.savez_compressed):
                  sinogram (64 bins, 90 angles) is centred 1.0 bin right of px/2: 9 shifts
                  from -2.0 in steps of 0.5, one OS-EM iteration of 10 subsets from 1.0 each,
                  masks and focus indices (work-group of 64 items, and in double).
+  reslice_small.npz  reslice (Reslice/reslice.cl) of 16 projections of 12 x 24 pixels
+                 (uniform 0.5..1.5, seed 16) with per-angle shifts U[-2.5, 2.5] (x) and
+                 U[-1.5, 1.5] (y), baseup 0.125, without and with the cosine correction,
+                 and denoiseSinogram (threshold 0.3) of the first result with planted spikes.
 """
 import os
 import sys
@@ -137,6 +141,31 @@ def rcs_case(name, n_img, px, pa, ss, n, start, step, offset, seed, i0, noise_se
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
 
 
+def reslice_case(name, A, H, W, seed, baseup, threshold):
+    rng = np.random.default_rng(seed)
+    mt = rng.uniform(0.5, 1.5, (A, H, W)).astype(np.float32)
+    xs = rng.uniform(-2.5, 2.5, A).astype(np.float32)
+    ys = rng.uniform(-1.5, 1.5, A).astype(np.float32)
+    out0 = O.reslice(mt, xs, ys, baseup, 0)
+    out1 = O.reslice(mt, xs, ys, baseup, 1)
+    spiky = out0.copy()
+    spiky[:, 5, ::3] += 1.0
+    spiky[:, 9, 1::4] -= 1.0
+    den = O.denoise_sinogram(spiky, threshold)
+    arrays = dict(mt=mt, xshift=xs, yshift=ys, sino=out0, sino_corr=out1, spiky=spiky, denoised=den,
+                  params=np.array([baseup, threshold], np.float32))
+    if O.reslice_available():
+        R = O.RefReslice(W, H, A)
+        assert np.array_equal(R.reslice(mt, xs, ys, baseup, 0), out0), name + ": reslice differs"
+        assert np.array_equal(R.reslice(mt, xs, ys, baseup, 1), out1), name + ": corrected reslice differs"
+        assert np.array_equal(R.denoise(spiky, threshold), den), name + ": denoiseSinogram differs"
+        arrays["pinned_by_reference_kernels"] = np.array([1], np.int32)
+        print(name, "pinned: bit-identical to the reference kernels")
+    else:
+        arrays["pinned_by_reference_kernels"] = np.array([0], np.int32)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+
+
 if __name__ == "__main__":
     O.build()
     case("small_64", 64, 64, 64, 90, 10, 2, 10, 1, 1e5, 11)
@@ -145,3 +174,4 @@ if __name__ == "__main__":
     fbp_case("fbp_64", 64, 64, 64, 90, 128, 10, 2, 4, 8, 3, 1e5, 13)
     fbp_case("fbp_odd", 48, 40, 57, 37, 256, 1, 2, 4, 6, 7, 1e5, 14)
     rcs_case("rcs_64", 64, 64, 90, 10, 9, -2.0, 0.5, 1.0, 5, 1e5, 15, 64)
+    reslice_case("reslice_small", 16, 12, 24, 16, 0.125, 0.3)

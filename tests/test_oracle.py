@@ -360,3 +360,49 @@ def test_rcs_oracle_bit_identical_to_reference_kernels(oracle_lib, shape):
         m = O.set_mask(n_img, n_img, sv[off + i], float(ang[0]), float(ang[-1]))
         assert np.array_equal(masks[i], m)
         assert np.float32(O.focus_index(imgs[i], m, L)) == fi[i]
+
+
+# ------------------------------------------------------------------------- reslice
+def test_reslice_oracle_reproduces_golden(oracle_lib):
+    O = oracle_lib
+    f = _load("reslice_small")
+    baseup, thr = [float(v) for v in f["params"]]
+    assert np.array_equal(O.reslice(f["mt"], f["xshift"], f["yshift"], baseup, 0), f["sino"])
+    assert np.array_equal(O.reslice(f["mt"], f["xshift"], f["yshift"], baseup, 1), f["sino_corr"])
+    assert np.array_equal(O.denoise_sinogram(f["spiky"], thr), f["denoised"])
+
+
+def test_reslice_known_answers(oracle_lib):
+    """Zero shifts and baseup: reslicing is an exact transpose of the angle and row axes;
+    an integer shift moves the data by whole pixels with zeros shifted in."""
+    O = oracle_lib
+    rng = np.random.default_rng(2)
+    mt = rng.normal(size=(7, 5, 9)).astype(np.float32)
+    assert np.array_equal(O.reslice(mt), mt.transpose(1, 0, 2))
+    xs = np.full(7, 2.0, np.float32)
+    out = O.reslice(mt, xs)
+    assert np.array_equal(out[:, :, :-2], mt.transpose(1, 0, 2)[:, :, 2:])
+    assert not np.any(out[:, :, -2:])
+    s = np.zeros((1, 6, 3), np.float32)
+    s[0, 2, 1] = 5.0  # a one-angle spike
+    d = O.denoise_sinogram(s, 1.0)
+    assert d[0, 2, 1] == 0.0 and d.sum() == 0.0
+
+
+@pytest.mark.parametrize("shape", [(64, 48, 30), (37, 21, 11)])
+def test_reslice_oracle_bit_identical_to_reference_kernels(oracle_lib, shape):
+    O = oracle_lib
+    if not O.reslice_available():
+        pytest.skip("reference checkout not present")
+    W, H, A = shape
+    rng = np.random.default_rng(W)
+    mt = rng.normal(1, 0.5, (A, H, W)).astype(np.float32)
+    xs = rng.uniform(-3, 3, A).astype(np.float32)
+    ys = rng.uniform(-2, 2, A).astype(np.float32)
+    R = O.RefReslice(W, H, A)
+    for x, y, bu, c in [(None, None, 0.0, 0), (xs, ys, 0.25, 0), (xs, ys, -0.1, 1)]:
+        assert np.array_equal(R.reslice(mt, x, y, bu, c), O.reslice(mt, x, y, bu, c))
+    s = O.reslice(mt)
+    s[:, 5, :] += 3.0
+    for thr in (0.5, 2.0):
+        assert np.array_equal(R.denoise(s, thr), O.denoise_sinogram(s, thr))
