@@ -7,6 +7,7 @@
 //   OSEM_execution      (GPU.cpp:125-240) + OSEM_thread copies (:440-463)    -> xct_osem_run[_device]
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -147,6 +148,7 @@ static void plan_free(xct_plan *p)
     cudaFree(p->d_red);
     cudaFree(p->d_rc_prm);
     cudaFree(p->d_fi);
+    cudaFree(p->d_cs);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -642,6 +644,101 @@ int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *c
     if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
     return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
         return hybrid_device(p, dN, zp, baseup_order, p->d_sino, p->d_img, sub, it, st);
+    });
+}
+
+// ------------------------------------------------------ compressed-sensing OS-EM (FISTA)
+// The kernels' lambda: -D LAMBDA_FISTA is the float CSlambda written by an ostream (six
+// significant digits, GPU.cpp:549) and compiled as a double literal; lambda =
+// LAMBDA_FISTA/L[sub]*0.5f with L[sub] = 0.5 for every subset (GPU.cpp:343, FISTA.cl:426).
+static float cs_kernel_lambda(float cs_lambda)
+{
+    char b[64];
+    snprintf(b, sizeof b, "%g", (double)cs_lambda);
+    const double d = strtod(b, nullptr);
+    return (float)(d / (double)0.5f * 0.5);
+}
+
+// FISTA_OSEM_execution (GPU.cpp:243-405) on dN slices on the device.  Per subset: OSEM1 and
+// OSEM2 (in place: the image becomes v, the OS-EM update), then FISTA3D(w, v, beta) writes x'
+// (then copied into the image), w' and beta' (in place).  The first cycle runs ISTA3D on the
+// image as it was BEFORE that subset's OS-EM step -- the reference passes reconst_img, not the
+// updated dest image, to ISTA3D (:335-336, :388) -- so its OS-EM step is dead work and is
+// skipped here (the ratio rows it would write are rewritten before every later read).
+static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, float lambda,
+                   cudaStream_t st)
+{
+    const KGeom &g = p->kg;
+    const size_t nimg = (size_t)g.nx * g.ny, nb = (size_t)p->g.max_batch;
+    if (!p->d_cs) {
+        cudaError_t e = cudaMalloc(&p->d_cs, sizeof(float) * 3 * nb * nimg);
+        if (e != cudaSuccess) {
+            p->d_cs = nullptr;
+            return xct_cuda_fail(e, "cudaMalloc compressed-sensing buffers");
+        }
+    }
+    float *w = p->d_cs, *beta = p->d_cs + nb * nimg, *xn = p->d_cs + 2 * nb * nimg;
+    const size_t bytes = sizeof(float) * dN * nimg;
+    const float *meas = d_sino;
+    if (p->g.correction_mode > 0) {
+        int rc = launch_sino_correction(g, d_sino, p->d_corr, p->d_corr_ang, p->d_corr_bin, p->g.correction_mode, dN,
+                                        st);
+        if (rc) return rc;
+        meas = p->d_corr;
+    }
+    XCT_CUDA_TRY(cudaMemcpyAsync(w, d_img, bytes, cudaMemcpyDeviceToDevice, st));  // w = x (:344)
+    XCT_CUDA_TRY(cudaMemsetAsync(beta, 0, bytes, st));                             // beta = 0 (:342)
+    const bool tiled = p->g.kernels == XCT_KERNELS_TILED;
+    bool first = true;
+    for (int i = 0; i < it; ++i)
+        for (int k = 0; k < p->g.ss; ++k) {
+            const int s = sub[k];
+            int rc;
+            if (first) {
+                rc = launch_ista3d(d_img, xn, g.nx, g.ny, dN, lambda, p->ctx->sm_count, st);
+                first = false;
+            } else {
+                if (tiled) {
+                    rc = launch_fwd_tiled(g, p->d_trig, d_img, meas, p->d_ratio, p->d_acc, dN, s, g.ss,
+                                          subset_rows(p, s), st);
+                    if (!rc) rc = launch_bp_update_tiled(g, p->d_trig, d_img, p->d_ratio, dN, s, st);
+                } else {
+                    rc = launch_fwd_plain(g, p->d_trig, d_img, meas, p->d_ratio, dN, s, g.ss, subset_rows(p, s), st);
+                    if (!rc) rc = launch_bp_update_plain(g, p->d_trig, d_img, p->d_ratio, dN, s, st);
+                }
+                if (!rc) rc = launch_fista3d(w, d_img, beta, xn, g.nx, g.ny, dN, lambda, p->ctx->sm_count, st);
+            }
+            if (rc) return rc;
+            XCT_CUDA_TRY(cudaMemcpyAsync(d_img, xn, bytes, cudaMemcpyDeviceToDevice, st));
+        }
+    return XCT_OK;
+}
+
+int xct_cs_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it,
+                           float cs_lambda, void *stream)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_cs_osem_run_device: null device pointer");
+    if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
+        return xct_fail(XCT_E_INVALID, "xct_cs_osem_run_device: cs_lambda must be finite and >= 0");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return cs_loop(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, cs_kernel_lambda(cs_lambda),
+                   (cudaStream_t)stream);
+}
+
+int xct_cs_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, const int *sub, int it,
+                    float cs_lambda)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
+        return xct_fail(XCT_E_INVALID, "xct_cs_osem_run: cs_lambda must be finite and >= 0");
+    const float lam = cs_kernel_lambda(cs_lambda);
+    return host_run(p, dN, sino_host, img_host, true, [&](cudaStream_t st) {
+        return cs_loop(p, dN, p->d_sino, p->d_img, sub ? sub : p->sub_default.data(), it, lam, st);
     });
 }
 

@@ -58,6 +58,8 @@ struct xct_plan {
     double *d_red = nullptr;     // [2*max_batch] focus-index sums (rotation-centre search)
     float *d_rc_prm = nullptr;   // [max_batch][16] mask constants per shift
     float *d_fi = nullptr;       // [max_batch] focus indices
+    float *d_cs = nullptr;       // compressed-sensing OS-EM: w, beta, x' [3][max_batch][ny][nx],
+                                 // allocated by the first such run
     int acc_rows = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -127,6 +129,10 @@ int launch_fbp_bp(const KGeom &g, const float2 *trig, const float *fprj, float *
 // baseUp (reconstShare.cl:87-109) with the slice minima of launch_fbp_bp, in place.
 int launch_base_up(const KGeom &g, float *img, int dN, int order, const int *min_keys, int sm_count,
                    cudaStream_t st);
+// Compressed-sensing proximal steps (xct_cs.cu): ISTA3D, FISTA3D over dN slices.
+int launch_ista3d(const float *v, float *x_new, int nx, int ny, int dN, float lambda, int sm_count, cudaStream_t st);
+int launch_fista3d(float *w, const float *v, float *beta, float *x_new, int nx, int ny, int dN, float lambda,
+                   int sm_count, cudaStream_t st);
 // Rotation-centre search (xct_rcs.cu).
 void xct_mask_params(int W, int H, float shift, float ang_min, float ang_max, float *prm16);
 float xct_shift_value(float start, float step, int i);

@@ -48,16 +48,18 @@ void join(std::thread &t)
     if (t.joinable()) t.join();
 }
 
-// output_thread (GPU.cpp:99-123): write slices startN..endN, report, free the images.
-void output_thread(int startN, int endN, std::vector<float *> imgs, bool ok)
+// output_thread (GPU.cpp:99-123): write slices startN+offset..endN (imgs[0] is slice
+// startN; the compressed-sensing batches overlap and skip their shared edge slices), report,
+// free the images.
+void output_thread(int startN, int endN, std::vector<float *> imgs, bool ok, int offset)
 {
     const size_t n = (size_t)g_ox * g_oy;
     if (ok)
-        for (int i = startN; i <= endN; ++i)
+        for (int i = startN + offset; i <= endN; ++i)
             if (!write_data_output(g_d2, slice_name(g_f2, i), imgs[i - startN], n)) fail(XCT_E_IO);
     time_t t1;
     time(&t1);
-    for (int i = startN; i <= endN; ++i)
+    for (int i = startN + offset; i <= endN; ++i)
         std::cout << "[Layer " << std::setfill('0') << std::setw(4) << i << "/" << g_st - 1 + g_num << "] "
                   << (float)(t1 - g_t0) << " s elapsed" << (ok ? "" : " (failed)") << std::endl;
     for (float *p : imgs) delete[] p;
@@ -72,13 +74,20 @@ void osem_thread(DeviceSlot *d, std::vector<float *> imgs, std::vector<float *> 
     if (g_method == METHOD_FBP) rc = xct_fbp_run(d->plan, dN, g_zp, prjs.data(), imgs.data());
     else if (g_method == METHOD_HYBRID)
         rc = xct_hybrid_run(d->plan, dN, g_zp, baseupOrder, prjs.data(), imgs.data(), g_sub.data(), g_it);
+    else if (CSitBool)  // FISTA_OSEM_execution (GPU.cpp:449-453)
+        rc = xct_cs_osem_run(d->plan, dN, prjs.data(), imgs.data(), g_sub.data(), g_it, CSlambda);
     else rc = xct_osem_run(d->plan, dN, prjs.data(), imgs.data(), g_sub.data(), g_it);
     if (rc != XCT_OK) {
         std::cerr << "ERROR: " << xct_last_error() << " (" << rc << ")" << std::endl;
         fail(rc);
     }
+    // compressed sensing: batches overlap by CSoverlap slices; inner batch edges are not
+    // written (GPU.cpp:456-460)
+    const bool cs = CSitBool && g_method == METHOD_OSEM;
+    const int offset = (cs && startN > g_st) ? CSoverlap : 0;
+    const int out_end = (cs && endN < g_st + g_num - 1) ? endN - CSoverlap : endN;
     join(d->output_th);
-    d->output_th = std::thread(output_thread, startN, endN, std::move(imgs), rc == XCT_OK);
+    d->output_th = std::thread(output_thread, startN, out_end, std::move(imgs), rc == XCT_OK, offset);
     for (float *p : prjs) delete[] p;
 }
 
@@ -158,12 +167,20 @@ int run_pipeline(const std::vector<int> &devices, const std::vector<float> &ang,
         slots.push_back(std::move(d));
     }
     const int last = g_st + g_num - 1;
+    // compressed sensing: consecutive batches overlap by 2*CSoverlap slices (GPU.cpp:636-647)
+    const int cs_delta = (CSitBool && method == METHOD_OSEM) ? CSoverlap : 0;
+    for (auto &d : slots)
+        if (d->dN - 2 * cs_delta <= 0) {
+            std::cerr << "ERROR: " << d->dN << " slices per call cannot overlap by " << cs_delta
+                      << " slices on each side (compressed sensing)" << std::endl;
+            return XCT_E_INVALID;
+        }
     for (int N = g_st; N <= last;) {
         for (auto &d : slots) {
             join(d->input_th);
             const int end = std::min(N + d->dN - 1, last);
             d->input_th = std::thread(osem_input_thread, d.get(), N, end);
-            N = end + 1;
+            N += d->dN - 2 * cs_delta;  // as the reference: a batch may start inside the last one
             if (N > last) break;
         }
     }
@@ -191,8 +208,9 @@ int GPU()
         std::cerr << "ERROR: an output size smaller than the reconstruction size is not supported" << std::endl;
         return XCT_E_INVALID;
     }
-    if (CSitBool) {
-        std::cerr << "ERROR: the compressed-sensing (FISTA) variant is not part of this build" << std::endl;
+    if (CSitBool && (g_mode == 7 || g_mode == 8)) {
+        std::cerr << "ERROR: compressed sensing is available with the OS-EM family (2, 4, 5, 6), not with method "
+                  << g_mode << std::endl;
         return XCT_E_UNSUPPORTED;
     }
     int ndev = 0;

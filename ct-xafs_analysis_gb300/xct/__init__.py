@@ -50,6 +50,7 @@ EXPORTS = (
     "xct_fbp_filter", "xct_fbp_backproject", "xct_fbp_run_device", "xct_hybrid_run_device", "xct_fbp_run",
     "xct_hybrid_run", "xct_rot_center_shift", "xct_focus_index", "xct_rot_center_search",
     "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_denoise_sinogram",
+    "xct_cs_osem_run_device", "xct_cs_osem_run",
 )
 
 
@@ -124,6 +125,9 @@ def load():
     L.xct_reslice.argtypes = [vp, ip, ip, vp, vp, vp]
     L.xct_reslice_plan_destroy.argtypes = [vp]
     L.xct_denoise_sinogram.argtypes = [ip, ip, ip, c_f, vp, vp, vp]
+    L.xct_cs_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
+    L.xct_cs_osem_run.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int), ip,
+                                  c_f]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong
@@ -268,6 +272,13 @@ class OSEMPlan:
         dN = len(sinos)
         return (fp * dN)(*[s.ctypes.data_as(fp) for s in sinos]), (fp * dN)(*[i.ctypes.data_as(fp) for i in imgs])
 
+    def cs_run(self, sinos, imgs, cs_lambda=1.0e-4, sub=None, it=-1):
+        """Compressed-sensing OS-EM (FISTA_OSEM_execution) on host arrays; the dN slices of
+        the call are the third axis of the proximal step."""
+        s_arr, i_arr = self._host_arrays(sinos, imgs)
+        _check(self._lib.xct_cs_osem_run(self.handle, len(sinos), s_arr, i_arr, self._sub(sub), it, cs_lambda))
+        return imgs
+
     def fbp_run(self, sinos, imgs, zp=0):
         """FBP (FBP_thread) on host arrays; reconstructions written into ``imgs``."""
         s_arr, i_arr = self._host_arrays(sinos, imgs)
@@ -291,6 +302,12 @@ class OSEMPlan:
         dN = d_img.shape[0] if dN is None else dN
         _check(self._lib.xct_osem_run_device(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
                                              _stream(stream)))
+
+    def cs_run_device(self, d_sino, d_img, cs_lambda=1.0e-4, dN=None, sub=None, it=-1, stream=None):
+        """Compressed-sensing OS-EM on device tensors [dN][pa][px] -> [dN][ny][nx] (in/out)."""
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_cs_osem_run_device(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
+                                                cs_lambda, _stream(stream)))
 
     def osem1(self, sub, d_img, d_sino, d_ratio, dN=None, stream=None):
         """OSEM1 (OSEM.cl:38-68) alone: ratio rows of subset ``sub`` into d_ratio."""
@@ -475,6 +492,18 @@ def OSEM_execution(plan, sub, reconst_img, prj_img, dN, it, prjCorrection=True, 
     if not prjCorrection and plan is not None and getattr(plan, "_correction", 0):
         raise XCTError(XCT_E_INVALID, "plan was built with a sinogram correction mode")
     plan.run_device(prj_img, reconst_img, dN=dN, sub=sub, it=it, stream=stream)
+    return 0
+
+
+def FISTA_OSEM_execution(plan, sub, reconst_img, prj_img, dN, it, prjCorrection=True, cs_lambda=1.0e-4,
+                         stream=None):
+    """Mirror of ``int FISTA_OSEM_execution(queue, kernels, angle_buffer, int *sub,
+    Image2DArray reconst_img, Image2DArray prj_img, int dN, int it, bool prjCorrection)``
+    (CT_reconstruction.hpp, GPU.cpp:243-405) on device tensors; CSlambda is cs_lambda.
+    Returns 0."""
+    if not prjCorrection and plan is not None and getattr(plan, "_correction", 0):
+        raise XCTError(XCT_E_INVALID, "plan was built with a sinogram correction mode")
+    plan.cs_run_device(prj_img, reconst_img, cs_lambda=cs_lambda, dN=dN, sub=sub, it=it, stream=stream)
     return 0
 
 

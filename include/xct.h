@@ -138,6 +138,21 @@ int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, const float
 int xct_osem_run_static(const xct_geom *geom, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                         void *stream);
 
+/* ---- compressed-sensing OS-EM: replaces FISTA_OSEM_execution (GPU.cpp:243-405), the
+ * path OSEM_thread takes when CSitBool is set (GPU.cpp:449-453) ----------------------
+ * Per subset: OSEM1 and OSEM2, then the proximal step of the l1 distance to the six
+ * neighbours across the dN slices of the call (ISTA3D in the first cycle, FISTA3D after,
+ * FISTA.cl:409-594), with cs_lambda = CSlambda (main.cpp:46, default 1e-4).  The slices of
+ * one call are the third axis of the neighbourhood, as in the reference (overlapping
+ * batches of CSoverlap slices are the caller's business, GPU.cpp:642-643).  The reference's
+ * own semantics are kept: the first cycle's proximal step starts from the image before that
+ * subset's OS-EM update; the lower-layer neighbour is always layer 0 (FISTA.cl:425,513).
+ * The plan allocates three image-sized buffers per slice on the first such call. */
+int xct_cs_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
+                           float cs_lambda, void *stream);
+int xct_cs_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *const *img_host, const int *sub,
+                    int it, float cs_lambda);
+
 /* ---- the two OS-EM kernels as separate steps (dN slices, device memory) -------------
  * xct_osem1 : OSEM1 (OSEM.cl:38-68) for subset `sub`: forward-projects d_img and writes
  *             the measured/estimated ratio rows of the subset into d_ratio [dN][pa][px]

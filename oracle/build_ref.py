@@ -3,8 +3,8 @@
 TEST INFRASTRUCTURE ONLY.  The reference (NozomuIshiguro/CT-XAFS_analysis) has no tests
 and no CPU build; its kernels are OpenCL C JIT-compiled at run time with the problem shape
 as -D macros (CT_reconstruction/GPU.cpp:537-550).  This recipe compiles
-CT_reconstruction/FBP.cl, CT_reconstruction/OSEM.cl and CT_reconstruction/reconstShare.cl,
-where they lie in the reference checkout, with g++ against oracle/ref_shim/cl_shim.hpp (an
+CT_reconstruction/FBP.cl, OSEM.cl, FISTA.cl and reconstShare.cl (OSEM_programBuild builds the
+last three as one program, GPU.cpp:527-535), where they lie in the reference checkout, with g++ against oracle/ref_shim/cl_shim.hpp (an
 OpenCL-C environment written for this project).  The only changes to the kernel text are
 mechanical and happen in the build output: OpenCL vector literals ``(float4)(a,b,c,d)``
 become constructor calls ``float4(a,b,c,d)`` (C++ would parse the former as a comma
@@ -25,7 +25,8 @@ import hashlib
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_ROOT = os.environ.get("XCT_REFERENCE_ROOT", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
-KERNELS = ("CT_reconstruction/FBP.cl", "CT_reconstruction/OSEM.cl", "CT_reconstruction/reconstShare.cl")
+KERNELS = ("CT_reconstruction/FBP.cl", "CT_reconstruction/OSEM.cl", "CT_reconstruction/FISTA.cl",
+           "CT_reconstruction/reconstShare.cl")
 _VEC = re.compile(r"\((float|int|uint)([234])\)\s*\(")
 _SWZ = re.compile(r"\.(xx|yy|yx)\b")
 _GLOBAL = re.compile(r"(?<![_\w])global(?=\s)")
@@ -50,8 +51,9 @@ def default_zp(px):
     return zp
 
 
-def build(nx, ny, px, pa, ss, zp=None, force=False):
-    """Compile the reference kernels for one shape; return the .so path."""
+def build(nx, ny, px, pa, ss, zp=None, force=False, cs_lambda="0.0001"):
+    """Compile the reference kernels for one shape; return the .so path.  cs_lambda is the
+    text of -D LAMBDA_FISTA (the reference streams the float CSlambda, GPU.cpp:549)."""
     zp = default_zp(px) if zp is None else int(zp)
     if not available():
         raise FileNotFoundError("reference kernel sources not found under %s" % REF_ROOT)
@@ -64,7 +66,7 @@ def build(nx, ny, px, pa, ss, zp=None, force=False):
     parts.append("}  // namespace clk")
     parts.append('#include "%s"' % os.path.join(HERE, "ref_shim", "ref_driver.inc"))
     src = "\n".join(parts) + "\n"
-    tag = "%dx%d_%dx%d_s%d_zp%d" % (nx, ny, px, pa, ss, zp)
+    tag = "%dx%d_%dx%d_s%d_zp%d_l%s" % (nx, ny, px, pa, ss, zp, cs_lambda)
     h = hashlib.sha1(src.encode())
     for dep in ("cl_shim.hpp", "ref_driver.inc"):
         with open(os.path.join(HERE, "ref_shim", dep), "rb") as f:
@@ -79,7 +81,7 @@ def build(nx, ny, px, pa, ss, zp=None, force=False):
     defs = [
         "-DIMAGESIZE_X=%d" % nx, "-DIMAGESIZE_Y=%d" % ny, "-DIMAGESIZE_M=%d" % (nx * ny),
         "-DDEPTHSIZE=%d" % max(nx, ny), "-DPRJ_IMAGESIZE=%d" % px, "-DPRJ_ANGLESIZE=%d" % pa,
-        "-DPRJ_IMAGESIZE_M=%d" % (px * pa), "-DSS=%d" % ss, "-DLAMBDA_FISTA=0.0001", "-DZP_SIZE=%d" % zp,
+        "-DPRJ_IMAGESIZE_M=%d" % (px * pa), "-DSS=%d" % ss, "-DLAMBDA_FISTA=%s" % cs_lambda, "-DZP_SIZE=%d" % zp,
     ]
     cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-shared", "-fPIC",
            "-w", "-o", so, cpp] + defs

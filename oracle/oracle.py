@@ -88,6 +88,8 @@ def lib():
         L.xo_reslice_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, fp, ctypes.c_float,
                                      ctypes.c_int, fp]
         L.xo_denoise_sinogram_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp]
+        L.xo_ista3d_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp]
+        L.xo_fista3d_f32.argtypes = [fp, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp, fp, fp]
         L.xo_trig_f32.argtypes = [fp, ctypes.c_int, fp]
         L.xo_trig_f64.argtypes = [fp, ctypes.c_int, dp]
         L.xo_subset_order.argtypes = [ctypes.c_int, ip]
@@ -298,6 +300,58 @@ def denoise_sinogram(sino, threshold):
     return out
 
 
+def cs_lambda(cs_lambda_f32):
+    """The kernels' float lambda: -D LAMBDA_FISTA is the float CSlambda streamed with six
+    significant digits (GPU.cpp:549), parsed as a double literal; lambda =
+    LAMBDA_FISTA/L*0.5f with L = 0.5 (FISTA.cl:426, GPU.cpp:343)."""
+    d = float("%g" % np.float32(cs_lambda_f32))
+    return float(np.float32(d / float(np.float32(0.5)) * 0.5))
+
+
+def ista3d(v, lam):
+    v = np.ascontiguousarray(v, dtype=np.float32)
+    dN, ny, nx = v.shape
+    out = np.empty_like(v)
+    lib().xo_ista3d_f32(_p(v), nx, ny, dN, lam, _p(out))
+    return out
+
+
+def fista3d(x_in, v, beta, lam):
+    x_in = np.ascontiguousarray(x_in, dtype=np.float32)
+    v = np.ascontiguousarray(v, dtype=np.float32)
+    beta = np.ascontiguousarray(beta, dtype=np.float32)
+    dN, ny, nx = v.shape
+    w, x, b = np.empty_like(v), np.empty_like(v), np.empty_like(v)
+    lib().xo_fista3d_f32(_p(x_in), _p(v), _p(beta), nx, ny, dN, lam, _p(w), _p(x), _p(b))
+    return w, x, b
+
+
+def cs_osem_run(imgs, meas, angles_deg, ss, it, cs_lambda_f32=1.0e-4, sub_order=None, order=ORDER_LITERAL):
+    """FISTA_OSEM_execution (GPU.cpp:243-405) on a batch imgs [dN][ny][nx], meas [dN][pa][px]:
+    per subset OSEM1 + OSEM2 of every slice, then ISTA3D of the PRE-update image in the first
+    cycle (its OS-EM update is discarded, as the reference's kernel arguments have it) and
+    FISTA3D(w, v = the OS-EM update, beta) after; the image becomes the proximal result."""
+    x = np.array(imgs, dtype=np.float32, copy=True, order="C")
+    meas = np.ascontiguousarray(meas, dtype=np.float32)
+    dN, ny, nx = x.shape
+    so = subset_order(ss) if sub_order is None else np.ascontiguousarray(sub_order, dtype=np.int32)
+    lam = cs_lambda(cs_lambda_f32)
+    w = x.copy()
+    beta = np.zeros_like(x)
+    first = True
+    for _ in range(it):
+        for k in range(ss):
+            s = int(so[k])
+            v = np.stack([osem2(x[z], osem1(x[z], meas[z], angles_deg, ss, s, order=order), angles_deg, ss, s,
+                                order=order) for z in range(dN)])
+            if first:
+                x = ista3d(x, lam)
+                first = False
+            else:
+                w, x, beta = fista3d(w, v, beta, lam)
+    return x
+
+
 def adjoint(sino, angles_deg, nx, ny, cx=None, dtype=np.float32):
     """Exact adjoint A^T of projection() over all angles."""
     sino = np.ascontiguousarray(sino, dtype=dtype)
@@ -353,6 +407,15 @@ class RefKernels:
         self.lib.ref_fbp.argtypes = [fp, fp, ctypes.c_int, fp, fp]
         self.lib.ref_bp_fbp.argtypes = [fp, fp, ctypes.c_int, fp]
         self.lib.ref_base_up.argtypes = [fp, ctypes.c_int, ctypes.c_int, fp]
+        self.lib.ref_fista_osem_execution.argtypes = [fp, fp, fp, ip, ctypes.c_int, ctypes.c_int]
+
+    def fista_osem_execution(self, imgs, prjs, angles_deg, sub_order, it):
+        imgs = np.array(imgs, dtype=np.float32, copy=True, order="C")
+        prjs = np.ascontiguousarray(prjs, dtype=np.float32)
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        so = np.ascontiguousarray(sub_order, dtype=np.int32)
+        self.lib.ref_fista_osem_execution(_p(imgs), _p(prjs), _p(ang), _p(so), imgs.shape[0], it)
+        return imgs
 
     def fbp(self, prjs, angles_deg):
         """FBP_execution: returns (filtered sinograms, images), one per layer."""

@@ -21,6 +21,8 @@
  *                                                    xo_mask_*, xo_set_mask_f32, xo_focus_index
  *   - reslice and denoiseSinogram (Reslice/reslice.cl:52-71, 223-248) -> xo_reslice_f32,
  *                                                    xo_denoise_sinogram_f32
+ *   - the compressed-sensing proximal steps ISTA3D / FISTA3D (FISTA.cl:409-594)
+ *                                                 -> xo_ista3d_f32, xo_fista3d_f32
  *
  * Parity pin: the reference ships no tests, fixtures or golden vectors, and its OpenCL
  * runtime is not available, so the pin is oracle/_ref: the reference's own OSEM.cl and
@@ -485,4 +487,84 @@ void xo_denoise_sinogram_f32(const float *src, int W, int A, int H, float thresh
                     ((d1 > threshold && d2 < -threshold) || (d1 < -threshold && d2 > threshold)) ? c : f1;
             }
         }
+}
+
+
+/* ------------------------------------------------- compressed sensing (ISTA3D / FISTA3D)
+ * Per voxel (FISTA.cl:409-494): the six neighbours of v -- x+1, x-1, y+1, y-1 (zero outside
+ * the slice), layer min(Z+1, dN-1), and layer 0 (the kernels take fmin(Z-1, 0), :425) --
+ * sorted in descending order by the kernel's exchange loop; then the candidate chain
+ * x = v - 6l, n0, v - 4l, n1, v - 2l, n2, v, n3, v + 2l, n4, v + 4l, n5, v + 6l selected by
+ * v < n0 + 6l, n0 + 4l, n1 + 4l, n1 + 2l, n2 + 2l, n2, n3, n3 - 2l, n4 - 2l, n4 - 4l,
+ * n5 - 4l, n5 - 6l (the last true comparison wins): the minimiser of
+ * (x - v)^2/2 + l sum_k |x - n_k| (the l1 distance to the neighbours).  ISTA3D then floors
+ * at 1e-6 (NaN -> 1e-6). */
+static float xo_cs_select(const float *v, int nx, int ny, int dN, int X, int Y, int Z, float lambda)
+{
+    const size_t m = (size_t)nx * ny;
+    const float *vz = v + (size_t)Z * m;
+    float nb[6];
+    nb[0] = xo_tex2(vz, nx, ny, X + 1, Y);
+    nb[1] = xo_tex2(vz, nx, ny, X - 1, Y);
+    nb[2] = xo_tex2(vz, nx, ny, X, Y + 1);
+    nb[3] = xo_tex2(vz, nx, ny, X, Y - 1);
+    const int zp = Z + 1 < dN - 1 ? Z + 1 : dN - 1;
+    nb[4] = v[(size_t)zp * m + (size_t)Y * nx + X];
+    nb[5] = v[(size_t)Y * nx + X];
+    const float vi = vz[(size_t)Y * nx + X];
+    for (int i = 0; i < 6; ++i) {
+        const float img1 = nb[i];
+        float img2 = img1;
+        int bigger = i;
+        for (int j = i + 1; j < 6; ++j) {
+            bigger = (nb[j] > img2) ? j : bigger;
+            img2 = (nb[j] > img2) ? nb[j] : img2;
+        }
+        nb[i] = img2;
+        nb[bigger] = img1;
+    }
+    const float l2 = 2.0f * lambda, l4 = 4.0f * lambda, l6 = 6.0f * lambda;
+    const float cnd[13] = {vi - l6, nb[0], vi - l4, nb[1], vi - l2, nb[2], vi,
+                           nb[3],   vi + l2, nb[4], vi + l4, nb[5], vi + l6};
+    const float rng[12] = {nb[0] + l6, nb[0] + l4, nb[1] + l4, nb[1] + l2, nb[2] + l2, nb[2],
+                           nb[3],      nb[3] - l2, nb[4] - l2, nb[4] - l4, nb[5] - l4, nb[5] - l6};
+    float x = cnd[0];
+    for (int i = 0; i < 12; ++i) x = (vi < rng[i]) ? cnd[i + 1] : x;
+    return x;
+}
+
+void xo_ista3d_f32(const float *v, int nx, int ny, int dN, float lambda, float *x_new)
+{
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int Z = 0; Z < dN; ++Z)
+        for (int Y = 0; Y < ny; ++Y)
+            for (int X = 0; X < nx; ++X) {
+                float x = xo_cs_select(v, nx, ny, dN, X, Y, Z, lambda);
+                x = fmaxf(1.0e-6f, x);
+                x = (x != x) ? 1.0e-6f : x;
+                x_new[((size_t)Z * ny + Y) * nx + X] = x;
+            }
+}
+
+/* FISTA3D (FISTA.cl:497-594): the same selection on v (no floor), then
+ * beta' = (sqrt(4 beta^2 + 1) + 1)/2, gamma = (beta - 1)/beta',
+ * w' = gamma x' + (1 - gamma) x_in (NaN -> 1e-6), all in float as written. */
+void xo_fista3d_f32(const float *x_in, const float *v, const float *beta, int nx, int ny, int dN, float lambda,
+                    float *w_new, float *x_new, float *beta_new)
+{
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int Z = 0; Z < dN; ++Z)
+        for (int Y = 0; Y < ny; ++Y)
+            for (int X = 0; X < nx; ++X) {
+                const size_t i = ((size_t)Z * ny + Y) * nx + X;
+                const float xi = x_in[i], b = beta[i];
+                const float x = xo_cs_select(v, nx, ny, dN, X, Y, Z, lambda);
+                x_new[i] = x;
+                float bn = b * b * 4.0f + 1.0f;
+                bn = (sqrtf(bn) + 1.0f) * 0.5f;
+                const float g = (b - 1.0f) / bn;
+                beta_new[i] = bn;
+                float w = g * x + (1.0f - g) * xi;
+                w_new[i] = (w != w) ? 1.0e-6f : w;
+            }
 }

@@ -61,6 +61,12 @@ void xo_reslice_f32(const float *mt, int W, int H, int A, const float *xs, const
                     int correction, float *prj);
 void xo_denoise_sinogram_f32(const float *src, int W, int A, int H, float threshold, float *dst);
 
+/* Compressed-sensing OS-EM (FISTA_OSEM_execution): ISTA3D and FISTA3D (FISTA.cl:409-594) on
+ * a batch of dN images [dN][ny][nx]; lambda is the kernels' float lambda. */
+void xo_ista3d_f32(const float *v, int nx, int ny, int dN, float lambda, float *x_new);
+void xo_fista3d_f32(const float *x_in, const float *v, const float *beta, int nx, int ny, int dN, float lambda,
+                    float *w_new, float *x_new, float *beta_new);
+
 #define XO_DECL(T, S)                                                                                   \
     void xo_projection##S(const T *img, const T *cs, const xo_geom *g, int sub, int ss, int nrows, T *prj); \
     void xo_osem1##S(const T *img, const T *meas, const T *cs, const xo_geom *g, int sub, int nrows,      \

@@ -29,6 +29,9 @@ Fixtures (np.savez_compressed):
                  (uniform 0.5..1.5, seed 16) with per-angle shifts U[-2.5, 2.5] (x) and
                  U[-1.5, 1.5] (y), baseup 0.125, without and with the cosine correction,
                  and denoiseSinogram (threshold 0.3) of the first result with planted spikes.
+  cs_64.npz      compressed-sensing OS-EM (FISTA_OSEM_execution with ISTA3D/FISTA3D) of a
+                 batch of 3 slices of a 64x64x3 ellipsoid phantom (seed 4), 90 angles, 64 bins,
+                 I0 = 1e4 (seeds 0..2), 10 subsets x 2 iterations, CSlambda 1e-4, from 1.0.
 """
 import os
 import sys
@@ -166,6 +169,27 @@ def reslice_case(name, A, H, W, seed, baseup, threshold):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
 
 
+def cs_case(name, n, px, pa, ss, it, dN, lam, seed, i0):
+    ang = P.uniform_angles(pa)
+    prm = P.ellipsoid_params(n, dN, count=6, seed=seed)
+    meas = np.stack([P.noisy_log_sinogram(O.projection(P.ellipsoid_slice(prm, z, n, n), ang, px, order=LIT), i0, z)
+                     for z in range(dN)])
+    x0 = np.ones((dN, n, n), np.float32)
+    sub = O.subset_order(ss)
+    out = O.cs_osem_run(x0, meas, ang, ss, it, lam, sub, order=LIT)
+    out_gpu_order = O.cs_osem_run(x0, meas, ang, ss, it, lam, sub, order=O.ORDER_GPU)
+    arrays = dict(angles=ang, meas=meas, x0=x0, sub=sub, cs=out, cs_gpu_order=out_gpu_order,
+                  shape=np.array([n, px, pa, ss, it, dN], np.int32), cs_lambda=np.array([lam], np.float32))
+    if O.ref_available():
+        ref = O.RefKernels(n, n, px, pa, ss)
+        assert np.array_equal(ref.fista_osem_execution(x0, meas, ang, sub, it), out), name + ": CS OS-EM differs"
+        arrays["pinned_by_reference_kernels"] = np.array([1], np.int32)
+        print(name, "pinned: bit-identical to the reference kernels")
+    else:
+        arrays["pinned_by_reference_kernels"] = np.array([0], np.int32)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+
+
 if __name__ == "__main__":
     O.build()
     case("small_64", 64, 64, 64, 90, 10, 2, 10, 1, 1e5, 11)
@@ -175,3 +199,4 @@ if __name__ == "__main__":
     fbp_case("fbp_odd", 48, 40, 57, 37, 256, 1, 2, 4, 6, 7, 1e5, 14)
     rcs_case("rcs_64", 64, 64, 90, 10, 9, -2.0, 0.5, 1.0, 5, 1e5, 15, 64)
     reslice_case("reslice_small", 16, 12, 24, 16, 0.125, 0.3)
+    cs_case("cs_64", 64, 64, 90, 10, 2, 3, 1.0e-4, 4, 1e4)

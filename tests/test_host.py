@@ -19,13 +19,13 @@ def host_bin(xct_lib):
 # an .inp as the reference reads it: key lines, values on the next line (CRLF on some)
 INP_KEYS = [
     ("#Open CL Platform & Device No", "1"),
-    ("#Number of Parallel processing per one device", "4"),
+    ("#Number of Parallel processing per one device", "{par}"),
     ("#測定ファイルディレクトリパス", "{d1}"),
     ("#測定ファイル名", "s****.raw"),
     ("#出力ファイルディレクトリパス", "{d2}"),
     ("#出力ファイル名", "rec_****.img"),
     ("#ログファイルパス", "{f3}"),
-    ("#レイヤー数", "3"),
+    ("#レイヤー数", "{layers}"),
     ("#開始ナンバー", "7"),
     ("#初期画像の使用 1:Yes 2: No", "2"),
     ("#カメラピクセル数", "{px}"),
@@ -40,6 +40,8 @@ INP_KEYS = [
 
 def write_inp(path, extra=(), **kw):
     kw.setdefault("method", 6)
+    kw.setdefault("layers", 3)
+    kw.setdefault("par", 4)
     with open(path, "wb") as f:
         for i, (k, v) in enumerate(list(INP_KEYS) + list(extra)):
             eol = b"\r\n" if i % 3 == 0 else b"\n"
@@ -129,3 +131,40 @@ def test_fbp_and_hybrid_methods_from_files(host_bin, oracle_lib, tmp_path, metho
             ref = O.osem_run(O.base_up(ref, order)[0], meas[z], ang, ss, it, order=O.ORDER_LITERAL)
         rel = np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)
         assert rel <= (2e-5 if method == 7 else 1e-4), (z, rel)
+
+
+@pytest.mark.gpu
+def test_compressed_sensing_batches_from_files(host_bin, oracle_lib, tmp_path):
+    """CSitBool with 4 slices per call overlapping by 1 (GPU.cpp:636-647, 449-460): slices
+    7..12 run as batches [7..10], [9..12] and -- the dispatcher steps by dN - 2 while the start
+    is in range -- [11..12]; each slice file holds the batch that writes it last."""
+    from xct import phantom as P
+    O = oracle_lib
+    n, px, pa, ss, it = 48, 48, 40, 4, 2
+    ang = P.uniform_angles(pa)
+    d1, d2 = tmp_path / "in", tmp_path / "out"
+    d1.mkdir()
+    with open(tmp_path / "angles.log", "w") as f:
+        for a in ang:
+            f.write("%.9g\n" % a)
+    prm = P.ellipsoid_params(n, 6, count=5, seed=9)
+    meas = {}
+    for z in range(7, 13):
+        meas[z] = P.noisy_log_sinogram(O.projection(P.ellipsoid_slice(prm, z - 7, n, n), ang, px), 1e4, z)
+        meas[z].astype(np.float32).tofile(d1 / ("s%04d.raw" % z))
+    inp = tmp_path / "run.inp"
+    keys = [("#逐次圧縮センシング計算 (FBP適応外)", "1"), ("#逐次圧縮センシング計算加算ファクター", "0.0002"),
+            ("#逐次圧縮センシング計算重複レイヤー数", "1")]
+    write_inp(inp, extra=keys, d1=str(d1), d2=str(d2), f3=str(tmp_path / "angles.log"), px=px, pa=pa, n=n, it=it,
+              ss=ss, layers=6, par=4)
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    x0 = np.ones((4, n, n), np.float32)
+    b1 = O.cs_osem_run(x0, np.stack([meas[z] for z in range(7, 11)]), ang, ss, it, 2e-4)
+    b2 = O.cs_osem_run(x0, np.stack([meas[z] for z in range(9, 13)]), ang, ss, it, 2e-4)
+    b3 = O.cs_osem_run(x0[:2], np.stack([meas[z] for z in range(11, 13)]), ang, ss, it, 2e-4)
+    want = {7: b1[0], 8: b1[1], 9: b1[2], 10: b2[1], 11: b2[2], 12: b3[1]}
+    for z, ref in want.items():
+        got = np.fromfile(d2 / ("rec_%04d.img" % z), np.float32).reshape(n, n)
+        rel = np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)
+        assert rel <= 1e-4, (z, rel)

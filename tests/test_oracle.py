@@ -406,3 +406,50 @@ def test_reslice_oracle_bit_identical_to_reference_kernels(oracle_lib, shape):
     s[:, 5, :] += 3.0
     for thr in (0.5, 2.0):
         assert np.array_equal(R.denoise(s, thr), O.denoise_sinogram(s, thr))
+
+
+# --------------------------------------------------------------- compressed sensing
+def test_cs_oracle_reproduces_golden(oracle_lib):
+    O = oracle_lib
+    f = _load("cs_64")
+    n, px, pa, ss, it, dN = [int(v) for v in f["shape"]]
+    lam = float(f["cs_lambda"][0])
+    out = O.cs_osem_run(f["x0"], f["meas"], f["angles"], ss, it, lam, f["sub"], order=O.ORDER_LITERAL)
+    assert np.array_equal(out, f["cs"])
+
+
+def test_cs_proximal_known_answers(oracle_lib):
+    """Interior voxels of a constant volume are fixed points of ISTA3D/FISTA3D's selection;
+    a lone bright voxel moves toward its neighbours by 6 lambda (the l1 pull of six
+    neighbours); lambda follows the reference's six-digit text of CSlambda."""
+    O = oracle_lib
+    lam = O.cs_lambda(1e-4)
+    assert lam == np.float32(1e-4)
+    assert O.cs_lambda(np.float32(1.2345678e-3)) == np.float32(1.23457e-3)
+    v = np.full((3, 8, 8), 0.5, np.float32)
+    x = O.ista3d(v, lam)
+    assert np.all(x[1:, 1:-1, 1:-1] == np.float32(0.5))
+    v2 = v.copy()
+    v2[1, 4, 4] = 0.9
+    x2 = O.ista3d(v2, lam)
+    assert x2[1, 4, 4] == np.float32(np.float32(0.9) - np.float32(6.0) * np.float32(lam))
+    w, xf, b = O.fista3d(v, v, np.zeros_like(v), lam)
+    assert np.all(b == 1.0) and np.all(xf[1:, 1:-1, 1:-1] == np.float32(0.5))
+
+
+@pytest.mark.parametrize("shape", [(48, 56, 36, 4, 4, 2), (40, 40, 30, 3, 2, 3)])
+def test_cs_oracle_bit_identical_to_reference_kernels(oracle_lib, shape):
+    O = oracle_lib
+    if not O.ref_available():
+        pytest.skip("reference checkout not present")
+    from xct import phantom as P
+    n, px, pa, ss, dN, it = shape
+    ang = (np.sort(np.random.default_rng(n).uniform(0, 180, pa))).astype(np.float32)
+    prm = P.ellipsoid_params(n, dN, count=5, seed=7)
+    meas = np.stack([P.noisy_log_sinogram(O.projection(P.ellipsoid_slice(prm, z, n, n), ang, px), 1e4, z)
+                     for z in range(dN)])
+    x0 = np.full((dN, n, n), 0.7, np.float32)
+    so = O.subset_order(ss)
+    ref = O.RefKernels(n, n, px, pa, ss)
+    assert np.array_equal(ref.fista_osem_execution(x0, meas, ang, so, it),
+                          O.cs_osem_run(x0, meas, ang, ss, it, 1e-4, so, order=O.ORDER_LITERAL))
