@@ -149,6 +149,10 @@ static void plan_free(xct_plan *p)
     cudaFree(p->d_rc_prm);
     cudaFree(p->d_fi);
     cudaFree(p->d_cs);
+    cudaFree(p->d_sino2);
+    cudaFree(p->d_img2);
+    if (p->s_h2d) cudaStreamDestroy(p->s_h2d);
+    if (p->s_d2h) cudaStreamDestroy(p->s_d2h);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -211,6 +215,7 @@ int xct_osem_plan_create(xct_ctx *ctx, const xct_geom *geom, xct_plan **out)
     k.hd = (float)k.depth * 0.5f;
     k.cx = geom->center_bin < 0.0f ? (float)geom->px * 0.5f : geom->center_bin;
     k.fetch = geom->measured_fetch_mode;
+    xct_plan_default_tuning(p);  // cached choice for this shape, else the default rule
 
     auto fail = [&](cudaError_t e, const char *what) {
         int r = xct_cuda_fail(e, what);
@@ -645,6 +650,94 @@ int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *c
     return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
         return hybrid_device(p, dN, zp, baseup_order, p->d_sino, p->d_img, sub, it, st);
     });
+}
+
+// --------------------------------------------------------------- streamed full volume
+// OS-EM of n slices held in host memory, max_batch slices per device batch, two staging sets
+// on the device: batch b computes on the plan stream while batch b+1's sinograms and initial
+// images go up on an upload stream and batch b-1's images come down on a download stream;
+// events order each staging set's reuse.  The volume never needs to fit in HBM.
+int xct_osem_run_volume(xct_plan *p, int n, const float *const *sino_host, float *const *img_host, const int *sub,
+                        int it)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, 1, sub, it);
+    if (rc) return rc;
+    if (n <= 0 || !sino_host || !img_host) return xct_fail(XCT_E_INVALID, "xct_osem_run_volume: bad arguments");
+    for (int i = 0; i < n; ++i)
+        if (!sino_host[i] || !img_host[i]) return xct_fail(XCT_E_INVALID, "xct_osem_run_volume: null slice pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    const size_t nimg = (size_t)p->g.nx * p->g.ny, nprj = (size_t)p->g.px * p->g.pa, nb = (size_t)p->g.max_batch;
+    if (!p->d_sino2) {
+        XCT_CUDA_TRY(cudaMalloc(&p->d_sino2, sizeof(float) * nb * nprj));
+        cudaError_t e = cudaMalloc(&p->d_img2, sizeof(float) * nb * nimg);
+        if (e != cudaSuccess) {
+            cudaFree(p->d_sino2);
+            p->d_sino2 = nullptr;
+            return xct_cuda_fail(e, "cudaMalloc volume staging");
+        }
+        XCT_CUDA_TRY(cudaStreamCreateWithFlags(&p->s_h2d, cudaStreamNonBlocking));
+        XCT_CUDA_TRY(cudaStreamCreateWithFlags(&p->s_d2h, cudaStreamNonBlocking));
+    }
+    float *dsino[2] = {p->d_sino, p->d_sino2}, *dimg[2] = {p->d_img, p->d_img2};
+    const int *so = sub ? sub : p->sub_default.data();
+    cudaEvent_t up[2], done[2], down[2];
+    for (int k = 0; k < 2; ++k) {
+        XCT_CUDA_TRY(cudaEventCreateWithFlags(&up[k], cudaEventDisableTiming));
+        XCT_CUDA_TRY(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming));
+        XCT_CUDA_TRY(cudaEventCreateWithFlags(&down[k], cudaEventDisableTiming));
+    }
+    auto cleanup = [&]() {
+        for (int k = 0; k < 2; ++k) {
+            cudaEventDestroy(up[k]);
+            cudaEventDestroy(done[k]);
+            cudaEventDestroy(down[k]);
+        }
+    };
+    auto upload = [&](int b) -> int {
+        const int s = b & 1, z0 = b * p->g.max_batch, dn = std::min(p->g.max_batch, n - z0);
+        if (b >= 2) XCT_CUDA_TRY(cudaStreamWaitEvent(p->s_h2d, down[s], 0));  // set s is free again
+        for (int i = 0; i < dn; ++i) {
+            XCT_CUDA_TRY(cudaMemcpyAsync(dsino[s] + i * nprj, sino_host[z0 + i], sizeof(float) * nprj,
+                                         cudaMemcpyHostToDevice, p->s_h2d));
+            XCT_CUDA_TRY(cudaMemcpyAsync(dimg[s] + i * nimg, img_host[z0 + i], sizeof(float) * nimg,
+                                         cudaMemcpyHostToDevice, p->s_h2d));
+        }
+        XCT_CUDA_TRY(cudaEventRecord(up[s], p->s_h2d));
+        return XCT_OK;
+    };
+    const int nbatch = (int)((n + nb - 1) / nb);
+    XCT_CUDA_TRY(cudaEventRecord(p->ev0, p->stream));
+    rc = upload(0);
+    for (int b = 0; b < nbatch && rc == XCT_OK; ++b) {
+        const int s = b & 1, z0 = b * p->g.max_batch, dn = std::min(p->g.max_batch, n - z0);
+        if (b + 1 < nbatch && (rc = upload(b + 1))) break;
+        cudaError_t e = cudaStreamWaitEvent(p->stream, up[s], 0);
+        if (e != cudaSuccess) {
+            rc = xct_cuda_fail(e, "volume wait");
+            break;
+        }
+        if ((rc = osem_loop(p, dn, dsino[s], dimg[s], so, it, p->stream))) break;
+        cudaEventRecord(done[s], p->stream);
+        cudaStreamWaitEvent(p->s_d2h, done[s], 0);
+        for (int i = 0; i < dn && rc == XCT_OK; ++i) {
+            e = cudaMemcpyAsync(img_host[z0 + i], dimg[s] + i * nimg, sizeof(float) * nimg, cudaMemcpyDeviceToHost,
+                                p->s_d2h);
+            if (e != cudaSuccess) rc = xct_cuda_fail(e, "volume download");
+        }
+        cudaEventRecord(down[s], p->s_d2h);
+    }
+    cudaError_t e1 = cudaStreamSynchronize(p->s_d2h), e2 = cudaStreamSynchronize(p->stream),
+                e3 = cudaStreamSynchronize(p->s_h2d);
+    if (rc == XCT_OK && (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess))
+        rc = xct_cuda_fail(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3), "xct_osem_run_volume: sync");
+    if (rc == XCT_OK) {
+        cudaEventRecord(p->ev1, p->stream);
+        cudaEventSynchronize(p->ev1);
+        cudaEventElapsedTime(&p->last_ms, p->ev0, p->ev1);
+    }
+    cleanup();
+    return rc;
 }
 
 // ------------------------------------------------------ compressed-sensing OS-EM (FISTA)

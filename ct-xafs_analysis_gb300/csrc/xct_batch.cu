@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "xct_internal.h"
@@ -31,6 +32,10 @@ struct xct_batch_plan {
     float *d_ratio = nullptr;
     double *d_acc = nullptr;
     int grids[3] = {0, 0, 0};
+    int fwd_T = 92, fwd_chunk = 128;  // forward tiles of every slice (autotuned, cached)
+    std::vector<int> bases;           // [3][n+1] work-unit prefix sums for fwd_T, fwd_chunk
+    size_t n_acc = 0;
+    std::string key;                  // tune-cache key of the batch's shapes
     cudaStream_t cap = nullptr;       // capture stream
     cudaGraphExec_t exec = nullptr;
     size_t queue_bytes = 0;
@@ -48,6 +53,34 @@ static void batch_free(xct_batch_plan *p)
     cudaFree(p->d_ratio);
     cudaFree(p->d_acc);
     delete p;
+}
+
+// Forward tiles (T, chunk) for every slice: work units, their prefix sums (uploaded), the
+// persistent grids; a captured graph is dropped (the next run captures again).
+static int batch_layout(xct_batch_plan *p, int T, int chunk)
+{
+    const int n = p->n;
+    p->bases.assign(3 * (size_t)(n + 1), 0);
+    for (int i = 0; i < n; ++i) {
+        XctItemDev &d = p->host[i];
+        d.g.fwd_T = T;
+        d.g.fwd_chunk = chunk;
+        int fu, fin, bu;
+        xct_batched_units(d.g, d.fwd_ntx, d.fwd_nty, fu, fin, d.bp_ntx, bu);
+        p->bases[0 * (n + 1) + i + 1] = p->bases[0 * (n + 1) + i] + fu;
+        p->bases[1 * (n + 1) + i + 1] = p->bases[1 * (n + 1) + i] + fin;
+        p->bases[2 * (n + 1) + i + 1] = p->bases[2 * (n + 1) + i] + bu;
+    }
+    XCT_CUDA_TRY(cudaMemcpy(p->d_bases, p->bases.data(), sizeof(int) * p->bases.size(), cudaMemcpyHostToDevice));
+    int rc = xct_batched_grids(p->ctx->device, p->ctx->sm_count, T, p->grids);
+    if (rc) return rc;
+    p->fwd_T = T;
+    p->fwd_chunk = chunk;
+    if (p->exec) {
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+    }
+    return XCT_OK;
 }
 
 extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms, int it, xct_batch_plan **out)
@@ -78,8 +111,7 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         batch_free(p);
         return r;
     };
-    // sizes and unit tables
-    std::vector<int> bases(3 * (size_t)(n + 1), 0);
+    // sizes
     size_t n_trig = 0, n_ratio = 0, n_acc = 0;
     p->host.resize(n);
     for (int i = 0; i < n; ++i) {
@@ -98,18 +130,15 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         k.cx = g.center_bin < 0.0f ? (float)g.px * 0.5f : g.center_bin;
         k.fetch = g.measured_fetch_mode;
         d.cover = g.subset_mode == XCT_SUBSETS_COVER;
-        int fu, fin, bu;
-        xct_batched_units(k, d.fwd_ntx, d.fwd_nty, fu, fin, d.bp_ntx, bu);
-        bases[0 * (n + 1) + i + 1] = bases[0 * (n + 1) + i] + fu;
-        bases[1 * (n + 1) + i + 1] = bases[1 * (n + 1) + i] + fin;
-        bases[2 * (n + 1) + i + 1] = bases[2 * (n + 1) + i] + bu;
         n_trig += g.pa;
         n_ratio += (size_t)g.pa * g.px;
         n_acc += (size_t)((g.pa + g.ss - 1) / g.ss) * g.px;
     }
     cudaError_t e;
     if ((e = cudaMalloc(&p->d_items, sizeof(XctItemDev) * n)) != cudaSuccess) return fail(e, "cudaMalloc items");
-    if ((e = cudaMalloc(&p->d_bases, sizeof(int) * bases.size())) != cudaSuccess) return fail(e, "cudaMalloc bases");
+    if ((e = cudaMalloc(&p->d_bases, sizeof(int) * 3 * (size_t)(n + 1))) != cudaSuccess)
+        return fail(e, "cudaMalloc bases");
+    p->n_acc = n_acc;
     p->queue_bytes = sizeof(int) * 3 * (size_t)std::max(1, it * ss);
     if ((e = cudaMalloc(&p->d_queues, p->queue_bytes)) != cudaSuccess) return fail(e, "cudaMalloc queues");
     if ((e = cudaMalloc(&p->d_trig, sizeof(float2) * n_trig)) != cudaSuccess) return fail(e, "cudaMalloc trig");
@@ -136,9 +165,29 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         orat += (size_t)g.pa * g.px;
         oacc += (size_t)((g.pa + g.ss - 1) / g.ss) * g.px;
     }
-    if ((e = cudaMemcpy(p->d_bases, bases.data(), sizeof(int) * bases.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-        return fail(e, "upload bases");
-    int rc = xct_batched_grids(ctx->device, ctx->sm_count, p->grids);
+    // forward tiles: this batch's cached choice, else the default rule
+    unsigned long long h = 1469598103934665603ull;  // FNV-1a over the shapes
+    for (int i = 0; i < n; ++i) {
+        const int v[6] = {geoms[i].nx, geoms[i].ny, geoms[i].px, geoms[i].pa, geoms[i].subset_mode, 0};
+        for (int q = 0; q < 6; ++q) {
+            h ^= (unsigned)v[q];
+            h *= 1099511628211ull;
+        }
+    }
+    char kb[96];
+    snprintf(kb, sizeof kb, "batch%d-%016llx", n, h);
+    p->key = xct_tune_key(ctx->name, 0, 0, 0, 0, ss, n) + "|" + kb;
+    TuneChoice c;
+    if (!xct_tune_lookup(p->key, xct_tune_env_path(), c))
+        c = xct_tune_default(ctx->sm_count, [&](int T, int ch) {
+            long long t = 0;
+            for (int i = 0; i < n; ++i) {
+                const int rows = (geoms[i].pa + ss - 1) / ss;
+                t += (long long)((geoms[i].nx + T) / T) * ((geoms[i].ny + T) / T) * ((rows + ch - 1) / ch);
+            }
+            return t;
+        });
+    int rc = batch_layout(p, c.T, c.chunk);
     if (rc) {
         batch_free(p);
         return rc;
@@ -166,7 +215,7 @@ static int capture(xct_batch_plan *p)
     for (int i = 0; i < p->it && rc == XCT_OK; ++i)
         for (int k = 0; k < p->ss && rc == XCT_OK; ++k)
             rc = launch_osem_step_batched(p->d_items, p->d_bases, p->n, p->sub[k],
-                                          p->d_queues + 3 * (size_t)(i * p->ss + k), p->grids, p->cap);
+                                          p->d_queues + 3 * (size_t)(i * p->ss + k), p->grids, p->fwd_T, p->cap);
     e = cudaStreamEndCapture(p->cap, &graph);
     if (rc == XCT_OK && e != cudaSuccess) rc = xct_cuda_fail(e, "cudaStreamEndCapture");
     if (rc == XCT_OK) {
@@ -211,4 +260,78 @@ extern "C" int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, 
     }
     xct_batch_plan_destroy(p);
     return rc;
+}
+
+extern "C" int xct_batch_plan_tuning(xct_batch_plan *p, int *fwd_tile, int *ang_chunk)
+{
+    if (!p || !fwd_tile || !ang_chunk) return xct_fail(XCT_E_INVALID, "xct_batch_plan_tuning: null argument");
+    *fwd_tile = p->fwd_T;
+    *ang_chunk = p->fwd_chunk;
+    return XCT_OK;
+}
+
+// Time the batched forward launch (subset 0) for every candidate (T, chunk) and keep the
+// fastest; the slices read one scratch image of the largest size (the cost depends on the
+// geometry only).  The choice is cached under the batch's shape key.
+extern "C" int xct_batch_plan_autotune(xct_batch_plan *p, const char *cache_path, int flags, void *stream)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "xct_batch_plan_autotune: plan is null");
+    if (!cache_path) cache_path = xct_tune_env_path();
+    TuneChoice best;
+    if (!(flags & XCT_TUNE_FORCE) && xct_tune_lookup(p->key, cache_path, best))
+        return batch_layout(p, best.T, best.chunk);
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t maxpix = 0;
+    int max_rows = 1;
+    for (const XctItemDev &d : p->host) {
+        maxpix = std::max(maxpix, (size_t)d.g.nx * d.g.ny);
+        max_rows = std::max(max_rows, (d.g.pa + d.g.ss - 1) / d.g.ss);
+    }
+    float *scratch = nullptr;
+    XCT_CUDA_TRY(cudaMalloc(&scratch, sizeof(float) * maxpix));
+    std::vector<XctItemDev> tmp = p->host;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int T0 = p->fwd_T, c0 = p->fwd_chunk;
+    best = TuneChoice{T0, c0, 3.0e38f};
+    int rc = cudaMemsetAsync(scratch, 0, sizeof(float) * maxpix, st) == cudaSuccess ? XCT_OK
+                                                                                    : xct_fail(XCT_E_CUDA, "memset");
+    for (const TuneChoice &c : xct_tune_candidates(max_rows)) {
+        if (rc) break;
+        if ((rc = batch_layout(p, c.T, c.chunk))) break;
+        for (int i = 0; i < p->n; ++i) {
+            tmp[i] = p->host[i];
+            tmp[i].img = scratch;
+            tmp[i].sino = nullptr;
+        }
+        cudaMemcpyAsync(p->d_items, tmp.data(), sizeof(XctItemDev) * p->n, cudaMemcpyHostToDevice, st);
+        float tmin = 3.0e38f;
+        for (int r = 0; r < 3 && rc == XCT_OK; ++r) {  // first run warms up
+            cudaMemsetAsync(p->d_acc, 0, sizeof(double) * p->n_acc, st);
+            cudaMemsetAsync(p->d_queues, 0, sizeof(int), st);
+            cudaEventRecord(e0, st);
+            rc = launch_fwd_batched(p->d_items, p->d_bases, p->n, p->sub[0], p->d_queues, p->grids[0], c.T, st);
+            cudaEventRecord(e1, st);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (rc == XCT_OK && e != cudaSuccess) rc = xct_cuda_fail(e, "xct_batch_plan_autotune");
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0) tmin = std::min(tmin, ms);
+        }
+        if (rc == XCT_OK && tmin < best.ms) best = TuneChoice{c.T, c.chunk, tmin};
+    }
+    cudaMemsetAsync(p->d_acc, 0, sizeof(double) * p->n_acc, st);
+    cudaStreamSynchronize(st);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(scratch);
+    if (rc) {
+        batch_layout(p, T0, c0);
+        return rc;
+    }
+    rc = batch_layout(p, best.T, best.chunk);
+    if (rc) return rc;
+    return xct_tune_store(p->key, cache_path, best);
 }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -19,6 +20,8 @@ struct KGeom {
     float hd;        // depth*0.5f
     float cx;        // detector centre (px*0.5f in the reference)
     int fetch;       // XCT_FETCH_*
+    int fwd_T;       // tiled forward projector: tile side (44, 60, 76, 92)
+    int fwd_chunk;   // tiled forward projector: subset angles per CTA (1..128)
 };
 
 // One slice of a batched launch (device-side descriptor).
@@ -60,6 +63,9 @@ struct xct_plan {
     float *d_fi = nullptr;       // [max_batch] focus indices
     float *d_cs = nullptr;       // compressed-sensing OS-EM: w, beta, x' [3][max_batch][ny][nx],
                                  // allocated by the first such run
+    float *d_sino2 = nullptr;    // volume streaming: the second staging set (first volume run)
+    float *d_img2 = nullptr;
+    cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
     int acc_rows = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -111,9 +117,12 @@ int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const
 // prefix sums of the units of each kernel, queues 3 zeroed counters.
 void xct_batched_units(const KGeom &g, int &fwd_ntx, int &fwd_nty, int &fwd_units, int &fin_units, int &bp_ntx,
                        int &bp_units);
-int xct_batched_grids(int device, int sm_count, int grids[3]);
+int xct_batched_grids(int device, int sm_count, int fwd_T, int grids[3]);
 int launch_osem_step_batched(const XctItemDev *items, const int *bases, int n, int sub, int *queues,
-                             const int grids[3], cudaStream_t st);
+                             const int grids[3], int fwd_T, cudaStream_t st);
+bool xct_fwd_tile_valid(int T);
+int launch_fwd_batched(const XctItemDev *items, const int *bases, int n, int sub, int *queue, int grid, int fwd_T,
+                       cudaStream_t st);
 int xct_check_geom(const xct_geom *g);
 // Exact adjoint of the forward projector over all angles: img = A^T sino (overwrites img).
 int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, cudaStream_t st);
@@ -129,6 +138,18 @@ int launch_fbp_bp(const KGeom &g, const float2 *trig, const float *fprj, float *
 // baseUp (reconstShare.cl:87-109) with the slice minima of launch_fbp_bp, in place.
 int launch_base_up(const KGeom &g, float *img, int dN, int order, const int *min_keys, int sm_count,
                    cudaStream_t st);
+// Forward-projector tile autotuning (xct_tune.cu).
+struct TuneChoice {
+    int T, chunk;
+    float ms;
+};
+std::string xct_tune_key(const char *device, int nx, int ny, int px, int pa, int ss, int dN);
+bool xct_tune_lookup(const std::string &key, const char *path, TuneChoice &c);
+int xct_tune_store(const std::string &key, const char *path, const TuneChoice &c);
+TuneChoice xct_tune_default(int sm_count, const std::function<long long(int, int)> &ctas);
+std::vector<TuneChoice> xct_tune_candidates(int max_rows);
+const char *xct_tune_env_path();
+void xct_plan_default_tuning(xct_plan *p);
 // Compressed-sensing proximal steps (xct_cs.cu): ISTA3D, FISTA3D over dN slices.
 int launch_ista3d(const float *v, float *x_new, int nx, int ny, int dN, float lambda, int sm_count, cudaStream_t st);
 int launch_fista3d(float *w, const float *v, float *beta, float *x_new, int nx, int ny, int dN, float lambda,

@@ -140,6 +140,8 @@ extern "C" int xct_osem_run_static(const xct_geom *g, int dN, const float *d_sin
     k.hd = (float)k.depth * 0.5f;
     k.cx = g->center_bin < 0.0f ? (float)g->px * 0.5f : g->center_bin;
     k.fetch = g->measured_fetch_mode;
+    k.fwd_T = 92;  // the default tiles; this path keeps no per-shape state
+    k.fwd_chunk = fwd_tiled_rows_cap();
 
     for (int i = 0; i < it; ++i)
         for (int kk = 0; kk < g->ss; ++kk) {

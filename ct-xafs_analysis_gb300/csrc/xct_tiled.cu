@@ -25,6 +25,8 @@
 //     bin expression ((Xc*c - Yc*s) + cx) + 0.5 with packed f32x2 instructions (each lane
 //     rounds exactly like the scalar expression) and the nearest rule as a round-down add;
 //   * the multiplicative update is fused.
+#include <type_traits>
+
 #include "xct_device.cuh"
 #include "xct_f32x2.cuh"
 
@@ -44,12 +46,17 @@ constexpr int kAngChunk = 128;  // angles per CTA (forward) / per staging pass (
 // distinct 64-bit bank pairs; 8 neighbouring rays also have similar lengths inside a tile,
 // so few lanes idle.  (A CPU model of the access pattern: 0.232 shared wavefronts and 90 %
 // active lanes per sample, against 0.293 and 73 % for one lane per ray with an odd pitch.)
-constexpr int kFwdT = 92;             // owned base texels per tile side
-constexpr int kFwdP = kFwdT;          // element pitch: 92 = 4 (mod 8)
-constexpr int kFwdRows = kFwdT + 1;   // a base row r reads element rows r and r+1
+// Tile side T (owned base texels per side) is a template parameter chosen per plan by the
+// autotuner from {44, 60, 76, 92}; every candidate has an element pitch of T = 4 (mod 8).
+template <int T>
+struct FwdTile {
+    static_assert(T % 8 == 4, "tile pitch must be 4 (mod 8)");
+    static constexpr int P = T;         // element pitch
+    static constexpr int Rows = T + 1;  // a base row r reads element rows r and r+1
+    static constexpr size_t Smem = (size_t)P * Rows * sizeof(float2) + kAngChunk * sizeof(float2);
+};
 constexpr int kLanesPerRay = 4;
 constexpr int kRaysPerWarp = 32 / kLanesPerRay;
-constexpr size_t kFwdSmem = (size_t)kFwdP * kFwdRows * sizeof(float2) + kAngChunk * sizeof(float2);
 
 constexpr int kBpTX = 64, kBpTY = 32;  // backprojection tile (pixels)
 constexpr int kBpW = 76;               // staged bins per angle (>= 63|c| + 31|s| + 3)
@@ -115,9 +122,10 @@ __device__ __forceinline__ void lds_f2(unsigned addr, float &a, float &b)
 {
     asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(a), "=f"(b) : "r"(addr));
 }
+template <int P>
 __device__ __forceinline__ void lds_f2_next_row(unsigned addr, float &a, float &b)
 {
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(a), "=f"(b) : "r"(addr), "n"(kFwdP * 8));
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(a), "=f"(b) : "r"(addr), "n"(P * 8));
 }
 __device__ __forceinline__ float lds_f1(unsigned addr)
 {
@@ -130,6 +138,7 @@ __device__ __forceinline__ float lds_f1(unsigned addr)
 // One bilinear sample at Yc (both halves of yc2): coordinates (fma(Yc,s,ax), fma(Yc,c,ay)),
 // floor as a round-down add of 1.5*2^23 (the low mantissa bits), fraction = coordinate -
 // floor, the footprint as two 64-bit loads of (t, t[x+1] - t), three FMA lerps.
+template <int P>
 __device__ __forceinline__ float fwd_sample(f2x yc2, f2x sc, f2x axy, f2x MM, unsigned base2)
 {
     const f2x xy = f2_fma(yc2, sc, axy);
@@ -139,24 +148,27 @@ __device__ __forceinline__ float fwd_sample(f2x yc2, f2x sc, f2x axy, f2x MM, un
     f2_unpack_bits(tb, ixb, iyb);
     float fx, fy;
     f2_unpack(fr, fx, fy);
-    const unsigned addr = (unsigned)iyb * (unsigned)(kFwdP * 8) + (unsigned)ixb * 8u + base2;
+    const unsigned addr = (unsigned)iyb * (unsigned)(P * 8) + (unsigned)ixb * 8u + base2;
     float t00, d0, t01, d1;
     lds_f2(addr, t00, d0);
-    lds_f2_next_row(addr, t01, d1);
+    lds_f2_next_row<P>(addr, t01, d1);
     const float r0 = fmaf(fx, d0, t00);
     const float r1 = fmaf(fx, d1, t01);
     return fmaf(fy, r1 - r0, r0);
 }
 
 // The work of one CTA: tile (bx, by) of one slice (image im, accumulator acc [nrows][px])
-// for the subset angles k0 .. k0+kAngChunk-1.  Starts and ends with all threads in step.
+// for the subset angles k0 .. k0+chunk-1 (chunk <= kAngChunk).  Starts and ends with all
+// threads in step.
+template <int T>
 __device__ __forceinline__ void fwd_tile(const KGeom &g, const float *__restrict__ im, double *__restrict__ acc,
                                          const float2 *__restrict__ trig, int sub, int step, int nrows, int bx,
-                                         int by, int k0, unsigned char *smem_raw)
+                                         int by, int k0, int chunk, unsigned char *smem_raw)
 {
+    constexpr int kFwdT = T, kFwdP = FwdTile<T>::P, kFwdRows = FwdTile<T>::Rows;
     float2 *tile = reinterpret_cast<float2 *>(smem_raw);
     float2 *scs = reinterpret_cast<float2 *>(smem_raw + (size_t)kFwdP * kFwdRows * sizeof(float2));
-    const int kn = min(kAngChunk, nrows - k0);
+    const int kn = min(chunk, nrows - k0);
     if (kn <= 0) return;
     const int x0 = -1 + bx * kFwdT, y0 = -1 + by * kFwdT;
 
@@ -243,11 +255,11 @@ __device__ __forceinline__ void fwd_tile(const KGeom &g, const float *__restrict
             int i = 0;
             for (; i + 1 < n; i += 2) {
                 const f2x yb2 = f2_add(yc2, step2);
-                sum += fwd_sample(yc2, sc, axy, MM, base2);
-                sum_b += fwd_sample(yb2, sc, axy, MM, base2);
+                sum += fwd_sample<kFwdP>(yc2, sc, axy, MM, base2);
+                sum_b += fwd_sample<kFwdP>(yb2, sc, axy, MM, base2);
                 yc2 = f2_add(yb2, step2);
             }
-            if (i < n) sum += fwd_sample(yc2, sc, axy, MM, base2);
+            if (i < n) sum += fwd_sample<kFwdP>(yc2, sc, axy, MM, base2);
             sum += sum_b;
             // the ray's partial sum over this tile: the 4 phases, then one atomic
             sum += __shfl_xor_sync(0xffffffffu, sum, 1);
@@ -258,6 +270,7 @@ __device__ __forceinline__ void fwd_tile(const KGeom &g, const float *__restrict
 }
 
 // grid: (ntx*nty tiles, angle chunks, dN).  acc: [dN][nrows][px] doubles.
+template <int T>
 __global__ void __launch_bounds__(kFwdThreads, 3) fwd_tiled_kernel(const float *__restrict__ img,
                                                                    double *__restrict__ acc,
                                                                    const float2 *__restrict__ trig, KGeom g, int sub,
@@ -265,8 +278,8 @@ __global__ void __launch_bounds__(kFwdThreads, 3) fwd_tiled_kernel(const float *
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int z = blockIdx.z;
-    fwd_tile(g, img + (size_t)z * g.nx * g.ny, acc + (size_t)z * nrows * g.px, trig, sub, step, nrows,
-             (int)blockIdx.x % ntx, (int)blockIdx.x / ntx, (int)blockIdx.y * kAngChunk, smem_raw);
+    fwd_tile<T>(g, img + (size_t)z * g.nx * g.ny, acc + (size_t)z * nrows * g.px, trig, sub, step, nrows,
+                (int)blockIdx.x % ntx, (int)blockIdx.x / ntx, (int)blockIdx.y * g.fwd_chunk, g.fwd_chunk, smem_raw);
 }
 
 // ------------------------------------------------------------------- exact adjoint
@@ -513,6 +526,7 @@ __device__ __forceinline__ int unit_item(const int *__restrict__ base, int n, in
     return i;
 }
 
+template <int T>
 __global__ void __launch_bounds__(kFwdThreads, 3) fwd_batched_kernel(const XctItemDev *__restrict__ items,
                                                                      const int *__restrict__ base, int n, int sub,
                                                                      int *queue)
@@ -530,8 +544,8 @@ __global__ void __launch_bounds__(kFwdThreads, 3) fwd_batched_kernel(const XctIt
         const int local = u - base[i];
         const int tiles = it.fwd_ntx * it.fwd_nty;
         const int t = local % tiles, ch = local / tiles;
-        fwd_tile(g, it.img, it.acc, it.trig, sub, g.ss, nrows, t % it.fwd_ntx, t / it.fwd_ntx, ch * kAngChunk,
-                 smem_raw);
+        fwd_tile<T>(g, it.img, it.acc, it.trig, sub, g.ss, nrows, t % it.fwd_ntx, t / it.fwd_ntx, ch * g.fwd_chunk,
+                    g.fwd_chunk, smem_raw);
         __syncthreads();  // the tile in shared memory is restaged by the next unit
     }
 }
@@ -583,28 +597,60 @@ __global__ void __launch_bounds__(kThreads) bp_batched_kernel(const XctItemDev *
 
 }  // namespace
 
+// ---------------------------------------------------------------- tile-size dispatch
+bool xct_fwd_tile_valid(int T) { return T == 44 || T == 60 || T == 76 || T == 92; }
+
+template <int T>
+static int fwd_smem_attr(const void *fn, bool *done)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !done[dev]) {
+        XCT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FwdTile<T>::Smem));
+        done[dev] = true;
+    }
+    return XCT_OK;
+}
+
+// Calls f(std::integral_constant<int, T>) for the plan's tile side T.
+template <class F>
+static int with_tile(int T, F &&f)
+{
+    switch (T) {
+    case 44: return f(std::integral_constant<int, 44>{});
+    case 60: return f(std::integral_constant<int, 60>{});
+    case 76: return f(std::integral_constant<int, 76>{});
+    case 92: return f(std::integral_constant<int, 92>{});
+    default: return xct_fail(XCT_E_INVALID, "forward tile side must be 44, 60, 76 or 92");
+    }
+}
+
 void xct_batched_units(const KGeom &g, int &fwd_ntx, int &fwd_nty, int &fwd_units, int &fin_units, int &bp_ntx,
                        int &bp_units)
 {
-    fwd_ntx = (g.nx + 1 + kFwdT - 1) / kFwdT;
-    fwd_nty = (g.ny + 1 + kFwdT - 1) / kFwdT;
+    fwd_ntx = (g.nx + 1 + g.fwd_T - 1) / g.fwd_T;
+    fwd_nty = (g.ny + 1 + g.fwd_T - 1) / g.fwd_T;
     const int rows = (g.pa + g.ss - 1) / g.ss;  // the largest subset (cover mode)
-    fwd_units = fwd_ntx * fwd_nty * ((rows + kAngChunk - 1) / kAngChunk);
+    fwd_units = fwd_ntx * fwd_nty * ((rows + g.fwd_chunk - 1) / g.fwd_chunk);
     fin_units = rows;
     bp_ntx = (g.nx + kBpTX - 1) / kBpTX;
     bp_units = bp_ntx * ((g.ny + kBpTY - 1) / kBpTY);
 }
 
-int xct_batched_grids(int device, int sm_count, int grids[3])
+int xct_batched_grids(int device, int sm_count, int fwd_T, int grids[3])
 {
-    static bool attr_set[64] = {};
-    if (device >= 0 && device < 64 && !attr_set[device]) {
-        XCT_CUDA_TRY(cudaFuncSetAttribute(fwd_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)kFwdSmem));
-        attr_set[device] = true;
-    }
+    (void)device;
     int a = 0, b = 0, c = 0;
-    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fwd_batched_kernel, kFwdThreads, kFwdSmem));
+    int rc = with_tile(fwd_T, [&](auto tc) -> int {
+        constexpr int T = decltype(tc)::value;
+        static bool done[64] = {};
+        int r = fwd_smem_attr<T>((const void *)fwd_batched_kernel<T>, done);
+        if (r) return r;
+        XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fwd_batched_kernel<T>, kFwdThreads,
+                                                                   FwdTile<T>::Smem));
+        return XCT_OK;
+    });
+    if (rc) return rc;
     XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fwd_finalize_batched_kernel, 256, 0));
     XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, bp_batched_kernel, kThreads, 0));
     grids[0] = sm_count * (a > 0 ? a : 1);
@@ -614,10 +660,15 @@ int xct_batched_grids(int device, int sm_count, int grids[3])
 }
 
 int launch_osem_step_batched(const XctItemDev *items, const int *bases /*[3][n+1]*/, int n, int sub,
-                             int *queues /*[3]*/, const int grids[3], cudaStream_t st)
+                             int *queues /*[3]*/, const int grids[3], int fwd_T, cudaStream_t st)
 {
-    fwd_batched_kernel<<<grids[0], kFwdThreads, kFwdSmem, st>>>(items, bases, n, sub, queues);
-    XCT_CUDA_TRY(cudaGetLastError());
+    int rc = with_tile(fwd_T, [&](auto tc) -> int {
+        constexpr int T = decltype(tc)::value;
+        fwd_batched_kernel<T><<<grids[0], kFwdThreads, FwdTile<T>::Smem, st>>>(items, bases, n, sub, queues);
+        XCT_CUDA_TRY(cudaGetLastError());
+        return XCT_OK;
+    });
+    if (rc) return rc;
     fwd_finalize_batched_kernel<<<grids[1], 256, 0, st>>>(items, bases + (n + 1), n, sub, queues + 1);
     XCT_CUDA_TRY(cudaGetLastError());
     bp_batched_kernel<<<grids[2], kThreads, 0, st>>>(items, bases + 2 * (n + 1), n, sub, queues + 2);
@@ -625,37 +676,39 @@ int launch_osem_step_batched(const XctItemDev *items, const int *bases /*[3][n+1
     return XCT_OK;  // launches are counted when the captured graph is replayed
 }
 
-int fwd_tiled_rows_cap() { return kAngChunk; }
-
-static int fwd_grid(const KGeom &g, int nrows, int dN, dim3 &grid, int &ntx)
+// The forward launch of one batched subset step alone (the autotuner times it).
+int launch_fwd_batched(const XctItemDev *items, const int *bases, int n, int sub, int *queue, int grid, int fwd_T,
+                       cudaStream_t st)
 {
-    ntx = (g.nx + 1 + kFwdT - 1) / kFwdT;  // base texels -1 .. nx-1
-    const int nty = (g.ny + 1 + kFwdT - 1) / kFwdT;
-    const int nch = (nrows + kAngChunk - 1) / kAngChunk;
-    grid = dim3(ntx * nty, nch, dN);
-    static bool attr_set[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        XCT_CUDA_TRY(cudaFuncSetAttribute(fwd_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)kFwdSmem));
-        attr_set[dev] = true;
-    }
-    return XCT_OK;
+    return with_tile(fwd_T, [&](auto tc) -> int {
+        constexpr int T = decltype(tc)::value;
+        fwd_batched_kernel<T><<<grid, kFwdThreads, FwdTile<T>::Smem, st>>>(items, bases, n, sub, queue);
+        XCT_CUDA_TRY(cudaGetLastError());
+        return XCT_OK;
+    });
 }
+
+int fwd_tiled_rows_cap() { return kAngChunk; }
 
 int launch_fwd_tiled_main(const KGeom &g, const float2 *trig, const float *img, double *acc, int dN, int sub, int step,
                           int nrows, cudaStream_t st)
 {
     if (nrows <= 0 || dN <= 0) return XCT_OK;
-    dim3 grid;
-    int ntx;
-    int rc = fwd_grid(g, nrows, dN, grid, ntx);
-    if (rc) return rc;
-    fwd_tiled_kernel<<<grid, kFwdThreads, kFwdSmem, st>>>(img, acc, trig, g, sub, step, nrows, ntx);
-    g_xct_launches.fetch_add(1, std::memory_order_relaxed);
-    XCT_CUDA_TRY(cudaGetLastError());
-    return XCT_OK;
+    if (g.fwd_chunk <= 0 || g.fwd_chunk > kAngChunk) return xct_fail(XCT_E_INVALID, "forward angle chunk out of range");
+    return with_tile(g.fwd_T, [&](auto tc) -> int {
+        constexpr int T = decltype(tc)::value;
+        static bool done[64] = {};
+        int r = fwd_smem_attr<T>((const void *)fwd_tiled_kernel<T>, done);
+        if (r) return r;
+        const int ntx = (g.nx + 1 + T - 1) / T;  // base texels -1 .. nx-1
+        const int nty = (g.ny + 1 + T - 1) / T;
+        const int nch = (nrows + g.fwd_chunk - 1) / g.fwd_chunk;
+        dim3 grid(ntx * nty, nch, dN);
+        fwd_tiled_kernel<T><<<grid, kFwdThreads, FwdTile<T>::Smem, st>>>(img, acc, trig, g, sub, step, nrows, ntx);
+        g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+        XCT_CUDA_TRY(cudaGetLastError());
+        return XCT_OK;
+    });
 }
 
 int launch_fwd_finalize(const KGeom &g, const float *meas, float *out, double *acc, int dN, int sub, int step,

@@ -50,8 +50,11 @@ EXPORTS = (
     "xct_fbp_filter", "xct_fbp_backproject", "xct_fbp_run_device", "xct_hybrid_run_device", "xct_fbp_run",
     "xct_hybrid_run", "xct_rot_center_shift", "xct_focus_index", "xct_rot_center_search",
     "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_denoise_sinogram",
-    "xct_cs_osem_run_device", "xct_cs_osem_run",
+    "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
+    "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume",
 )
+
+TUNE_FORCE = 1
 
 
 class XCTError(RuntimeError):
@@ -128,6 +131,13 @@ def load():
     L.xct_cs_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
     L.xct_cs_osem_run.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int), ip,
                                   c_f]
+    L.xct_osem_run_volume.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int),
+                                      ip]
+    L.xct_plan_autotune.argtypes = [vp, ip, ctypes.c_char_p, ip, vp]
+    L.xct_plan_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.xct_plan_set_tuning.argtypes = [vp, ip, ip]
+    L.xct_batch_plan_autotune.argtypes = [vp, ctypes.c_char_p, ip, vp]
+    L.xct_batch_plan_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
     L.xct_launch_count.restype = ctypes.c_longlong
@@ -272,6 +282,26 @@ class OSEMPlan:
         dN = len(sinos)
         return (fp * dN)(*[s.ctypes.data_as(fp) for s in sinos]), (fp * dN)(*[i.ctypes.data_as(fp) for i in imgs])
 
+    def run_volume(self, sinos, imgs, sub=None, it=-1):
+        """OS-EM of a whole volume from host memory in streamed batches of max_batch slices.
+        sinos/imgs: sequences of host slices -- float32 numpy arrays, or CPU torch tensors
+        (page-locked ones give overlapped copies)."""
+        fp = ctypes.POINTER(ctypes.c_float)
+
+        def addr(a):
+            if hasattr(a, "data_ptr"):
+                if a.is_cuda or not a.is_contiguous() or str(a.dtype) != "torch.float32":
+                    raise XCTError(XCT_E_INVALID, "host slices must be contiguous float32 CPU tensors")
+                return ctypes.cast(a.data_ptr(), fp)
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                raise XCTError(XCT_E_INVALID, "host arrays must be C-contiguous float32 numpy arrays")
+            return a.ctypes.data_as(fp)
+        n = len(sinos)
+        s_arr = (fp * n)(*[addr(a) for a in sinos])
+        i_arr = (fp * n)(*[addr(a) for a in imgs])
+        _check(self._lib.xct_osem_run_volume(self.handle, n, s_arr, i_arr, self._sub(sub), it))
+        return imgs
+
     def cs_run(self, sinos, imgs, cs_lambda=1.0e-4, sub=None, it=-1):
         """Compressed-sensing OS-EM (FISTA_OSEM_execution) on host arrays; the dN slices of
         the call are the third axis of the proximal step."""
@@ -381,6 +411,23 @@ class OSEMPlan:
                                                _stream(stream)))
         return fi, best.value
 
+    # ---- forward-projector tiles --------------------------------------------------------
+    def autotune(self, dN=None, cache_path=None, force=False, stream=None):
+        """Time every (tile side, angles per CTA) candidate for dN slices and keep the fastest
+        (cached per shape in memory and in cache_path / $XCT_TUNE_CACHE)."""
+        dN = self.max_batch if dN is None else dN
+        cp = None if cache_path is None else str(cache_path).encode()
+        _check(self._lib.xct_plan_autotune(self.handle, dN, cp, TUNE_FORCE if force else 0, _stream(stream)))
+        return self.tuning()
+
+    def tuning(self):
+        t, c = ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.xct_plan_tuning(self.handle, ctypes.byref(t), ctypes.byref(c)))
+        return t.value, c.value
+
+    def set_tuning(self, fwd_tile, ang_chunk):
+        _check(self._lib.xct_plan_set_tuning(self.handle, fwd_tile, ang_chunk))
+
     def profile(self, d_sino, d_img, dN=None, sub=None, it=-1, stream=None):
         """Run OS-EM with CUDA events around every launch; returns a dict of summed device
         milliseconds and launch counts per kernel kind (fwd, finalize, bp) and the total."""
@@ -419,6 +466,16 @@ class BatchPlan:
         h = ctypes.c_void_p()
         _check(self._lib.xct_batch_plan_create(ctx.handle, len(self.geoms), arr, it, ctypes.byref(h)))
         self.handle = h
+
+    def autotune(self, cache_path=None, force=False, stream=None):
+        cp = None if cache_path is None else str(cache_path).encode()
+        _check(self._lib.xct_batch_plan_autotune(self.handle, cp, TUNE_FORCE if force else 0, _stream(stream)))
+        return self.tuning()
+
+    def tuning(self):
+        t, c = ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.xct_batch_plan_tuning(self.handle, ctypes.byref(t), ctypes.byref(c)))
+        return t.value, c.value
 
     def run(self, sinos, imgs, stream=None):
         n = len(self.geoms)

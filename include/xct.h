@@ -91,6 +91,18 @@ int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *c
 int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                         void *stream);
 
+/* ---- a whole volume from host memory -------------------------------------------------
+ * OS-EM of n slices (sino_host[i] [pa][px] in, img_host[i] [ny][nx] initial image in and
+ * reconstruction out) in device batches of max_batch slices: while one batch computes, the
+ * next batch's inputs are uploaded and the previous batch's images downloaded on their own
+ * streams (two device staging sets, the second allocated on the first call), so the volume
+ * needs no more HBM than two batches.  Page-locked host buffers (cudaHostAlloc /
+ * cudaHostRegister) give full overlap; pageable ones are correct but copy synchronously.
+ * Blocking; xct_plan_last_ms reports the whole run.  Replaces OSEM_ocl's dispatch of
+ * OSEM_input_thread / OSEM_thread over the slices (GPU.cpp:629-658) for one device. */
+int xct_osem_run_volume(xct_plan *plan, int n, const float *const *sino_host, float *const *img_host, const int *sub,
+                        int it);
+
 /* ---- batches of slices of different shapes (CT-XAFS stacks) -------------------------
  * The reference reconstructs dN slices of ONE shape per OSEM_execution call
  * (GPU.cpp:125-240, image2d_array layers).  A batch plan takes n slices of any shapes
@@ -260,6 +272,26 @@ int xct_denoise_sinogram(int width, int n_angles, int n_rows, float threshold, c
  * Synchronous. */
 int xct_osem_profile(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                      void *stream, float *ms, long long *launches);
+
+/* ---- forward-projector tiles: autotuner -------------------------------------------------
+ * No counterpart in the reference (it launches one work-item per ray).  The tiled forward
+ * projector has two launch-shape parameters: the tile side (44, 60, 76 or 92 texels) and the
+ * subset angles one CTA serves (1..128).  A plan starts with the choice cached for its shape
+ * (device name, nx, ny, px, pa, ss, max_batch) -- in this process, or in the JSON file named by
+ * the environment variable XCT_TUNE_CACHE -- or else the largest tiles that still give two
+ * waves of CTAs.  xct_plan_autotune times every candidate for dN slices on the plan's own
+ * geometry (its staging buffers are the input; no caller data is read or written), keeps the
+ * fastest, and records it in memory and in cache_path (NULL: XCT_TUNE_CACHE; no file if
+ * neither).  A cached entry is reused without timing unless flags has XCT_TUNE_FORCE.
+ * Synchronous.  xct_batch_plan_autotune does the same for a batch plan (one choice for all
+ * its slices; the next xct_batch_run captures its graph again).  The *_tuning calls report
+ * the current choice; xct_plan_set_tuning sets one by hand. */
+#define XCT_TUNE_FORCE 1
+int xct_plan_autotune(xct_plan *plan, int dN, const char *cache_path, int flags, void *stream);
+int xct_plan_tuning(xct_plan *plan, int *fwd_tile, int *ang_chunk);
+int xct_plan_set_tuning(xct_plan *plan, int fwd_tile, int ang_chunk);
+int xct_batch_plan_autotune(xct_batch_plan *plan, const char *cache_path, int flags, void *stream);
+int xct_batch_plan_tuning(xct_batch_plan *plan, int *fwd_tile, int *ang_chunk);
 
 /* FP32 FMA throughput of a device (TFLOP/s), measured by a dependent-chain-free FMA
  * kernel: the roofline denominator for the projectors. */
