@@ -19,6 +19,12 @@ Metric: slice-iterations per second (one slice through all 15 subsets once).
                     inside the timed region);
   per_slice      -- the plain one-slice-per-call path (plain kernels, dN = 1) and the tiled
                     kernels at dN = 1, each on a bounded sample of slices;
+  ctxafs_batched -- the CT-XAFS stack sample (uneven slices) in one autotuned batched graph
+                    against one call per slice;
+  volume_stream  -- a sample of the full-volume workload (2048^2, 1800 angles, 20 subsets x 3
+                    it, rotation centre +3.5 bins, I0 = 2e4) streamed from page-locked host
+                    memory by xct_osem_run_volume, against blocking per-batch calls and the
+                    plain per-slice path;
   roofline       -- the dominant kernel (tiled forward projector) timed live with CUDA
                     events inside this run; its algorithmic FLOPs (12 per bilinear sample
                     whose footprint meets the image) over its measured time, against the
@@ -289,6 +295,9 @@ def ctxafs_batched(ctx, n_items=32, ss=10, it=5):
         return a.elapsed_time(b) / reps
 
     bp = xct.BatchPlan(ctx, geoms, it)
+    t_tune = time.perf_counter()
+    res["tuning"] = dict(zip(("fwd_tile", "ang_chunk"), bp.autotune()))
+    res["autotune_s"] = time.perf_counter() - t_tune
     imgs = [torch.ones((w, w), device="cuda") for w, _ in shapes]
 
     def run_batched():
@@ -300,6 +309,9 @@ def ctxafs_batched(ctx, n_items=32, ss=10, it=5):
     res["batched"] = {"value": n_items * it / (ms * 1e-3), "ms": ms}
     for name, kern in (("per_slice_tiled", xct.KERNELS_TILED), ("per_slice_plain", xct.KERNELS_PLAIN)):
         plans = [xct.OSEMPlan(ctx, w, w, w, g._angles, ss, it, kernels=kern) for (w, _), g in zip(shapes, geoms)]
+        if kern == xct.KERNELS_TILED:
+            for p in plans:
+                p.autotune(dN=1)
         ximgs = [torch.ones((1, w, w), device="cuda") for w, _ in shapes]
 
         def run_single():
@@ -314,6 +326,72 @@ def ctxafs_batched(ctx, n_items=32, ss=10, it=5):
     bp.close()
     res["batched_over_plain"] = res["batched"]["value"] / res["per_slice_plain"]["value"]
     res["batched_over_tiled_per_slice"] = res["batched"]["value"] / res["per_slice_tiled"]["value"]
+    return res
+
+
+def volume_stream(ctx, nslices=40, dn=10):
+    """Sample of the full-volume workload: nslices of 2048^2 (a slab of the 2048-slice
+    ellipsoid volume), 1800 angles, 2048 bins, centre 1024 + 3.5 (the sinograms are
+    projected about it and the plan reconstructs about it), I0 = 2e4, 20 subsets x 3 it.
+    Host-resident page-locked sinograms and images; xct_osem_run_volume streams them in
+    batches of dn with overlapped copies.  Wall-clock slice-iters/s, the same with one
+    blocking xct_osem_run per batch, and the plain per-slice path on 1 slice."""
+    import torch
+    import xct
+    from xct import phantom
+    pa, ss, it, cx, i0 = 1800, 20, 3, 1024.0 + 3.5, 2e4
+    ang = phantom.uniform_angles(pa)
+    pars = phantom.ellipsoid_params(NX, 2048, 30, 5, mu=(0.005, 0.1))
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(5)
+    plan = xct.OSEMPlan(ctx, NX, NY, PX, ang, ss, it, center_bin=cx, max_batch=dn)
+    z0 = 1024 - nslices // 2  # a slab through the middle of the volume
+    h_sino, h_img = [], []
+    clean = torch.empty((1, pa, PX), device="cuda")
+    for z in range(nslices):
+        img = phantom.ellipsoid_slice(pars, z0 + z, NX, NY, torch_device="cuda").reshape(1, NY, NX).contiguous()
+        plan.fwd(img, clean)
+        h_sino.append(phantom.noisy_log_sinogram_torch(clean[0], i0, generator=gen).cpu().pin_memory())
+        h_img.append(torch.ones((NY, NX)).pin_memory())
+    torch.cuda.synchronize()
+    t_tune = time.perf_counter()
+    tuning = plan.autotune(dN=dn)
+    tune_s = time.perf_counter() - t_tune
+    res = {"slices": nslices, "of_volume_slices": 2048, "angles": pa, "subsets": ss, "iterations": it,
+           "center_bin": cx, "batch": dn, "tuning": dict(zip(("fwd_tile", "ang_chunk"), tuning)),
+           "autotune_s": tune_s,
+           "h2d_bytes": nslices * (pa * PX + NX * NY) * 4, "d2h_bytes": nslices * NX * NY * 4}
+    plan.run_volume(h_sino[:dn], h_img[:dn])  # warm
+    for x in h_img:
+        x.fill_(1.0)
+    t0 = time.perf_counter()
+    plan.run_volume(h_sino, h_img)
+    dt = time.perf_counter() - t0
+    res["streamed"] = {"value": nslices * it / dt, "s": dt}
+    vol0 = h_img[0].clone()
+    np_s = [t.numpy() for t in h_sino]
+    np_i = [t.numpy() for t in h_img]
+    for x in np_i:
+        x.fill(1.0)
+    t0 = time.perf_counter()
+    for b in range(0, nslices, dn):
+        plan.run(np_s[b:b + dn], np_i[b:b + dn])
+    dt = time.perf_counter() - t0
+    res["per_batch_blocking"] = {"value": nslices * it / dt, "s": dt}
+    plan.close()
+    # plain per-slice path (the reference's launch shape), one slice
+    p1 = xct.OSEMPlan(ctx, NX, NY, PX, ang, ss, it, center_bin=cx, max_batch=1, kernels=xct.KERNELS_PLAIN)
+    x1 = [np.ones((NY, NX), np.float32)]
+    p1.run([np_s[0]], x1, it=1)  # warm
+    x1[0].fill(1.0)
+    t0 = time.perf_counter()
+    p1.run([np_s[0]], x1)
+    dt = time.perf_counter() - t0
+    p1.close()
+    res["per_slice_plain"] = {"value": it / dt, "s": dt}
+    v = vol0.numpy().astype(np.float64)
+    res["rel_l2_streamed_vs_plain"] = float(np.linalg.norm(v - x1[0]) / np.linalg.norm(x1[0]))
+    res["streamed_over_plain"] = res["streamed"]["value"] / res["per_slice_plain"]["value"]
     return res
 
 
@@ -376,6 +454,7 @@ def main():
     ang = phantom.uniform_angles(PA)
     ctx = xct.Context(local)
     plan = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, IT, max_batch=DN, kernels=xct.KERNELS_TILED)
+    tuning = plan.autotune(dN=DN)  # before the timed region; cached per shape
     stream = torch.cuda.current_stream(dev)
     nb = NSLICES // DN
 
@@ -440,6 +519,8 @@ def main():
     per_slice = {}
     for name, kern, nsl in (("plain", xct.KERNELS_PLAIN, 2), ("tiled", xct.KERNELS_TILED, 4)):
         p1 = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, IT, max_batch=1, kernels=kern)
+        if kern == xct.KERNELS_TILED:
+            p1.autotune(dN=1)
         x = imgs[:1].clone()
         p1.run_device(sino[:1], x, dN=1, it=1, stream=stream)
         torch.cuda.synchronize()
@@ -459,6 +540,12 @@ def main():
         batched = ctxafs_batched(ctx)
     except Exception as e:  # reported, never fatal
         batched = {"error": str(e)[:300]}
+
+    # ---- full-volume workload sample, streamed from host memory ----
+    try:
+        volume = volume_stream(ctx)
+    except Exception as e:  # reported, never fatal
+        volume = {"error": str(e)[:300]}
 
     # ---- roofline of the dominant kernel (live CUDA events, same stream) ----
     prof = plan.profile(sino[:DN], imgs[:DN].fill_(1.0), dN=DN, stream=stream)
@@ -514,10 +601,11 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantom, Poisson I0=5e4)",
             "config": {"workload": WORKLOAD, "batch_slices_per_call": DN, "kernels": "tiled",
+                       "fwd_tiles": dict(zip(("fwd_tile", "ang_chunk"), tuning)),
                        "l2": "inputs larger than L2 (each step a new 290 MB batch)",
                        "parallelism": "dp%d over slices" % world},
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "per_slice": per_slice,
-            "ctxafs_batched": batched,
+            "ctxafs_batched": batched, "volume_stream": volume,
             "roofline": roofline, "cpu_baseline": cpu, "finite": finite,
             "launches_per_step": launches / max(args.steps, 1),
         }
