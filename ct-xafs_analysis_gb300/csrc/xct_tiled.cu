@@ -54,6 +54,9 @@ struct FwdTile {
     static constexpr int P = T;         // element pitch
     static constexpr int Rows = T + 1;  // a base row r reads element rows r and r+1
     static constexpr size_t Smem = (size_t)P * Rows * sizeof(float2) + kAngChunk * sizeof(float2);
+    // CTAs per SM: 4 (48 warps, <= 40 registers, no spills) where four tiles fit in the
+    // 227 KB of shared memory (T <= 76), else 3 (56 registers)
+    static constexpr int MinBlocks = Smem * 4 <= 227u * 1024u ? 4 : 3;
 };
 constexpr int kLanesPerRay = 4;
 constexpr int kRaysPerWarp = 32 / kLanesPerRay;
@@ -271,7 +274,7 @@ __device__ __forceinline__ void fwd_tile(const KGeom &g, const float *__restrict
 
 // grid: (ntx*nty tiles, angle chunks, dN).  acc: [dN][nrows][px] doubles.
 template <int T>
-__global__ void __launch_bounds__(kFwdThreads, 3) fwd_tiled_kernel(const float *__restrict__ img,
+__global__ void __launch_bounds__(kFwdThreads, FwdTile<T>::MinBlocks) fwd_tiled_kernel(const float *__restrict__ img,
                                                                    double *__restrict__ acc,
                                                                    const float2 *__restrict__ trig, KGeom g, int sub,
                                                                    int step, int nrows, int ntx)
@@ -527,7 +530,7 @@ __device__ __forceinline__ int unit_item(const int *__restrict__ base, int n, in
 }
 
 template <int T>
-__global__ void __launch_bounds__(kFwdThreads, 3) fwd_batched_kernel(const XctItemDev *__restrict__ items,
+__global__ void __launch_bounds__(kFwdThreads, FwdTile<T>::MinBlocks) fwd_batched_kernel(const XctItemDev *__restrict__ items,
                                                                      const int *__restrict__ base, int n, int sub,
                                                                      int *queue)
 {
