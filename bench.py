@@ -21,6 +21,9 @@ Metric: slice-iterations per second (one slice through all 15 subsets once).
                     kernels at dN = 1, each on a bounded sample of slices;
   ctxafs_batched -- the CT-XAFS stack sample (uneven slices) in one autotuned batched graph
                     against one call per slice;
+  next_components-- throughput of FBP, the hybrid, the compressed-sensing OS-EM, reslice,
+                    denoise and the rotation-centre search (HBM-bound ones against the
+                    measured HBM peak);
   volume_stream  -- a sample of the full-volume workload (2048^2, 1800 angles, 20 subsets x 3
                     it, rotation centre +3.5 bins, I0 = 2e4) streamed from page-locked host
                     memory by xct_osem_run_volume, against blocking per-batch calls and the
@@ -395,6 +398,93 @@ def volume_stream(ctx, nslices=40, dn=10):
     return res
 
 
+def next_components(ctx, hbm_gbs):
+    """Throughput of the components either side of the OS-EM path, on the device-resident
+    per-slice workload shape (2048^2, 1500 angles, 2048 bins) unless stated, CUDA-event
+    timing, 3 warm-ups then 5 timed calls each:
+      fbp            -- ramp filter (zp 4096) + FBP backprojection of 10 slices (FBP.cl);
+      hybrid         -- FBP + base-up + 1 OS-EM iteration (15 subsets) of 10 slices;
+      cs_osem        -- compressed-sensing OS-EM (ISTA3D/FISTA3D) 1 iteration, 10 slices;
+      reslice        -- 1500 projections of 2048 x 64 rows -> 64 sinograms, with drift shifts;
+      rot_center     -- rotation-centre search: 16 shifts of one slice (1 OS-EM it each).
+    HBM-bound kernels report GB/s of compulsory traffic against the measured HBM peak."""
+    import torch
+    import xct
+    from xct import phantom
+    st = torch.cuda.current_stream()
+    out = {}
+    ang = phantom.uniform_angles(PA)
+    dn = 10
+
+    def timed(fn, reps=5):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(reps):
+            fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    plan = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, 1, max_batch=dn)
+    pars = phantom.ellipsoid_params(NX, 100, 30, 2, mu=(0.005, 0.1))
+    sino = torch.empty((dn, PA, PX), device="cuda")
+    for z in range(dn):
+        img = phantom.ellipsoid_slice(pars, 45 + z, NX, NY, torch_device="cuda").reshape(1, NY, NX).contiguous()
+        plan.fwd(img, sino[z:z + 1])
+    x = torch.empty((dn, NY, NX), device="cuda")
+    fp = torch.empty_like(sino)
+    ms_f = timed(lambda: plan.fbp_filter(sino, fp, zp=4096))
+    ms_b = timed(lambda: plan.fbp_backproject(fp, x))
+    ms = timed(lambda: plan.fbp(sino, x, zp=4096))
+    t_fwd, t_bp = algorithmic_counts(ang, NX, NY, PX)
+    # FBP backprojection: every (pixel, angle) inside the circle: the bin coordinate (5), its
+    # floor and fraction (2), the two-bin lerp (4) and the accumulation (1) -- 12 flop
+    bp_flop = 12.0 * math.pi * (NX / 2) ** 2 * PA * dn
+    out["fbp"] = {"slices_per_s": dn / (ms * 1e-3), "ms_per_10": ms, "filter_ms": ms_f, "backproject_ms": ms_b,
+                  "filter_hbm_gbs": 2 * dn * PA * PX * 4 / (ms_f * 1e-3) / 1e9, "hbm_peak_gbs": hbm_gbs,
+                  "backproject_tflops": bp_flop / (ms_b * 1e-3) / 1e12}
+    ms = timed(lambda: (x.fill_(0.0), plan.hybrid(sino, x, zp=4096, it=1)), reps=3)
+    out["hybrid"] = {"slices_per_s": dn / (ms * 1e-3), "ms_per_10": ms, "osem_iterations": 1}
+    ms = timed(lambda: (x.fill_(1.0), plan.cs_run_device(sino, x, it=1)), reps=3)
+    out["cs_osem"] = {"slice_iters_per_s": dn / (ms * 1e-3), "ms_per_10": ms}
+    plan.close()
+    # reslice: 1500 projections of 64 rows x 2048 -> 64 sinograms [1500][2048]
+    H = 64
+    mt = torch.rand((PA, H, PX), device="cuda")
+    dsino = torch.empty((H, PA, PX), device="cuda")
+    rng = np.random.default_rng(1)
+    rp = xct.ReslicePlan(ctx, PX, H, PA, rng.uniform(-2, 2, PA), rng.uniform(-1, 1, PA), 0.0, 1)
+    ms = timed(lambda: rp.reslice(mt, dsino))
+    gb = 2.0 * PA * H * PX * 4 / 1e9
+    out["reslice"] = {"rows": H, "projections": PA, "width": PX, "ms": ms, "hbm_gbs": gb / (ms * 1e-3),
+                      "hbm_peak_gbs": hbm_gbs, "frac": gb / (ms * 1e-3) / hbm_gbs if hbm_gbs else None}
+    d2 = torch.empty_like(dsino)
+    ms = timed(lambda: xct.denoise_sinogram(dsino, d2, 0.1))
+    out["denoise"] = {"ms": ms, "hbm_gbs": gb / (ms * 1e-3), "frac": gb / (ms * 1e-3) / hbm_gbs if hbm_gbs else None}
+    rp.close()
+    # rotation-centre search: 9 shifts (-4..4 bins) of one noisy 2048^2 slice whose true centre
+    # is px/2, 1500 angles, 15 subsets, one OS-EM iteration per shift
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(7)
+    noisy = phantom.noisy_log_sinogram_torch(sino[0], I0, generator=gen).contiguous()
+    rplan = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, 1, max_batch=9)
+    imgs = torch.empty((9, NY, NX), device="cuda")
+    rplan.rot_center_search(noisy, imgs, -4.0, 1.0)  # warm
+    t0 = time.perf_counter()
+    fi, best = rplan.rot_center_search(noisy, imgs, -4.0, 1.0)
+    dt = time.perf_counter() - t0
+    out["rot_center"] = {"shifts": 9, "s": dt, "shifts_per_s": 9 / dt, "best_shift": -4.0 + 1.0 * best,
+                         "sinogram_centre_offset": 0.0,
+                         "criterion": "the reference's smallest focus index (the oracle picks the same "
+                                      "shift for this phantom at 256^2 and 512^2)"}
+    rplan.close()
+    return out
+
+
 def profile_case():
     """Small case for profilers: one 2048^2 slice of the workload, its sinogram made with the
     forward projector (15 launches), then one OS-EM iteration (15 subsets: forward, finalize,
@@ -547,6 +637,18 @@ def main():
     except Exception as e:  # reported, never fatal
         volume = {"error": str(e)[:300]}
 
+    # ---- the components either side of the path ----
+    try:
+        hbm_peak = None
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = json.load(f).get("hbm_gbs")
+    except Exception:
+        pass
+    try:
+        nxt = next_components(ctx, hbm_peak)
+    except Exception as e:  # reported, never fatal
+        nxt = {"error": str(e)[:300]}
+
     # ---- roofline of the dominant kernel (live CUDA events, same stream) ----
     prof = plan.profile(sino[:DN], imgs[:DN].fill_(1.0), dN=DN, stream=stream)
     t_fwd, t_bp = algorithmic_counts(ang, NX, NY, PX)
@@ -605,7 +707,7 @@ def main():
                        "l2": "inputs larger than L2 (each step a new 290 MB batch)",
                        "parallelism": "dp%d over slices" % world},
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "per_slice": per_slice,
-            "ctxafs_batched": batched, "volume_stream": volume,
+            "ctxafs_batched": batched, "volume_stream": volume, "next_components": nxt,
             "roofline": roofline, "cpu_baseline": cpu, "finite": finite,
             "launches_per_step": launches / max(args.steps, 1),
         }

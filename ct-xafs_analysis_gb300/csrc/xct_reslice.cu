@@ -39,42 +39,108 @@ __device__ __forceinline__ float tex2(const float *__restrict__ im, int W, int H
     return (i >= 0 && j >= 0 && i < W && j < H) ? __ldg(im + (size_t)j * W + i) : 0.0f;
 }
 
-// grid: (ceil(W/256), H, n); prj[Y][th0 + th][X] for projection th of the chunk.
+constexpr int kRowsPerThread = 8;  // output rows a thread walks (reslice: Y; denoise: th)
+
+constexpr int kColsPerThread = 1;  // reslice: columns per thread (2 measured slower: fewer threads in flight)
+
+// grid: (ceil(W/(256*kColsPerThread)), ceil(H/8), n); prj[Y][th0 + th][X] for projection th
+// of the chunk.  A thread serves 8 rows Y of kColsPerThread columns X (256 apart).  The
+// sampler rows j(Y) = floor(Y + sy) are the same for every column and consecutive unless
+// rounding says otherwise (checked):
+// then the 9 texel rows the 8 outputs need are loaded at once -- every load in flight
+// together, each texel read once -- and each output is formed from registers with the
+// reference's arithmetic; otherwise each row loads its own 2x2 footprint.
 __global__ void __launch_bounds__(256) reslice_kernel(const float *__restrict__ mt, float *__restrict__ prj, int W,
                                                       int H, int A, int th0, const float *__restrict__ xs,
                                                       const float *__restrict__ ys, float baseup,
                                                       const float *__restrict__ corr)
 {
-    const int X = blockIdx.x * blockDim.x + threadIdx.x;
-    const int Y = blockIdx.y, th = blockIdx.z;
-    if (X >= W) return;
+    const int Yb = blockIdx.y * kRowsPerThread, th = blockIdx.z;
     const float *im = mt + (size_t)th * H * W;
     const float sx = __ldg(xs + th0 + th), sy = __ldg(ys + th0 + th);
-    const float uu = (((float)X + sx) + 0.5f) - 0.5f, vv = (((float)Y + sy) + 0.5f) - 0.5f;
-    const float fi = floorf(uu), fj = floorf(vv);
-    const float a = uu - fi, b = vv - fj;
-    const int i = (int)fi, j = (int)fj;
-    float t = (1.0f - a) * (1.0f - b) * tex2(im, W, H, i, j) + a * (1.0f - b) * tex2(im, W, H, i + 1, j) +
-              (1.0f - a) * b * tex2(im, W, H, i, j + 1) + a * b * tex2(im, W, H, i + 1, j + 1);
-    t += baseup;
-    if (corr != nullptr) t *= __ldg(corr + X);
-    prj[((size_t)Y * A + th0 + th) * W + X] = t;
+    const int n = min(kRowsPerThread, H - Yb);
+    int j[kRowsPerThread];
+    float b[kRowsPerThread];
+    bool run = true;
+#pragma unroll
+    for (int r = 0; r < kRowsPerThread; ++r) {
+        const float vv = (((float)(Yb + r) + sy) + 0.5f) - 0.5f;
+        const float fj = floorf(vv);
+        b[r] = vv - fj;
+        j[r] = (int)fj;
+        if (r > 0 && r < n && j[r] != j[r - 1] + 1) run = false;
+    }
+    const size_t ostep = (size_t)A * W;
+#pragma unroll
+    for (int cc = 0; cc < kColsPerThread; ++cc) {
+        const int X = blockIdx.x * (blockDim.x * kColsPerThread) + cc * blockDim.x + threadIdx.x;
+        if (X >= W) break;
+        const float uu = (((float)X + sx) + 0.5f) - 0.5f;
+        const float fi = floorf(uu);
+        const float a = uu - fi;
+        const int i = (int)fi;
+        const float cf = corr != nullptr ? __ldg(corr + X) : 1.0f;
+        float *out = prj + ((size_t)Yb * A + th0 + th) * W + X;
+        if (run) {
+            // zero border: the column tests once per column, the row test once per row
+            const bool in0 = (unsigned)i < (unsigned)W, in1 = (unsigned)(i + 1) < (unsigned)W;
+            const float *col = im + i;
+            float c0[kRowsPerThread + 1], c1[kRowsPerThread + 1];
+#pragma unroll
+            for (int r = 0; r <= kRowsPerThread; ++r) {
+                const int jr = j[0] + r;
+                const bool rok = r <= n && (unsigned)jr < (unsigned)H;
+                const float *p = col + (size_t)(rok ? jr : 0) * W;
+                c0[r] = (rok && in0) ? __ldg(p) : 0.0f;
+                c1[r] = (rok && in1) ? __ldg(p + 1) : 0.0f;
+            }
+#pragma unroll
+            for (int r = 0; r < kRowsPerThread; ++r) {
+                if (r < n) {
+                    float t = (1.0f - a) * (1.0f - b[r]) * c0[r] + a * (1.0f - b[r]) * c1[r] +
+                              (1.0f - a) * b[r] * c0[r + 1] + a * b[r] * c1[r + 1];
+                    t += baseup;
+                    if (corr != nullptr) t *= cf;
+                    out[r * ostep] = t;
+                }
+            }
+        } else {
+            for (int r = 0; r < n; ++r) {
+                float t = (1.0f - a) * (1.0f - b[r]) * tex2(im, W, H, i, j[r]) +
+                          a * (1.0f - b[r]) * tex2(im, W, H, i + 1, j[r]) +
+                          (1.0f - a) * b[r] * tex2(im, W, H, i, j[r] + 1) +
+                          a * b[r] * tex2(im, W, H, i + 1, j[r] + 1);
+                t += baseup;
+                if (corr != nullptr) t *= cf;
+                out[r * ostep] = t;
+            }
+        }
+    }
 }
 
-// grid: (ceil(W/256), A, H) over sinograms [H][A][W]; angle neighbours clamped to the edge.
+// grid: (ceil(W/256), ceil(A/8), H) over sinograms [H][A][W]; a thread walks 8 angles of one
+// column with the three angle rows in registers; neighbours clamped to the edge.
 __global__ void __launch_bounds__(256) denoise_kernel(const float *__restrict__ src, float *__restrict__ dst, int W,
                                                       int A, float thr)
 {
     const int X = blockIdx.x * blockDim.x + threadIdx.x;
-    const int th = blockIdx.y, Y = blockIdx.z;
+    const int t0 = blockIdx.y * kRowsPerThread, Y = blockIdx.z;
     if (X >= W) return;
     const float *base = src + (size_t)Y * A * W + X;
-    const float f1 = __ldg(base + (size_t)th * W);
-    const float f2 = __ldg(base + (size_t)min(th + 1, A - 1) * W);
-    const float f3 = __ldg(base + (size_t)max(th - 1, 0) * W);
-    const float d1 = f2 - f1, d2 = f1 - f3;
-    const float c = __fdiv_rn(f2 + f3, 2.0f);
-    dst[((size_t)Y * A + th) * W + X] = ((d1 > thr && d2 < -thr) || (d1 < -thr && d2 > thr)) ? c : f1;
+    // rows t0-1 .. t0+8 (clamped), all loads first
+    float f[kRowsPerThread + 2];
+#pragma unroll
+    for (int r = 0; r < kRowsPerThread + 2; ++r) f[r] = __ldg(base + (size_t)min(max(t0 - 1 + r, 0), A - 1) * W);
+    float *out = dst + ((size_t)Y * A + t0) * W + X;
+#pragma unroll
+    for (int r = 0; r < kRowsPerThread; ++r) {
+        if (t0 + r < A) {
+            const float f3 = f[r], f1 = f[r + 1], f2 = f[r + 2];
+            const float d1 = f2 - f1, d2 = f1 - f3;
+            const float c = (f2 + f3) * 0.5f;  // == (f2 + f3) / 2.0f exactly (a power of two)
+            out[(size_t)r * W] = ((d1 > thr && d2 < -thr) || (d1 < -thr && d2 > thr)) ? c : f1;
+        }
+    }
 }
 
 void reslice_free(xct_reslice_plan *p)
@@ -161,7 +227,8 @@ int xct_reslice(xct_reslice_plan *p, int first_angle, int n, const float *d_proj
         return xct_fail(XCT_E_INVALID, b);
     }
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
-    dim3 grid((p->W + 255) / 256, p->H, n);
+    dim3 grid((p->W + 256 * kColsPerThread - 1) / (256 * kColsPerThread), (p->H + kRowsPerThread - 1) / kRowsPerThread,
+              n);
     reslice_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_proj, d_sino, p->W, p->H, p->A, first_angle, p->d_xs,
                                                            p->d_ys, p->baseup, p->d_corr);
     XCT_CUDA_TRY(cudaGetLastError());
@@ -179,7 +246,7 @@ int xct_denoise_sinogram(int width, int n_angles, int n_rows, float threshold, c
     const char *s = (const char *)d_src, *d = (const char *)d_dst;
     if (s < d + bytes && d < s + bytes)
         return xct_fail(XCT_E_INVALID, "xct_denoise_sinogram: source and destination overlap");
-    dim3 grid((width + 255) / 256, n_angles, n_rows);
+    dim3 grid((width + 255) / 256, (n_angles + kRowsPerThread - 1) / kRowsPerThread, n_rows);
     denoise_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_src, d_dst, width, n_angles, threshold);
     XCT_CUDA_TRY(cudaGetLastError());
     g_xct_launches.fetch_add(1);
