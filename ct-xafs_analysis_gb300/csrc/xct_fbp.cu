@@ -29,6 +29,7 @@
 #include <algorithm>
 
 #include "xct_device.cuh"
+#include "xct_f32x2.cuh"
 #include "xct_internal.h"
 
 namespace {
@@ -228,6 +229,8 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
         xc[i] = (float)min(X0 + tx * 8 + i, X1) - g.hx;
         acc[i] = 0.0f;
     }
+    const f2x cxp = f2_pack(g.cx, g.cx), hp = f2_pack(0.5f, 0.5f), MM = f2_pack(12582912.0f, 12582912.0f);
+    const f2x one2 = f2_pack(1.0f, 1.0f);
     for (int k0 = 0; k0 < g.pa; k0 += kFbpChunk) {
         const int kn = min(kFbpChunk, g.pa - k0);
         __syncthreads();
@@ -257,13 +260,26 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
             // window entry of bin b: k*W + b - lo = (floor bits of b) + wb
             const int wb = k * kFbpW - sh.slo[k] - XCT_FLOOR_BIAS;
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const float uu = xct_bin_coord(xc[i], c, q, g.cx) - 0.5f;
-                const float tb = __fadd_rd(uu, 12582912.0f);
-                const float fi = tb - 12582912.0f;
-                const float a = uu - fi;
-                const int e = __float_as_int(tb) + wb;
-                acc[i] += (1.0f - a) * sh.win[e] + a * sh.win[e + 1];
+            for (int i = 0; i < 8; i += 2) {
+                // Xc*c - q in scalar (ptxas fuses a packed multiply feeding a packed subtract,
+                // and the reference rounds them separately); the additions, the round-down
+                // floor and the fraction packed over the pixel pair, each lane rounding as the
+                // scalar expression: uu = (((Xc*c - q) + cx) + 0.5) - 0.5, fi = floor(uu),
+                // a = uu - fi, then (1 - a) t[i] + a t[i+1]
+                const f2x d = f2_pack(xc[i] * c - q, xc[i + 1] * c - q);
+                const f2x uu = f2_sub(f2_add(f2_add(d, cxp), hp), hp);
+                const f2x tb = f2_add_rd(uu, MM);
+                const f2x a2 = f2_sub(uu, f2_sub(tb, MM));
+                const f2x w2 = f2_sub(one2, a2);
+                int e0, e1;
+                f2_unpack_bits(tb, e0, e1);
+                float a0, a1, w0, w1;
+                f2_unpack(a2, a0, a1);
+                f2_unpack(w2, w0, w1);
+                e0 += wb;
+                e1 += wb;
+                acc[i] += w0 * sh.win[e0] + a0 * sh.win[e0 + 1];
+                acc[i + 1] += w1 * sh.win[e1] + a1 * sh.win[e1 + 1];
             }
         }
     }
