@@ -485,6 +485,40 @@ def next_components(ctx, hbm_gbs):
     return out
 
 
+def profile_case_next():
+    """Small case for profilers, the components either side of the path, each once: FBP
+    (filter, backprojection, base-up) of one 2048^2 slice with 1500 angles; one
+    compressed-sensing iteration of 2 slices; the rotation-centre shift and focus index of 4
+    shifts; reslice and denoise of 1500 projections x 64 rows x 2048.  ~2 GB on the device."""
+    import torch
+    import xct
+    from xct import phantom
+    ang = phantom.uniform_angles(PA)
+    ctx = xct.Context(0)
+    plan = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, 1, max_batch=4)
+    pars = phantom.ellipsoid_params(NX, NSLICES, 30, 2, mu=(0.005, 0.1))
+    img = phantom.ellipsoid_slice(pars, NSLICES // 2, NX, NY, torch_device="cuda").reshape(1, NY, NX).contiguous()
+    sino = torch.empty((2, PA, PX), device="cuda")
+    plan.fwd(img, sino[:1])
+    sino[1].copy_(sino[0])
+    x = torch.empty((2, NY, NX), device="cuda")
+    plan.hybrid(sino[:1], x[:1], zp=4096, it=0)
+    x.fill_(1.0)
+    plan.cs_run_device(sino, x, it=1)
+    sh = torch.empty((4, PA, PX), device="cuda")
+    plan.rot_center_shift(sino[0], sh, -1.0, 0.5)
+    fi = torch.empty(4, device="cuda")
+    plan.focus_index(x[:1].expand(4, NY, NX).contiguous(), fi, -1.0, 0.5, float(ang[0]), float(ang[-1]))
+    mt = torch.rand((PA, 64, PX), device="cuda")
+    rp = xct.ReslicePlan(ctx, PX, 64, PA, None, np.linspace(-1, 1, PA), 0.0, 0)
+    d = torch.empty((64, PA, PX), device="cuda")
+    rp.reslice(mt, d)
+    d2 = torch.empty_like(d)
+    xct.denoise_sinogram(d, d2, 0.1)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "next", "ok": bool(torch.isfinite(x).all())}))
+
+
 def profile_case():
     """Small case for profilers: one 2048^2 slice of the workload, its sinogram made with the
     forward projector (15 launches), then one OS-EM iteration (15 subsets: forward, finalize,
@@ -512,11 +546,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", action="store_true",
-                    help="run the small profiling case (one slice, one iteration) and exit")
+    ap.add_argument("--profile-case", nargs="?", const="osem", choices=["osem", "next"],
+                    help="run a small profiling case and exit: osem (one slice, one OS-EM iteration) or next "
+                         "(the components either side of the path, each once)")
     args = ap.parse_args()
-    if args.profile_case:
+    if args.profile_case == "osem":
         profile_case()
+        return
+    if args.profile_case == "next":
+        profile_case_next()
         return
 
     rank = _env_int("RANK", 0)
