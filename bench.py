@@ -612,9 +612,8 @@ def main():
     clk.stop()
     ms = e0.elapsed_time(e1)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        from xct import shard
+        ms = shard.max_over_ranks(ms, device=dev)
     slice_iters = args.steps * DN * IT * world
     value = slice_iters / (ms * 1e-3)
 
