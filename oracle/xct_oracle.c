@@ -25,10 +25,12 @@
  *                                                 -> xo_ista3d_f32, xo_fista3d_f32
  *
  * Parity pin: the reference ships no tests, fixtures or golden vectors, and its OpenCL
- * runtime is not available, so the pin is oracle/_ref: the reference's own OSEM.cl and
- * reconstShare.cl kernel bodies compiled with g++ against an OpenCL-C shim (recipe:
- * oracle/build_ref.py), driven by the same host loop.  The literal evaluation order of
- * this oracle matches that build to the last bit on the committed fixtures (tests/).
+ * runtime is not available, so the pin is oracle/_ref: the reference's own kernel bodies --
+ * CT_reconstruction/OSEM.cl, FISTA.cl, reconstShare.cl, FBP.cl,
+ * RotationCenterSearch/rotCenterSearch.cl and Reslice/reslice.cl -- compiled with g++
+ * against an OpenCL-C shim (recipe: oracle/build_ref.py), driven by host loops that restate
+ * the reference's executors.  The literal evaluation order of this oracle matches that build
+ * to the last bit on the committed fixtures (tests/).
  * Where oracle/_ref cannot be built (no reference sources present), parity rests on the
  * committed golden fixtures generated here.
  *
