@@ -418,9 +418,9 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
         const float b = (float)min(X0 + tx * 8 + 2 * j + 1, X1) - g.hx;
         xcp[j] = f2_pack(a, b);
     }
-    float acc[8];
+    f2x acc2[4];  // pixel pairs, accumulated with packed adds (each lane an IEEE add)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) acc[i] = 0.0f;
+    for (int j = 0; j < 4; ++j) acc2[j] = f2_pack(0.0f, 0.0f);
     const f2x cxp = f2_pack(g.cx, g.cx);
     const f2x hp = f2_pack(0.5f, 0.5f);
     const f2x MM = f2_pack(kMagic, kMagic);
@@ -469,13 +469,15 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
                 const f2x t = f2_add_rd(f2_add(f2_add(f2_pack(da, db), cxp), hp), MM);
                 int b0, b1;
                 f2_unpack_bits(t, b0, b1);
-                acc[2 * j] += lds_f1((unsigned)b0 * 4u + off);
-                acc[2 * j + 1] += lds_f1((unsigned)b1 * 4u + off);
+                acc2[j] = f2_add(acc2[j], f2_pack(lds_f1((unsigned)b0 * 4u + off), lds_f1((unsigned)b1 * 4u + off)));
             }
         }
     }
     if (Y <= Y1) {
         float *row = img + (size_t)Y * g.nx;
+        float acc[8];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) f2_unpack(acc2[j], acc[2 * j], acc[2 * j + 1]);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int X = X0 + tx * 8 + i;
