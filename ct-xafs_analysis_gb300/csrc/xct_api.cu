@@ -574,17 +574,23 @@ int xct_fbp_run_device(xct_plan *p, int dN, int zp, const float *d_sino, float *
     return fbp_device(p, dN, zp, d_sino, d_img, false, nullptr, (cudaStream_t)stream);
 }
 
+static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, float lambda,
+                   cudaStream_t st, bool correct = true);
+static float cs_kernel_lambda(float cs_lambda);
+
 // hybrid_thread (GPU.cpp:1458-1600): FBP_execution with the sinogram correction, the
 // base-up of FBPcorrection = 1 (slice minimum, then baseUp with baseupOrder), then
-// OSEM_execution on the corrected sinogram without correcting it again.
+// OSEM_execution -- or FISTA_OSEM_execution when CSitBool is set (:1569-1574) -- on the
+// corrected sinogram without correcting it again.
 static int hybrid_device(xct_plan *p, int dN, int zp, int order, const float *d_sino, float *d_img, const int *sub,
-                         int it, cudaStream_t st)
+                         int it, cudaStream_t st, bool cs = false, float lambda = 0.0f)
 {
     const float *meas = nullptr;
     int rc = fbp_device(p, dN, zp, d_sino, d_img, true, &meas, st);
     if (rc) return rc;
     rc = launch_base_up(p->kg, d_img, dN, order, p->d_min_keys, p->ctx->sm_count, st);
     if (rc) return rc;
+    if (cs) return cs_loop(p, dN, meas, d_img, sub ? sub : p->sub_default.data(), it, lambda, st, false);
     return osem_loop(p, dN, meas, d_img, sub ? sub : p->sub_default.data(), it, st, false);
 }
 
@@ -649,6 +655,40 @@ int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *c
     if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
     return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
         return hybrid_device(p, dN, zp, baseup_order, p->d_sino, p->d_img, sub, it, st);
+    });
+}
+
+// The hybrid with CSitBool: FBP, base-up, then the compressed-sensing OS-EM.
+int xct_hybrid_cs_run_device(xct_plan *p, int dN, int zp, int baseup_order, const float *d_sino, float *d_img,
+                             const int *sub, int it, float cs_lambda, void *stream)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_hybrid_cs_run_device: null device pointer");
+    if (baseup_order < 0 || baseup_order > 64)
+        return xct_fail(XCT_E_INVALID, "xct_hybrid_cs_run_device: order 0..64");
+    if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
+        return xct_fail(XCT_E_INVALID, "xct_hybrid_cs_run_device: cs_lambda must be finite and >= 0");
+    if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return hybrid_device(p, dN, zp, baseup_order, d_sino, d_img, sub, it, (cudaStream_t)stream, true,
+                         cs_kernel_lambda(cs_lambda));
+}
+
+int xct_hybrid_cs_run(xct_plan *p, int dN, int zp, int baseup_order, const float *const *sino_host,
+                      float *const *img_host, const int *sub, int it, float cs_lambda)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (baseup_order < 0 || baseup_order > 64) return xct_fail(XCT_E_INVALID, "xct_hybrid_cs_run: order 0..64");
+    if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
+        return xct_fail(XCT_E_INVALID, "xct_hybrid_cs_run: cs_lambda must be finite and >= 0");
+    if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    const float lam = cs_kernel_lambda(cs_lambda);
+    return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
+        return hybrid_device(p, dN, zp, baseup_order, p->d_sino, p->d_img, sub, it, st, true, lam);
     });
 }
 
@@ -759,7 +799,7 @@ static float cs_kernel_lambda(float cs_lambda)
 // updated dest image, to ISTA3D (:335-336, :388) -- so its OS-EM step is dead work and is
 // skipped here (the ratio rows it would write are rewritten before every later read).
 static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, float lambda,
-                   cudaStream_t st)
+                   cudaStream_t st, bool correct)
 {
     const KGeom &g = p->kg;
     const size_t nimg = (size_t)g.nx * g.ny, nb = (size_t)p->g.max_batch;
@@ -773,7 +813,7 @@ static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const
     float *w = p->d_cs, *beta = p->d_cs + nb * nimg, *xn = p->d_cs + 2 * nb * nimg;
     const size_t bytes = sizeof(float) * dN * nimg;
     const float *meas = d_sino;
-    if (p->g.correction_mode > 0) {
+    if (correct && p->g.correction_mode > 0) {
         int rc = launch_sino_correction(g, d_sino, p->d_corr, p->d_corr_ang, p->d_corr_bin, p->g.correction_mode, dN,
                                         st);
         if (rc) return rc;

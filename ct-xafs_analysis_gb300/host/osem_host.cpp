@@ -72,6 +72,8 @@ void osem_thread(DeviceSlot *d, std::vector<float *> imgs, std::vector<float *> 
     const int dN = endN - startN + 1;
     int rc;
     if (g_method == METHOD_FBP) rc = xct_fbp_run(d->plan, dN, g_zp, prjs.data(), imgs.data());
+    else if (g_method == METHOD_HYBRID && CSitBool)  // hybrid_thread's FISTA branch (GPU.cpp:1569-1571)
+        rc = xct_hybrid_cs_run(d->plan, dN, g_zp, baseupOrder, prjs.data(), imgs.data(), g_sub.data(), g_it, CSlambda);
     else if (g_method == METHOD_HYBRID)
         rc = xct_hybrid_run(d->plan, dN, g_zp, baseupOrder, prjs.data(), imgs.data(), g_sub.data(), g_it);
     else if (CSitBool)  // FISTA_OSEM_execution (GPU.cpp:449-453)
@@ -83,7 +85,7 @@ void osem_thread(DeviceSlot *d, std::vector<float *> imgs, std::vector<float *> 
     }
     // compressed sensing: batches overlap by CSoverlap slices; inner batch edges are not
     // written (GPU.cpp:456-460)
-    const bool cs = CSitBool && g_method == METHOD_OSEM;
+    const bool cs = CSitBool && g_method != METHOD_FBP;
     const int offset = (cs && startN > g_st) ? CSoverlap : 0;
     const int out_end = (cs && endN < g_st + g_num - 1) ? endN - CSoverlap : endN;
     join(d->output_th);
@@ -168,7 +170,8 @@ int run_pipeline(const std::vector<int> &devices, const std::vector<float> &ang,
     }
     const int last = g_st + g_num - 1;
     // compressed sensing: consecutive batches overlap by 2*CSoverlap slices (GPU.cpp:636-647)
-    const int cs_delta = (CSitBool && method == METHOD_OSEM) ? CSoverlap : 0;
+    // (OSEM_ocl and hybrid_ocl, GPU.cpp:636-647, 1718-1734; FBP_ocl never overlaps)
+    const int cs_delta = (CSitBool && method != METHOD_FBP) ? CSoverlap : 0;
     for (auto &d : slots)
         if (d->dN - 2 * cs_delta <= 0) {
             std::cerr << "ERROR: " << d->dN << " slices per call cannot overlap by " << cs_delta
@@ -207,11 +210,6 @@ int GPU()
     if (g_ox != g_nx || g_oy != g_ny) {
         std::cerr << "ERROR: an output size smaller than the reconstruction size is not supported" << std::endl;
         return XCT_E_INVALID;
-    }
-    if (CSitBool && (g_mode == 7 || g_mode == 8)) {
-        std::cerr << "ERROR: compressed sensing is available with the OS-EM family (2, 4, 5, 6), not with method "
-                  << g_mode << std::endl;
-        return XCT_E_UNSUPPORTED;
     }
     int ndev = 0;
     if (xct_device_count(&ndev) != XCT_OK) {

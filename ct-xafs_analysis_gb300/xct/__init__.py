@@ -51,7 +51,8 @@ EXPORTS = (
     "xct_hybrid_run", "xct_rot_center_shift", "xct_focus_index", "xct_rot_center_search",
     "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_denoise_sinogram",
     "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
-    "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume",
+    "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume", "xct_hybrid_cs_run_device",
+    "xct_hybrid_cs_run",
 )
 
 TUNE_FORCE = 1
@@ -131,6 +132,9 @@ def load():
     L.xct_cs_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
     L.xct_cs_osem_run.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int), ip,
                                   c_f]
+    L.xct_hybrid_cs_run_device.argtypes = [vp, ip, ip, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
+    L.xct_hybrid_cs_run.argtypes = [vp, ip, ip, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int),
+                                    ip, c_f]
     L.xct_osem_run_volume.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int),
                                       ip]
     L.xct_plan_autotune.argtypes = [vp, ip, ctypes.c_char_p, ip, vp]
@@ -315,6 +319,13 @@ class OSEMPlan:
         _check(self._lib.xct_fbp_run(self.handle, len(sinos), zp, s_arr, i_arr))
         return imgs
 
+    def hybrid_cs_run(self, sinos, imgs, zp=0, baseup_order=4, cs_lambda=1.0e-4, sub=None, it=-1):
+        """FBP + base-up + compressed-sensing OS-EM (hybrid_thread with CSitBool) on host arrays."""
+        s_arr, i_arr = self._host_arrays(sinos, imgs)
+        _check(self._lib.xct_hybrid_cs_run(self.handle, len(sinos), zp, baseup_order, s_arr, i_arr, self._sub(sub),
+                                           it, cs_lambda))
+        return imgs
+
     def hybrid_run(self, sinos, imgs, zp=0, baseup_order=4, sub=None, it=-1):
         """FBP + base-up + OS-EM (hybrid_thread) on host arrays."""
         s_arr, i_arr = self._host_arrays(sinos, imgs)
@@ -376,6 +387,13 @@ class OSEMPlan:
         """FBP_execution: (correction), filter, backprojection."""
         dN = d_img.shape[0] if dN is None else dN
         _check(self._lib.xct_fbp_run_device(self.handle, dN, zp, _ptr(d_sino), _ptr(d_img), _stream(stream)))
+
+    def hybrid_cs(self, d_sino, d_img, zp=0, baseup_order=4, cs_lambda=1.0e-4, dN=None, sub=None, it=-1,
+                  stream=None):
+        """FBP + base-up + compressed-sensing OS-EM on device tensors."""
+        dN = d_img.shape[0] if dN is None else dN
+        _check(self._lib.xct_hybrid_cs_run_device(self.handle, dN, zp, baseup_order, _ptr(d_sino), _ptr(d_img),
+                                                  self._sub(sub), it, cs_lambda, _stream(stream)))
 
     def hybrid(self, d_sino, d_img, zp=0, baseup_order=4, dN=None, sub=None, it=-1, stream=None):
         """FBP + base-up + OS-EM of hybrid_thread on device tensors."""

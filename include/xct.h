@@ -211,6 +211,13 @@ int xct_fbp_run_device(xct_plan *plan, int dN, int zp, const float *d_sino, floa
 int xct_hybrid_run_device(xct_plan *plan, int dN, int zp, int baseup_order, const float *d_sino, float *d_img,
                           const int *sub, int it, void *stream);
 int xct_fbp_run(xct_plan *plan, int dN, int zp, const float *const *sino_host, float *const *img_host);
+/* The hybrid with CSitBool set (hybrid_thread, GPU.cpp:1569-1574): FBP and base-up as above,
+ * then the compressed-sensing OS-EM of xct_cs_osem_run_device (FISTA_OSEM_execution) instead
+ * of OSEM_execution; cs_lambda is CSlambda.  Host-buffer and device forms. */
+int xct_hybrid_cs_run_device(xct_plan *plan, int dN, int zp, int baseup_order, const float *d_sino, float *d_img,
+                             const int *sub, int it, float cs_lambda, void *stream);
+int xct_hybrid_cs_run(xct_plan *plan, int dN, int zp, int baseup_order, const float *const *sino_host,
+                      float *const *img_host, const int *sub, int it, float cs_lambda);
 int xct_hybrid_run(xct_plan *plan, int dN, int zp, int baseup_order, const float *const *sino_host,
                    float *const *img_host, const int *sub, int it);
 

@@ -74,3 +74,28 @@ def test_cs_argument_errors(gpu_ctx):
         with pytest.raises(xct.XCTError):
             plan.cs_run_device(d_s, d_x, cs_lambda=lam)
     plan.close()
+
+
+def test_hybrid_with_compressed_sensing(gpu_ctx, oracle_lib):
+    """hybrid_thread with CSitBool (GPU.cpp:1569-1571): FBP, base-up, then the compressed-
+    sensing OS-EM on the corrected sinogram; against the oracle's composition of the three
+    (each pinned to the reference's kernels), the FBP filter's rounding carried through."""
+    import xct
+    O = oracle_lib
+    f = _load("cs_64")
+    n, px, pa, ss, it, dN = [int(v) for v in f["shape"]]
+    lam = float(f["cs_lambda"][0])
+    plan = _plan(gpu_ctx, f, xct.KERNELS_TILED)
+    d_s = torch.from_numpy(f["meas"]).cuda()
+    d_x = torch.zeros((dN, n, n), device="cuda")
+    plan.hybrid_cs(d_s, d_x, zp=128, baseup_order=4, cs_lambda=lam, sub=f["sub"])
+    torch.cuda.synchronize()
+    x0 = np.stack([O.base_up(O.fbp(f["meas"][z], f["angles"], n, n, 128), 4)[0] for z in range(dN)])
+    want = O.cs_osem_run(x0, f["meas"], f["angles"], ss, it, lam, f["sub"], order=O.ORDER_LITERAL)
+    got = d_x.cpu().numpy()
+    assert _rel(got, want) <= 1e-4
+    out = [np.zeros((n, n), np.float32) for _ in range(dN)]
+    plan.hybrid_cs_run([f["meas"][z].copy() for z in range(dN)], out, zp=128, baseup_order=4, cs_lambda=lam,
+                       sub=f["sub"])
+    assert _rel(np.stack(out), got) <= 1e-6
+    plan.close()

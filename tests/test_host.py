@@ -134,10 +134,13 @@ def test_fbp_and_hybrid_methods_from_files(host_bin, oracle_lib, tmp_path, metho
 
 
 @pytest.mark.gpu
-def test_compressed_sensing_batches_from_files(host_bin, oracle_lib, tmp_path):
-    """CSitBool with 4 slices per call overlapping by 1 (GPU.cpp:636-647, 449-460): slices
-    7..12 run as batches [7..10], [9..12] and -- the dispatcher steps by dN - 2 while the start
-    is in range -- [11..12]; each slice file holds the batch that writes it last."""
+@pytest.mark.parametrize("method", [6, 8])
+def test_compressed_sensing_batches_from_files(host_bin, oracle_lib, tmp_path, method):
+    """CSitBool with 4 slices per call overlapping by 1 (GPU.cpp:636-647, 449-460; the hybrid's
+    dispatcher likewise, :1718-1734): slices 7..12 run as batches [7..10], [9..12] and -- the
+    dispatcher steps by dN - 2 while the start is in range -- [11..12]; each slice file holds
+    the batch that writes it last.  Method 6: OS-EM; method 8: FBP, base-up, then the
+    compressed-sensing OS-EM (hybrid_thread, :1569-1571)."""
     from xct import phantom as P
     O = oracle_lib
     n, px, pa, ss, it = 48, 48, 40, 4, 2
@@ -155,14 +158,18 @@ def test_compressed_sensing_batches_from_files(host_bin, oracle_lib, tmp_path):
     inp = tmp_path / "run.inp"
     keys = [("#逐次圧縮センシング計算 (FBP適応外)", "1"), ("#逐次圧縮センシング計算加算ファクター", "0.0002"),
             ("#逐次圧縮センシング計算重複レイヤー数", "1")]
+    keys += [("#ゼロパディングサイズ(FBP)", "128"), ("#Base up 減少速度次数 (Hybrid)", "4")]
     write_inp(inp, extra=keys, d1=str(d1), d2=str(d2), f3=str(tmp_path / "angles.log"), px=px, pa=pa, n=n, it=it,
-              ss=ss, layers=6, par=4)
+              ss=ss, layers=6, par=4, method=method)
     r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
     assert r.returncode == 0, r.stdout + r.stderr
-    x0 = np.ones((4, n, n), np.float32)
-    b1 = O.cs_osem_run(x0, np.stack([meas[z] for z in range(7, 11)]), ang, ss, it, 2e-4)
-    b2 = O.cs_osem_run(x0, np.stack([meas[z] for z in range(9, 13)]), ang, ss, it, 2e-4)
-    b3 = O.cs_osem_run(x0[:2], np.stack([meas[z] for z in range(11, 13)]), ang, ss, it, 2e-4)
+    def batch(zs):
+        if method == 6:
+            x0 = np.ones((len(zs), n, n), np.float32)
+        else:
+            x0 = np.stack([O.base_up(O.fbp(meas[z], ang, n, n, 128), 4)[0] for z in zs])
+        return O.cs_osem_run(x0, np.stack([meas[z] for z in zs]), ang, ss, it, 2e-4)
+    b1, b2, b3 = batch(range(7, 11)), batch(range(9, 13)), batch(range(11, 13))
     want = {7: b1[0], 8: b1[1], 9: b1[2], 10: b2[1], 11: b2[2], 12: b3[1]}
     for z, ref in want.items():
         got = np.fromfile(d2 / ("rec_%04d.img" % z), np.float32).reshape(n, n)
