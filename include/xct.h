@@ -51,7 +51,9 @@ typedef struct xct_plan xct_plan;
  * GPU.cpp:538-548, plus the globals g_it, g_ss of main.cpp:29,35). */
 typedef struct {
     int nx, ny;                /* reconstruction size (IMAGESIZE_X, IMAGESIZE_Y)              */
-    int ox, oy;                /* output ROI; must equal nx, ny (see DESIGN: ROI < full)      */
+    int ox, oy;                /* output ROI; must equal nx, ny (the reference's ROI < full
+                                  path writes the top-left corner but reads and saves a centred
+                                  window, GPU.cpp:152-153,170; only the full image is defined) */
     int px, pa;                /* detector bins (PRJ_IMAGESIZE), angles (PRJ_ANGLESIZE)       */
     int ss;                    /* subsets (SS)                                                 */
     int it;                    /* iterations (g_it)                                            */
