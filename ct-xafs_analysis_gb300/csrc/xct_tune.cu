@@ -4,15 +4,16 @@
 // 92 base texels; a CTA stages one tile and serves its angles from shared memory) and the
 // number of subset angles one CTA serves (the chunk, 16..128).  Large values amortise the
 // staging and the per-ray interval search; small values give more CTAs, which small slices
-// and small subsets need to fill 152 SMs.  The kernel is register-limited to 3 CTAs (36 warps)
-// per SM at every T, so the choice only changes the grid's granularity and the per-tile
-// overheads -- a trade-off that depends on the slice size, the angles per subset and the
-// slices per call, so it is measured: xct_plan_autotune times every candidate on the plan's
+// and small subsets need to fill 152 SMs.  Four CTAs (48 warps) fit on an SM for T <= 76 and
+// three (36 warps) for T = 92, so the choice changes the occupancy, the grid's granularity and
+// the per-tile overheads -- a trade-off that depends on the slice size, the angles per subset
+// and the slices per call, so it is measured: xct_plan_autotune times every candidate on the plan's
 // own geometry and keeps the fastest; the choice is cached per (device, shape) in memory and,
 // optionally, in a JSON file that later plans (and processes) read.
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <map>
@@ -61,7 +62,9 @@ void load_file(const char *path, std::map<std::string, TuneChoice> &out)
 
 int save_file(const char *path, const std::map<std::string, TuneChoice> &m)
 {
-    std::string tmp = std::string(path) + ".tmp";
+    // a per-process temporary, so that processes saving at once never share one; the
+    // rename replaces the file atomically (the last writer's entries win)
+    std::string tmp = std::string(path) + ".tmp." + std::to_string((long long)getpid());
     FILE *f = fopen(tmp.c_str(), "w");
     if (!f) return xct_fail(XCT_E_IO, std::string("tune cache: cannot write ") + tmp);
     fprintf(f, "{\n  \"xct_tune_cache\": 1,\n  \"entries\": {\n");
