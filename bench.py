@@ -510,7 +510,8 @@ def profile_case_next():
     fi = torch.empty(4, device="cuda")
     plan.focus_index(x[:1].expand(4, NY, NX).contiguous(), fi, -1.0, 0.5, float(ang[0]), float(ang[-1]))
     mt = torch.rand((PA, 64, PX), device="cuda")
-    rp = xct.ReslicePlan(ctx, PX, 64, PA, None, np.linspace(-1, 1, PA), 0.0, 0)
+    rng = np.random.default_rng(1)  # the benchmark's drift shifts and correction
+    rp = xct.ReslicePlan(ctx, PX, 64, PA, rng.uniform(-2, 2, PA), rng.uniform(-1, 1, PA), 0.0, 1)
     d = torch.empty((64, PA, PX), device="cuda")
     rp.reslice(mt, d)
     d2 = torch.empty_like(d)

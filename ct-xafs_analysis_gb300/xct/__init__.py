@@ -539,9 +539,11 @@ class ReslicePlan:
         _check(self._lib.xct_reslice(self.handle, first_angle, n, _ptr(d_proj), _ptr(d_sino), _stream(stream)))
 
     def close(self):
+        """Destroys the plan; raises XCTError (XCT_E_TIMEOUT) if a staged-window copy of any
+        reslice call missed its wait limit (those tiles were computed from global memory)."""
         if self.handle:
-            self._lib.xct_reslice_plan_destroy(self.handle)
-            self.handle = None
+            h, self.handle = self.handle, None
+            _check(self._lib.xct_reslice_plan_destroy(h))
 
     def __del__(self):
         try:

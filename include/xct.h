@@ -261,6 +261,12 @@ int xct_rot_center_search(xct_plan *plan, int n, float shift_start, float shift_
  *               d_sino[Y][th][X] = bilinear(projection th at (X + xshift[th], Y + yshift[th]),
  *               zero outside) + baseup.  Row Y of d_sino is slice Y's sinogram [n_angles][width],
  *               so d_sino + Y0*n_angles*width is a ready dN-slice input of the OS-EM/FBP calls.
+ *               Widths that are a multiple of 4 with a 16-byte aligned d_proj run a kernel
+ *               that stages each tile's sampler window in shared memory by tensor copies
+ *               (TMA); its waits are bounded (about a second), and a tile whose copy misses the
+ *               limit is computed from global memory instead, so the output is always complete.
+ * xct_reslice_plan_destroy : synchronises the device; returns XCT_E_TIMEOUT if any copy of
+ *               the plan's calls missed its wait limit (a fault report only).
  * xct_denoise_sinogram : denoiseSinogram (reslice.cl:223-248) on n_rows sinograms
  *               [n_angles][width]: a value that is a one-angle spike beyond +-threshold against
  *               both angle neighbours (clamped at the ends) becomes their mean.  d_src and
