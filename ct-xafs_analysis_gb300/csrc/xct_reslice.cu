@@ -48,6 +48,7 @@ struct xct_reslice_plan {
     float *d_corr = nullptr;  // [W] cos(asin(2|X - W/2|/W)) when correction == 1
     int *d_err = nullptr;     // set by reslice_tma_kernel when a copy wait gave up
     int tma_grid = 0;         // persistent CTAs of reslice_tma_kernel (0: not set up)
+    long long wait_clocks = 0;  // limit of its waits for staged copies (SM clocks)
 };
 
 namespace {
@@ -176,7 +177,8 @@ constexpr size_t kTmaSlotBytes = 512;  // one TmaTileInfo per stage
 constexpr size_t kTmaBarBytes = (8 * kTmaStages + 15) / 16 * 16;
 constexpr size_t kTmaSmem = 1024 + (size_t)kTmaStages * kTmaStagePitch + kTmaBarBytes + kTmaStages * kTmaSlotBytes;
 // A copy normally lands in microseconds; a wait gives up after ~2^31 SM clocks (about a
-// second), flags the plan and the CTA finishes its tiles from global memory.
+// second; xct_reslice_plan_set_wait_limit changes the tile waits, not the final drain),
+// flags the plan and the CTA finishes its tiles from global memory.
 constexpr long long kTmaWaitClocks = 1ll << 31;
 
 __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
@@ -199,15 +201,17 @@ __device__ __forceinline__ bool mbar_test(unsigned bar, unsigned parity)
         : "memory");
     return ok != 0;
 }
-// Wait for phase `parity` of the barrier to complete, at most kTmaWaitClocks.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity)
+// Wait for phase `parity` of the barrier to complete, at most `limit` SM clocks; a negative
+// limit gives up at once (the plan's diagnostic setting).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity, long long limit)
 {
+    if (limit < 0) return false;
     if (mbar_test(bar, parity)) return true;
     const long long t0 = clock64();
     for (;;) {
         __nanosleep(32);
         if (mbar_test(bar, parity)) return true;
-        if (clock64() - t0 > kTmaWaitClocks) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
 // Box (x, y, z) of the tensor map into shared memory at dst; completion counted on bar.
@@ -251,7 +255,8 @@ __global__ void __launch_bounds__(kTmaThreads, 4) reslice_tma_kernel(const __gri
                                                                   float *__restrict__ prj, int W, int H, int A,
                                                                   int th0, int n, const float *__restrict__ xs,
                                                                   const float *__restrict__ ys, float baseup,
-                                                                  const float *__restrict__ corr, int *err)
+                                                                  const float *__restrict__ corr, int *err,
+                                                                  long long wait_clocks)
 {
     extern __shared__ unsigned char smem_raw[];
     const unsigned raw = (unsigned)__cvta_generic_to_shared(smem_raw);
@@ -354,7 +359,7 @@ __global__ void __launch_bounds__(kTmaThreads, 4) reslice_tma_kernel(const __gri
     const size_t ostep = (size_t)A * W;
     for (long long k = 0; k < nmine; ++k) {
         const unsigned s = (unsigned)(k % kTmaStages), parity = (unsigned)((k / kTmaStages) & 1);
-        bool ok = alive && mbar_wait_bounded(bars + 8u * s, parity);
+        bool ok = alive && mbar_wait_bounded(bars + 8u * s, parity, wait_clocks);
         // one barrier per tile: makes the outcome uniform, publishes the slots written since
         // the last one, and frees the previous tile's stage and slot
         ok = __syncthreads_and(ok) != 0;
@@ -430,7 +435,8 @@ __global__ void __launch_bounds__(kTmaThreads, 4) reslice_tma_kernel(const __gri
     // let them land before the CTA's shared memory is released, each wait again bounded
     if (tid == 0)
         for (long long k = consumed; k < issued; ++k)
-            (void)mbar_wait_bounded(bars + 8u * (unsigned)(k % kTmaStages), (unsigned)((k / kTmaStages) & 1));
+            (void)mbar_wait_bounded(bars + 8u * (unsigned)(k % kTmaStages), (unsigned)((k / kTmaStages) & 1),
+                                    kTmaWaitClocks);
 }
 
 // grid: (ceil(W/256), ceil(A/8), H) over sinograms [H][A][W]; a thread walks 8 angles of one
@@ -529,6 +535,7 @@ int xct_reslice_plan_create(xct_ctx *ctx, int width, int height, int n_angles, c
     p->A = n_angles;
     p->baseup = baseup;
     p->correction = correction;
+    p->wait_clocks = kTmaWaitClocks;
     auto fail = [&](cudaError_t e, const char *what) {
         int r = xct_cuda_fail(e, what);
         reslice_free(p);
@@ -599,7 +606,8 @@ int xct_reslice(xct_reslice_plan *p, int first_angle, int n, const float *d_proj
         const long long tiles = (long long)((p->W + kTmaCols - 1) / kTmaCols) * ((p->H + kTmaRows - 1) / kTmaRows) * n;
         const int grid = (int)std::min<long long>(tiles, p->tma_grid);
         reslice_tma_kernel<<<grid, kTmaThreads, kTmaSmem, (cudaStream_t)stream>>>(
-            map, d_proj, d_sino, p->W, p->H, p->A, first_angle, n, p->d_xs, p->d_ys, p->baseup, p->d_corr, p->d_err);
+            map, d_proj, d_sino, p->W, p->H, p->A, first_angle, n, p->d_xs, p->d_ys, p->baseup, p->d_corr, p->d_err,
+            p->wait_clocks);
     } else {
         dim3 grid((p->W + 256 * kColsPerThread - 1) / (256 * kColsPerThread),
                   (p->H + kRowsPerThread - 1) / kRowsPerThread, n);
@@ -608,6 +616,13 @@ int xct_reslice(xct_reslice_plan *p, int first_angle, int n, const float *d_proj
     }
     XCT_CUDA_TRY(cudaGetLastError());
     g_xct_launches.fetch_add(1);
+    return XCT_OK;
+}
+
+int xct_reslice_plan_set_wait_limit(xct_reslice_plan *p, long long sm_clocks)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "xct_reslice_plan_set_wait_limit: plan is null");
+    p->wait_clocks = sm_clocks;
     return XCT_OK;
 }
 

@@ -49,7 +49,8 @@ EXPORTS = (
     "xct_batch_plan_create", "xct_batch_run", "xct_batch_plan_destroy", "xct_osem_run_batched",
     "xct_fbp_filter", "xct_fbp_backproject", "xct_fbp_run_device", "xct_hybrid_run_device", "xct_fbp_run",
     "xct_hybrid_run", "xct_rot_center_shift", "xct_focus_index", "xct_rot_center_search",
-    "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_denoise_sinogram",
+    "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_reslice_plan_set_wait_limit",
+    "xct_denoise_sinogram",
     "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
     "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume", "xct_hybrid_cs_run_device",
     "xct_hybrid_cs_run",
@@ -128,6 +129,7 @@ def load():
     L.xct_reslice_plan_create.argtypes = [vp, ip, ip, ip, fp, fp, c_f, ip, ctypes.POINTER(vp)]
     L.xct_reslice.argtypes = [vp, ip, ip, vp, vp, vp]
     L.xct_reslice_plan_destroy.argtypes = [vp]
+    L.xct_reslice_plan_set_wait_limit.argtypes = [vp, ctypes.c_longlong]
     L.xct_denoise_sinogram.argtypes = [ip, ip, ip, c_f, vp, vp, vp]
     L.xct_cs_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
     L.xct_cs_osem_run.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int), ip,
@@ -537,6 +539,11 @@ class ReslicePlan:
         """d_proj [n][height][width] (angles first_angle..) -> rows of d_sino [height][n_angles][width]."""
         n = d_proj.shape[0] if n is None else n
         _check(self._lib.xct_reslice(self.handle, first_angle, n, _ptr(d_proj), _ptr(d_sino), _stream(stream)))
+
+    def set_wait_limit(self, sm_clocks):
+        """Diagnostics: limit of the staged kernel's waits for its tile copies (SM clocks); a
+        negative value makes every wait give up at once (global-memory fallback)."""
+        _check(self._lib.xct_reslice_plan_set_wait_limit(self.handle, int(sm_clocks)))
 
     def close(self):
         """Destroys the plan; raises XCTError (XCT_E_TIMEOUT) if a staged-window copy of any

@@ -276,6 +276,12 @@ int xct_reslice_plan_create(xct_ctx *ctx, int width, int height, int n_angles, c
                             const float *yshift, float baseup, int correction, xct_reslice_plan **out);
 int xct_reslice(xct_reslice_plan *plan, int first_angle, int n, const float *d_proj, float *d_sino, void *stream);
 int xct_reslice_plan_destroy(xct_reslice_plan *plan);
+/* Diagnostics (no counterpart in the reference): the limit, in SM clocks, of the staged
+ * kernel's waits for its tile copies (default 2^31, about a second).  A negative limit makes
+ * every such wait give up at once, so a test can run the global-memory fallback and the
+ * XCT_E_TIMEOUT report of xct_reslice_plan_destroy without stalling anything; the copies
+ * already issued are still waited for, with the default limit, before the kernel ends. */
+int xct_reslice_plan_set_wait_limit(xct_reslice_plan *plan, long long sm_clocks);
 int xct_denoise_sinogram(int width, int n_angles, int n_rows, float threshold, const float *d_src, float *d_dst,
                          void *stream);
 

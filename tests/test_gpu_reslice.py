@@ -136,3 +136,34 @@ def test_reslice_staged_windows_bit_exact(gpu_ctx, oracle_lib):
         torch.cuda.synchronize()
         np.testing.assert_array_equal(d_s.cpu().numpy(), want)
         rp.close()  # raises if a staged copy missed its wait limit
+
+
+def test_reslice_staged_wait_limit_fallback(gpu_ctx, oracle_lib):
+    """Waits that give up: with a negative limit every CTA of the staged kernel abandons its
+    copies at the first tile (nothing stalls; the copies in flight still land before the
+    kernel ends), computes every tile from global memory -- still bit-exact -- and the plan
+    reports XCT_E_TIMEOUT when destroyed.  The context stays usable afterwards."""
+    import xct
+    O = oracle_lib
+    rng = np.random.default_rng(12)
+    A, H, W = 20, 40, 260
+    mt = rng.uniform(0, 2, (A, H, W)).astype(np.float32)
+    xs = rng.uniform(-3, 3, A).astype(np.float32)
+    ys = rng.uniform(-2, 2, A).astype(np.float32)
+    want = O.reslice(mt, xs, ys, 0.25, 1)
+    d_mt = torch.from_numpy(mt).cuda()
+    rp = xct.ReslicePlan(gpu_ctx, W, H, A, xs, ys, 0.25, 1)
+    rp.set_wait_limit(-1)
+    d_s = torch.full((H, A, W), -3.0, device="cuda")
+    rp.reslice(d_mt, d_s)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(d_s.cpu().numpy(), want)
+    with pytest.raises(xct.XCTError) as e:
+        rp.close()
+    assert e.value.code == xct.XCT_E_TIMEOUT and "wait limit" in str(e.value)
+    rp2 = xct.ReslicePlan(gpu_ctx, W, H, A, xs, ys, 0.25, 1)
+    d_s.fill_(-3.0)
+    rp2.reslice(d_mt, d_s)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(d_s.cpu().numpy(), want)
+    rp2.close()
