@@ -194,8 +194,22 @@ struct FbpShared {
     float win[kFbpChunk * kFbpW];
     float2 scs[kFbpChunk];
     int slo[kFbpChunk];
+    unsigned soff[kFbpChunk];  // shared address of angle k's entry for floor bits fb: soff[k] + 4*fb
     float red[kFbpThreads / 32];
 };
+
+__device__ __forceinline__ float fbp_lds(unsigned addr)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+__device__ __forceinline__ float fbp_lds_next(unsigned addr)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1+4];" : "=f"(v) : "r"(addr));
+    return v;
+}
 
 // Monotone integer key of a float (atomicMin on keys orders as the floats do).
 __device__ __forceinline__ int fkey(float f)
@@ -223,12 +237,13 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
     const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
     const int Y = Y0 + ty;
     const float Yc = (float)min(Y, Y1) - g.hy;
-    float xc[8], acc[8];
+    float xc[8];
+    f2x acc2[4];  // pixel pairs, accumulated with packed adds (each lane an IEEE add)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        xc[i] = (float)min(X0 + tx * 8 + i, X1) - g.hx;
-        acc[i] = 0.0f;
-    }
+    for (int i = 0; i < 8; ++i) xc[i] = (float)min(X0 + tx * 8 + i, X1) - g.hx;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc2[j] = f2_pack(0.0f, 0.0f);
+    const unsigned wbase = (unsigned)__cvta_generic_to_shared(sh.win);
     const f2x cxp = f2_pack(g.cx, g.cx), hp = f2_pack(0.5f, 0.5f), MM = f2_pack(12582912.0f, 12582912.0f);
     const f2x one2 = f2_pack(1.0f, 1.0f);
     for (int k0 = 0; k0 < g.pa; k0 += kFbpChunk) {
@@ -246,6 +261,8 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
             lo = min(lo, xct_floor_bits(xct_bin_coord(xa, cs.x, qb, g.cx) - 0.5f));
             lo = min(lo, xct_floor_bits(xct_bin_coord(xb, cs.x, qb, g.cx) - 0.5f));
             sh.slo[k] = lo - XCT_FLOOR_BIAS;
+            // entry for floor bits fb: k*W + fb - lo  (mod 2^32)
+            sh.soff[k] = wbase + 4u * (unsigned)(k * kFbpW) - 4u * (unsigned)lo;
         }
         __syncthreads();
         for (int i = threadIdx.x; i < kn * kFbpW; i += kFbpThreads) {
@@ -257,8 +274,7 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
         for (int k = 0; k < kn; ++k) {
             const float c = sh.scs[k].x;
             const float q = Yc * sh.scs[k].y;
-            // window entry of bin b: k*W + b - lo = (floor bits of b) + wb
-            const int wb = k * kFbpW - sh.slo[k] - XCT_FLOOR_BIAS;
+            const unsigned off = sh.soff[k];
 #pragma unroll
             for (int i = 0; i < 8; i += 2) {
                 // Xc*c - q in scalar (ptxas fuses a packed multiply feeding a packed subtract,
@@ -276,15 +292,20 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
                 float a0, a1, w0, w1;
                 f2_unpack(a2, a0, a1);
                 f2_unpack(w2, w0, w1);
-                e0 += wb;
-                e1 += wb;
-                acc[i] += w0 * sh.win[e0] + a0 * sh.win[e0 + 1];
-                acc[i + 1] += w1 * sh.win[e1] + a1 * sh.win[e1 + 1];
+                const unsigned ad0 = (unsigned)e0 * 4u + off, ad1 = (unsigned)e1 * 4u + off;
+                // products in scalar (a packed multiply feeding a packed add would be fused);
+                // their sum and the accumulation packed: acc += (w t0 + a t1) per lane
+                const float p00 = w0 * fbp_lds(ad0), p01 = a0 * fbp_lds_next(ad0);
+                const float p10 = w1 * fbp_lds(ad1), p11 = a1 * fbp_lds_next(ad1);
+                acc2[i / 2] = f2_add(acc2[i / 2], f2_add(f2_pack(p00, p10), f2_pack(p01, p11)));
             }
         }
     }
     const float two_pa = (float)g.pa * 2.0f;
     float vmin = INFINITY;
+    float acc[8];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) f2_unpack(acc2[j], acc[2 * j], acc[2 * j + 1]);
     if (Y <= Y1) {
         float *row = img + ((size_t)z * g.ny + Y) * g.nx;
 #pragma unroll
