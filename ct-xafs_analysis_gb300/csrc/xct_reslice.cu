@@ -439,22 +439,25 @@ __global__ void __launch_bounds__(kTmaThreads, 4) reslice_tma_kernel(const __gri
                                     kTmaWaitClocks);
 }
 
-// grid: (ceil(W/256), ceil(A/8), H) over sinograms [H][A][W]; a thread walks 8 angles of one
-// column with the three angle rows in registers; neighbours clamped to the edge.
+constexpr int kDenoiseRows = 16;  // angles a denoise thread walks
+
+// grid: (ceil(W/256), ceil(A/16), H) over sinograms [H][A][W]; a thread walks 16 angles of one
+// column with the angle rows in registers (18 loads for 16 outputs, all in flight at once);
+// neighbours clamped to the edge.
 __global__ void __launch_bounds__(256) denoise_kernel(const float *__restrict__ src, float *__restrict__ dst, int W,
                                                       int A, float thr)
 {
     const int X = blockIdx.x * blockDim.x + threadIdx.x;
-    const int t0 = blockIdx.y * kRowsPerThread, Y = blockIdx.z;
+    const int t0 = blockIdx.y * kDenoiseRows, Y = blockIdx.z;
     if (X >= W) return;
     const float *base = src + (size_t)Y * A * W + X;
-    // rows t0-1 .. t0+8 (clamped), all loads first
-    float f[kRowsPerThread + 2];
+    // rows t0-1 .. t0+16 (clamped), all loads first
+    float f[kDenoiseRows + 2];
 #pragma unroll
-    for (int r = 0; r < kRowsPerThread + 2; ++r) f[r] = __ldg(base + (size_t)min(max(t0 - 1 + r, 0), A - 1) * W);
+    for (int r = 0; r < kDenoiseRows + 2; ++r) f[r] = __ldg(base + (size_t)min(max(t0 - 1 + r, 0), A - 1) * W);
     float *out = dst + ((size_t)Y * A + t0) * W + X;
 #pragma unroll
-    for (int r = 0; r < kRowsPerThread; ++r) {
+    for (int r = 0; r < kDenoiseRows; ++r) {
         if (t0 + r < A) {
             const float f3 = f[r], f1 = f[r + 1], f2 = f[r + 2];
             const float d1 = f2 - f1, d2 = f1 - f3;
@@ -636,7 +639,7 @@ int xct_denoise_sinogram(int width, int n_angles, int n_rows, float threshold, c
     const char *s = (const char *)d_src, *d = (const char *)d_dst;
     if (s < d + bytes && d < s + bytes)
         return xct_fail(XCT_E_INVALID, "xct_denoise_sinogram: source and destination overlap");
-    dim3 grid((width + 255) / 256, (n_angles + kRowsPerThread - 1) / kRowsPerThread, n_rows);
+    dim3 grid((width + 255) / 256, (n_angles + kDenoiseRows - 1) / kDenoiseRows, n_rows);
     denoise_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_src, d_dst, width, n_angles, threshold);
     XCT_CUDA_TRY(cudaGetLastError());
     g_xct_launches.fetch_add(1);

@@ -100,6 +100,43 @@ def test_end_to_end_reconstruction_from_files(host_bin, oracle_lib, tmp_path):
 
 
 @pytest.mark.gpu
+def test_initial_image_from_file(host_bin, oracle_lib, tmp_path):
+    """g_fst = 1: every slice starts from the raw float32 image named by the initial-image
+    key (first_image, fileIO.cpp:55-68), here an absolute path."""
+    from xct import phantom as P
+    O = oracle_lib
+    n, px, pa, ss, it = 64, 72, 45, 5, 2
+    ang = P.uniform_angles(pa)
+    d1, d2 = tmp_path / "in", tmp_path / "out"
+    d1.mkdir()
+    with open(tmp_path / "angles.log", "w") as f:
+        for a in ang:
+            f.write("%.9g\n" % a)
+    meas = {}
+    for z in range(7, 10):
+        img = P.rasterize_ellipses(P.ellipse_params(n, 4, z, axes=(3, 16)), n, n)
+        meas[z] = P.noisy_log_sinogram(O.projection(img, ang, px), 1e5, z)
+        meas[z].astype(np.float32).tofile(d1 / ("s%04d.raw" % z))
+    x0 = np.random.default_rng(2).uniform(0.5, 1.5, (n, n)).astype(np.float32)
+    x0.tofile(tmp_path / "start.img")
+    keys = [("#初期画像の使用 1:Yes 2: No", "1"), ("#初期画像ファイル名", str(tmp_path / "start.img"))]
+    inp = tmp_path / "run.inp"
+    write_inp(inp, extra=keys, d1=str(d1), d2=str(d2), f3=str(tmp_path / "angles.log"), px=px, pa=pa, n=n, it=it,
+              ss=ss)
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for z in range(7, 10):
+        got = np.fromfile(d2 / ("rec_%04d.img" % z), np.float32).reshape(n, n)
+        ref = O.osem_run(x0, meas[z], ang, ss, it, order=O.ORDER_LITERAL)
+        rel = np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)
+        assert rel <= 1e-4, (z, rel)
+    # a missing initial image is an error, not a silent uniform start
+    os.remove(tmp_path / "start.img")
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode != 0 and "start.img" in (r.stdout + r.stderr)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("method", [7, 8])
 def test_fbp_and_hybrid_methods_from_files(host_bin, oracle_lib, tmp_path, method):
     """Methods 7 (FBP) and 8 (FBP + OS-EM hybrid) of GPU() (GPU.cpp:80-90) with the .inp's
