@@ -196,6 +196,17 @@ def _ptr(t):
     return t.data_ptr()
 
 
+def _need(t, count, what):
+    """A buffer handed to the library as a bare pointer must hold the elements the call
+    touches: the library cannot see sizes, and a short buffer would be read or written past
+    its end on the device."""
+    if t is None or isinstance(t, int):
+        return
+    have = t.numel() if hasattr(t, "numel") else int(np.asarray(t).size)
+    if have < count:
+        raise XCTError(XCT_E_INVALID, "%s holds %d elements; the call needs %d" % (what, have, count))
+
+
 def _stream(stream):
     if stream is None:
         try:
@@ -270,14 +281,8 @@ class OSEMPlan:
     def run(self, sinos, imgs, sub=None, it=-1):
         """OS-EM on host arrays: ``sinos`` dN float32 [pa][px], ``imgs`` dN float32
         [ny][nx] (initial images in, reconstructions written back in place)."""
-        dN = len(sinos)
-        fp = ctypes.POINTER(ctypes.c_float)
-        for a in list(sinos) + list(imgs):
-            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
-                raise XCTError(XCT_E_INVALID, "host arrays must be C-contiguous float32 numpy arrays")
-        s_arr = (fp * dN)(*[s.ctypes.data_as(fp) for s in sinos])
-        i_arr = (fp * dN)(*[i.ctypes.data_as(fp) for i in imgs])
-        _check(self._lib.xct_osem_run(self.handle, dN, s_arr, i_arr, self._sub(sub), it))
+        s_arr, i_arr = self._host_arrays(sinos, imgs)
+        _check(self._lib.xct_osem_run(self.handle, len(sinos), s_arr, i_arr, self._sub(sub), it))
         return imgs
 
     def _host_arrays(self, sinos, imgs):
@@ -285,6 +290,12 @@ class OSEMPlan:
         for a in list(sinos) + list(imgs):
             if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
                 raise XCTError(XCT_E_INVALID, "host arrays must be C-contiguous float32 numpy arrays")
+        if len(imgs) != len(sinos):
+            raise XCTError(XCT_E_INVALID, "as many images as sinograms are needed")
+        for a in sinos:
+            _need(a, self.pa * self.px, "host sinogram")
+        for a in imgs:
+            _need(a, self.ny * self.nx, "host image")
         dN = len(sinos)
         return (fp * dN)(*[s.ctypes.data_as(fp) for s in sinos]), (fp * dN)(*[i.ctypes.data_as(fp) for i in imgs])
 
@@ -302,6 +313,12 @@ class OSEMPlan:
             if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
                 raise XCTError(XCT_E_INVALID, "host arrays must be C-contiguous float32 numpy arrays")
             return a.ctypes.data_as(fp)
+        if len(imgs) != len(sinos):
+            raise XCTError(XCT_E_INVALID, "as many images as sinograms are needed")
+        for a in sinos:
+            _need(a, self.pa * self.px, "host sinogram")
+        for a in imgs:
+            _need(a, self.ny * self.nx, "host image")
         n = len(sinos)
         s_arr = (fp * n)(*[addr(a) for a in sinos])
         i_arr = (fp * n)(*[addr(a) for a in imgs])
@@ -343,63 +360,88 @@ class OSEMPlan:
     # ---- device tensors (asynchronous on the stream) ----------------------------------
     def run_device(self, d_sino, d_img, dN=None, sub=None, it=-1, stream=None):
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_osem_run_device(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
                                              _stream(stream)))
 
     def cs_run_device(self, d_sino, d_img, cs_lambda=1.0e-4, dN=None, sub=None, it=-1, stream=None):
         """Compressed-sensing OS-EM on device tensors [dN][pa][px] -> [dN][ny][nx] (in/out)."""
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_cs_osem_run_device(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
                                                 cs_lambda, _stream(stream)))
 
     def osem1(self, sub, d_img, d_sino, d_ratio, dN=None, stream=None):
         """OSEM1 (OSEM.cl:38-68) alone: ratio rows of subset ``sub`` into d_ratio."""
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_img, dN * self.ny * self.nx, "d_img")
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_ratio, dN * self.pa * self.px, "d_ratio")
         _check(self._lib.xct_osem1(self.handle, dN, sub, _ptr(d_img), _ptr(d_sino), _ptr(d_ratio),
                                    _stream(stream)))
 
     def osem2(self, sub, d_img, d_ratio, dN=None, stream=None):
         """OSEM2 (OSEM.cl:71-105) alone: backprojection of d_ratio + update of d_img."""
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_img, dN * self.ny * self.nx, "d_img")
+        _need(d_ratio, dN * self.pa * self.px, "d_ratio")
         _check(self._lib.xct_osem2(self.handle, dN, sub, _ptr(d_img), _ptr(d_ratio), _stream(stream)))
 
     def fwd(self, d_img, d_sino, dN=None, stream=None):
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_img, dN * self.ny * self.nx, "d_img")
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
         _check(self._lib.xct_fwd(self.handle, dN, _ptr(d_img), _ptr(d_sino), _stream(stream)))
 
     def bp_ref(self, d_sino, d_img, dN=None, stream=None):
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_bp_ref(self.handle, dN, _ptr(d_sino), _ptr(d_img), _stream(stream)))
 
     def adj(self, d_sino, d_img, dN=None, stream=None):
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_adj(self.handle, dN, _ptr(d_sino), _ptr(d_img), _stream(stream)))
 
     def fbp_filter(self, d_sino, d_fprj, zp=0, dN=None, stream=None):
         """Ramp-filtered sinograms (FBP.cl:34-160) into d_fprj."""
         dN = d_sino.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_fprj, dN * self.pa * self.px, "d_fprj")
         _check(self._lib.xct_fbp_filter(self.handle, dN, zp, _ptr(d_sino), _ptr(d_fprj), _stream(stream)))
 
     def fbp_backproject(self, d_fprj, d_img, dN=None, stream=None):
         """backProjectionFBP (FBP.cl:164-188) of filtered sinograms into d_img."""
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_fprj, dN * self.pa * self.px, "d_fprj")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_fbp_backproject(self.handle, dN, _ptr(d_fprj), _ptr(d_img), _stream(stream)))
 
     def fbp(self, d_sino, d_img, zp=0, dN=None, stream=None):
         """FBP_execution: (correction), filter, backprojection."""
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_fbp_run_device(self.handle, dN, zp, _ptr(d_sino), _ptr(d_img), _stream(stream)))
 
     def hybrid_cs(self, d_sino, d_img, zp=0, baseup_order=4, cs_lambda=1.0e-4, dN=None, sub=None, it=-1,
                   stream=None):
         """FBP + base-up + compressed-sensing OS-EM on device tensors."""
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_hybrid_cs_run_device(self.handle, dN, zp, baseup_order, _ptr(d_sino), _ptr(d_img),
                                                   self._sub(sub), it, cs_lambda, _stream(stream)))
 
     def hybrid(self, d_sino, d_img, zp=0, baseup_order=4, dN=None, sub=None, it=-1, stream=None):
         """FBP + base-up + OS-EM of hybrid_thread on device tensors."""
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_hybrid_run_device(self.handle, dN, zp, baseup_order, _ptr(d_sino), _ptr(d_img),
                                                self._sub(sub), it, _stream(stream)))
 
@@ -407,12 +449,16 @@ class OSEMPlan:
     def rot_center_shift(self, d_sino, d_shifted, start, step, n=None, stream=None):
         """rotCenterShift of one sinogram [pa][px] for shifts start + step*i -> [n][pa][px]."""
         n = d_shifted.shape[0] if n is None else n
+        _need(d_sino, self.pa * self.px, "d_sino")
+        _need(d_shifted, n * self.pa * self.px, "d_shifted")
         _check(self._lib.xct_rot_center_shift(self.handle, n, start, step, _ptr(d_sino), _ptr(d_shifted),
                                               _stream(stream)))
 
     def focus_index(self, d_imgs, d_findex, start, step, ang_ini, ang_fin, offset=0, n=None, stream=None):
         """setMask + imgFocusIndex of images [n][ny][nx] -> d_findex [n] (device)."""
         n = d_imgs.shape[0] if n is None else n
+        _need(d_imgs, n * self.ny * self.nx, "d_imgs")
+        _need(d_findex, n, "d_findex")
         _check(self._lib.xct_focus_index(self.handle, n, offset, start, step, ang_ini, ang_fin, _ptr(d_imgs),
                                          _ptr(d_findex), _stream(stream)))
 
@@ -421,6 +467,8 @@ class OSEMPlan:
         """The whole search; returns (focus indices [n] (numpy), index of the best shift).
         ang_ini/ang_fin default to the plan's first and last angle."""
         n = d_imgs.shape[0] if n is None else n
+        _need(d_sino, self.pa * self.px, "d_sino")
+        _need(d_imgs, n * self.ny * self.nx, "d_imgs")
         ang_ini = float(self.angles[0]) if ang_ini is None else ang_ini
         ang_fin = float(self.angles[-1]) if ang_fin is None else ang_fin
         fi = np.zeros(n, np.float32)
@@ -452,6 +500,8 @@ class OSEMPlan:
         """Run OS-EM with CUDA events around every launch; returns a dict of summed device
         milliseconds and launch counts per kernel kind (fwd, finalize, bp) and the total."""
         dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
         ms = (ctypes.c_float * 4)()
         n = (ctypes.c_longlong * 4)()
         _check(self._lib.xct_osem_profile(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
@@ -499,6 +549,11 @@ class BatchPlan:
 
     def run(self, sinos, imgs, stream=None):
         n = len(self.geoms)
+        if len(sinos) != n or len(imgs) != n:
+            raise XCTError(XCT_E_INVALID, "one sinogram and one image per item are needed")
+        for g, a, b in zip(self.geoms, sinos, imgs):
+            _need(a, g.pa * g.px, "item sinogram")
+            _need(b, g.ny * g.nx, "item image")
         s = (ctypes.c_void_p * n)(*[_ptr(t) for t in sinos])
         i = (ctypes.c_void_p * n)(*[_ptr(t) for t in imgs])
         _check(self._lib.xct_batch_run(self.handle, s, i, _stream(stream)))
@@ -538,6 +593,8 @@ class ReslicePlan:
     def reslice(self, d_proj, d_sino, first_angle=0, n=None, stream=None):
         """d_proj [n][height][width] (angles first_angle..) -> rows of d_sino [height][n_angles][width]."""
         n = d_proj.shape[0] if n is None else n
+        _need(d_proj, n * self.height * self.width, "d_proj")
+        _need(d_sino, self.height * self.n_angles * self.width, "d_sino")
         _check(self._lib.xct_reslice(self.handle, first_angle, n, _ptr(d_proj), _ptr(d_sino), _stream(stream)))
 
     def set_wait_limit(self, sm_clocks):
@@ -562,6 +619,7 @@ class ReslicePlan:
 def denoise_sinogram(d_src, d_dst, threshold, stream=None):
     """denoiseSinogram (Reslice/reslice.cl:223-248) on sinograms [rows][angles][width]."""
     rows, na, w = d_src.shape
+    _need(d_dst, rows * na * w, "d_dst")
     _check(load().xct_denoise_sinogram(w, na, rows, threshold, _ptr(d_src), _ptr(d_dst), _stream(stream)))
 
 

@@ -88,3 +88,39 @@ def test_osem1_ratio_matches_oracle(gpu_ctx, oracle_lib, shape, kernels):
             assert np.linalg.norm(g - w) / np.linalg.norm(w) <= 5e-6
             assert np.max(np.abs(g - w) / np.abs(w)) <= 1e-4
     plan.close()
+
+
+def test_short_buffers_are_rejected_before_launch(gpu_ctx):
+    """The library takes bare pointers; the Python mirror refuses buffers shorter than the
+    call touches (no kernel runs), and the plan works afterwards."""
+    import xct
+    nx, ny, px, pa = 40, 30, 48, 20
+    plan = xct.OSEMPlan(gpu_ctx, nx, ny, px, np.arange(pa, dtype=np.float32) * 9.0, 4, 1, max_batch=2)
+    sino = torch.rand((2, pa, px), device="cuda") + 0.1
+    img = torch.ones((2, ny, nx), device="cuda")
+    short_sino = torch.rand((2, pa - 1, px), device="cuda")
+    short_img = torch.ones((2, ny, nx - 1), device="cuda")
+    before = xct.launch_count()
+    for call in (lambda: plan.run_device(short_sino, img), lambda: plan.run_device(sino, short_img),
+                 lambda: plan.fwd(img, short_sino), lambda: plan.adj(short_sino, img),
+                 lambda: plan.fbp(sino, short_img), lambda: plan.hybrid(short_sino, img),
+                 lambda: plan.cs_run_device(sino, short_img),
+                 lambda: plan.rot_center_shift(sino[0], short_sino, -1.0, 1.0),
+                 lambda: plan.run([np.zeros(pa * px - 1, np.float32)], [np.zeros(ny * nx, np.float32)])):
+        with pytest.raises(xct.XCTError) as e:
+            call()
+        assert e.value.code == xct.XCT_E_INVALID and "elements" in str(e.value)
+    torch.cuda.synchronize()
+    assert xct.launch_count() == before
+    rp = xct.ReslicePlan(gpu_ctx, px, 6, pa)
+    with pytest.raises(xct.XCTError):
+        rp.reslice(torch.rand((pa, 6, px - 1), device="cuda"), torch.empty((6, pa, px), device="cuda"))
+    with pytest.raises(xct.XCTError):
+        rp.reslice(torch.rand((pa, 6, px), device="cuda"), torch.empty((6, pa - 1, px), device="cuda"))
+    rp.close()
+    with pytest.raises(xct.XCTError):
+        xct.denoise_sinogram(sino, torch.empty((2, pa, px - 1), device="cuda"), 0.1)
+    plan.run_device(sino, img)
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(img).all())
+    plan.close()
