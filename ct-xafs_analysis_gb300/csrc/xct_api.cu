@@ -12,7 +12,9 @@
 
 #include <algorithm>
 #include <functional>
+#include <mutex>
 #include <new>
+#include <string>
 
 #include "xct_internal.h"
 
@@ -335,6 +337,62 @@ static int osem_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, con
     return XCT_OK;
 }
 
+// ---- tracing: XCT_TRACE=<file> (or 1 for stderr) ------------------------------------
+// Every xct_osem_run_device / xct_osem_run call of a plan without a sinogram correction then
+// runs with CUDA events around each launch, synchronously, and appends one JSON line: the
+// shape, dN, iterations, the summed milliseconds and launch counts per kernel kind, and per
+// subset step [forward, finalize, backprojection] milliseconds in launch order.
+static std::mutex g_trace_mu;
+static FILE *trace_file()
+{
+    static FILE *f = nullptr;
+    static bool init = false;
+    std::lock_guard<std::mutex> lk(g_trace_mu);
+    if (!init) {
+        init = true;
+        const char *v = getenv("XCT_TRACE");
+        if (v && *v && strcmp(v, "0") != 0) {
+            if (strcmp(v, "1") == 0 || strcmp(v, "stderr") == 0) f = stderr;
+            else f = fopen(v, "a");
+        }
+    }
+    return f;
+}
+static int osem_loop_timed(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *so, int it,
+                           cudaStream_t st, float *ms, long long *launches, std::vector<float> *per_launch);
+// osem_loop, traced when XCT_TRACE is set
+static int osem_loop_maybe_traced(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *so, int it,
+                                  cudaStream_t st, const char *call)
+{
+    FILE *f = trace_file();
+    if (!f || p->g.correction_mode > 0) return osem_loop(p, dN, d_sino, d_img, so, it, st);
+    float ms[4];
+    long long n[4];
+    std::vector<float> per;
+    int rc = osem_loop_timed(p, dN, d_sino, d_img, so, it, st, ms, n, &per);
+    if (rc) return rc;
+    std::string line;
+    char b[512];
+    snprintf(b, sizeof b,
+             "{\"call\": \"%s\", \"device\": %d, \"nx\": %d, \"ny\": %d, \"px\": %d, \"pa\": %d, "
+             "\"ss\": %d, \"it\": %d, \"dN\": %d, \"kernels\": \"%s\", \"fwd_tile\": %d, \"ang_chunk\": %d, "
+             "\"ms\": {\"fwd\": %.4f, \"finalize\": %.4f, \"bp\": %.4f, \"total\": %.4f}, "
+             "\"launches\": %lld, \"slice_iters_per_s\": %.4f, \"subset_ms\": [",
+             call, p->ctx->device, p->g.nx, p->g.ny, p->g.px, p->g.pa, p->g.ss, it, dN,
+             p->g.kernels == XCT_KERNELS_TILED ? "tiled" : "plain", p->kg.fwd_T, p->kg.fwd_chunk, ms[0], ms[1], ms[2],
+             ms[3], n[3], ms[3] > 0.0f ? dN * it / (ms[3] * 1e-3) : 0.0);
+    line = b;
+    for (size_t j = 0; j + 2 < per.size(); j += 3) {
+        snprintf(b, sizeof b, "%s[%.4f, %.4f, %.4f]", j ? ", " : "", per[j], per[j + 1], per[j + 2]);
+        line += b;
+    }
+    line += "]}\n";
+    std::lock_guard<std::mutex> lk(g_trace_mu);
+    fputs(line.c_str(), f);
+    fflush(f);
+    return XCT_OK;
+}
+
 static int check_run(xct_plan *p, int dN, const int *sub, int it)
 {
     if (!p) return xct_fail(XCT_E_INVALID, "plan is null");
@@ -358,7 +416,8 @@ int xct_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, 
     if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_osem_run_device: null device pointer");
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
     cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
-    return osem_loop(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, st);
+    return osem_loop_maybe_traced(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, st,
+                                  "xct_osem_run_device");
 }
 
 int xct_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, const int *sub, int it)
@@ -380,7 +439,7 @@ int xct_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *cons
             cudaMemcpyAsync(p->d_img + i * nimg, img_host[i], sizeof(float) * nimg, cudaMemcpyHostToDevice, st));
     }
     XCT_CUDA_TRY(cudaEventRecord(p->ev0, st));
-    rc = osem_loop(p, dN, p->d_sino, p->d_img, sub ? sub : p->sub_default.data(), it, st);
+    rc = osem_loop_maybe_traced(p, dN, p->d_sino, p->d_img, sub ? sub : p->sub_default.data(), it, st, "xct_osem_run");
     if (rc) return rc;
     XCT_CUDA_TRY(cudaEventRecord(p->ev1, st));
     // device -> host (GPU.cpp:460-463)
@@ -455,29 +514,23 @@ int xct_adj(xct_plan *p, int dN, const float *d_sino, float *d_img, void *stream
     return launch_adj_tiled(p->kg, p->d_trig, d_sino, d_img, dN, (cudaStream_t)stream);
 }
 
-int xct_osem_profile(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, void *stream,
-                     float *ms, long long *launches)
+// OS-EM of the plan's tiled or plain kernels with a CUDA event pair around every launch
+// (forward, finalize, backprojection per subset); synchronous.  per_launch receives each
+// launch's milliseconds in launch order (the plain kernels' finalize slot stays 0).
+static int osem_loop_timed(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *so, int it,
+                           cudaStream_t st, float *ms, long long *launches, std::vector<float> *per_launch)
 {
-    if (p && it < 0) it = p->g.it;
-    int rc = check_run(p, dN, sub, it);
-    if (rc) return rc;
-    if (!d_sino || !d_img || !ms || !launches) return xct_fail(XCT_E_INVALID, "xct_osem_profile: null argument");
-    if (p->g.correction_mode > 0)
-        return xct_fail(XCT_E_UNSUPPORTED, "xct_osem_profile: plans with a sinogram correction are not profiled");
-    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
-    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
-    const int *so = sub ? sub : p->sub_default.data();
     const bool tiled = p->g.kernels == XCT_KERNELS_TILED;
     const int nk = 3;
-    std::vector<cudaEvent_t> ev;
     const int nlaunch = it * p->g.ss * nk;
-    ev.resize(2 * (size_t)nlaunch + 2);
+    std::vector<cudaEvent_t> ev(2 * (size_t)nlaunch + 2, nullptr);
     for (auto &e : ev)
-        if (cudaEventCreate(&e) != cudaSuccess) return xct_fail(XCT_E_CUDA, "xct_osem_profile: event create");
-    auto cleanup = [&]() {
-        for (auto &e : ev) cudaEventDestroy(e);
-    };
-    int q = 0;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            for (auto &f : ev)
+                if (f) cudaEventDestroy(f);
+            return xct_fail(XCT_E_CUDA, "osem timing: event create");
+        }
+    int rc = XCT_OK, q = 0;
     cudaEventRecord(ev[ev.size() - 2], st);
     for (int i = 0; i < it && rc == 0; ++i)
         for (int k = 0; k < p->g.ss && rc == 0; ++k) {
@@ -501,23 +554,39 @@ int xct_osem_profile(xct_plan *p, int dN, const float *d_sino, float *d_img, con
         }
     cudaEventRecord(ev[ev.size() - 1], st);
     cudaError_t e = cudaEventSynchronize(ev[ev.size() - 1]);
-    if (rc == 0 && e != cudaSuccess) rc = xct_cuda_fail(e, "xct_osem_profile: sync");
+    if (rc == 0 && e != cudaSuccess) rc = xct_cuda_fail(e, "osem timing: sync");
     if (rc == 0) {
         for (int kk = 0; kk < 4; ++kk) {
             ms[kk] = 0.0f;
             launches[kk] = 0;
         }
+        if (per_launch) per_launch->assign(q, 0.0f);
         for (int j = 0; j < q; ++j) {
             float t = 0.0f;
             cudaEventElapsedTime(&t, ev[2 * j], ev[2 * j + 1]);
             ms[j % nk] += t;
+            if (per_launch) (*per_launch)[j] = t;
             if (tiled || j % nk != 1) launches[j % nk] += 1;
         }
         cudaEventElapsedTime(&ms[3], ev[ev.size() - 2], ev[ev.size() - 1]);
         launches[3] = launches[0] + launches[1] + launches[2];
     }
-    cleanup();
+    for (auto &f : ev) cudaEventDestroy(f);
     return rc;
+}
+
+int xct_osem_profile(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, void *stream,
+                     float *ms, long long *launches)
+{
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!d_sino || !d_img || !ms || !launches) return xct_fail(XCT_E_INVALID, "xct_osem_profile: null argument");
+    if (p->g.correction_mode > 0)
+        return xct_fail(XCT_E_UNSUPPORTED, "xct_osem_profile: plans with a sinogram correction are not profiled");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    return osem_loop_timed(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, (cudaStream_t)stream, ms,
+                           launches, nullptr);
 }
 
 // ---------------------------------------------------------------------------- FBP

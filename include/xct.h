@@ -285,7 +285,13 @@ int xct_reslice_plan_set_wait_limit(xct_reslice_plan *plan, long long sm_clocks)
 int xct_denoise_sinogram(int width, int n_angles, int n_rows, float threshold, const float *d_src, float *d_dst,
                          void *stream);
 
-/* Tracing: xct_osem_run_device with CUDA events around every launch.  The reference
+/* Tracing by environment: with XCT_TRACE set to a file name (or 1 for stderr) when the
+ * library is first used, every xct_osem_run_device / xct_osem_run call of a plan without a
+ * sinogram correction runs with CUDA events around each launch, synchronously, and appends
+ * one JSON line: shape, dN, iterations, summed milliseconds and launch counts per kernel kind,
+ * and [forward, finalize, backprojection] milliseconds per subset step.
+ *
+ * Tracing by call: xct_osem_run_device with CUDA events around every launch.  The reference
  * enables CL_QUEUE_PROFILING_ENABLE but never reads the events
  * (share source/OCL_platform_device_class.cpp:175-178).  ms[0..3] = summed device time of
  * the forward-projection launches, of the ratio/finalize launches, of the
