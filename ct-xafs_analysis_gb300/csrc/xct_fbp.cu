@@ -28,6 +28,7 @@
 
 #include <algorithm>
 
+#include "xct_check.cuh"
 #include "xct_device.cuh"
 #include "xct_f32x2.cuh"
 #include "xct_internal.h"
@@ -271,6 +272,10 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
             sh.win[i] = ((unsigned)bin < (unsigned)g.px) ? __ldg(rt + (size_t)(k0 + k) * g.px + bin) : 0.0f;
         }
         __syncthreads();
+        // a pair's first entry may be any but the window's last (the pair reads the next one)
+        const unsigned wlo = wbase, whi = wbase + 4u * (unsigned)(kn * kFbpW - 2);
+        (void)wlo;
+        (void)whi;
         for (int k = 0; k < kn; ++k) {
             const float c = sh.scs[k].x;
             const float q = Yc * sh.scs[k].y;
@@ -295,8 +300,9 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
                 const unsigned ad0 = (unsigned)e0 * 4u + off, ad1 = (unsigned)e1 * 4u + off;
                 // products in scalar (a packed multiply feeding a packed add would be fused);
                 // their sum and the accumulation packed: acc += (w t0 + a t1) per lane
-                const float p00 = w0 * fbp_lds(ad0), p01 = a0 * fbp_lds_next(ad0);
-                const float p10 = w1 * fbp_lds(ad1), p11 = a1 * fbp_lds_next(ad1);
+                const bool in0 = XCT_IN(ad0, wlo, whi, XCT_SITE_FBP_WIN), in1 = XCT_IN(ad1, wlo, whi, XCT_SITE_FBP_WIN);
+                const float p00 = w0 * (in0 ? fbp_lds(ad0) : 0.0f), p01 = a0 * (in0 ? fbp_lds_next(ad0) : 0.0f);
+                const float p10 = w1 * (in1 ? fbp_lds(ad1) : 0.0f), p11 = a1 * (in1 ? fbp_lds_next(ad1) : 0.0f);
                 acc2[i / 2] = f2_add(acc2[i / 2], f2_add(f2_pack(p00, p10), f2_pack(p01, p11)));
             }
         }
@@ -435,3 +441,5 @@ int launch_base_up(const KGeom &g, float *img, int dN, int order, const int *min
     g_xct_launches.fetch_add(1);
     return XCT_OK;
 }
+
+XCT_CHECK_READER(xct_check_read_fbp)

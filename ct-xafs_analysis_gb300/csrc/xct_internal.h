@@ -165,3 +165,22 @@ int launch_focus_index(const float *imgs, int nx, int ny, int n, const float *d_
 // sinogramCorrection (reconstShare.cl:35-70), modes 1..4, src -> dst.
 int launch_sino_correction(const KGeom &g, const float *src, float *dst, const float *ang_fac, const float *bin_fac,
                            int mode, int dN, cudaStream_t st);
+
+// ---- bounds-checked build (xct_check.cuh) ------------------------------------------------
+struct XctCheckWord {
+    unsigned long long count;  // accesses skipped since the last reset
+    int site;                  // XCT_SITE_* of the first
+    int pad;
+    long long value, lo, hi;   // its index and the bounds it missed
+};
+enum {
+    XCT_SITE_FWD_TAP = 1,   // forward tile: footprint loads (byte address in the tile)
+    XCT_SITE_FWD_ACC = 2,   // forward tile: accumulator row and bin
+    XCT_SITE_ADJ = 3,       // adjoint tile: shared accumulator element
+    XCT_SITE_BP_WIN = 4,    // OS-EM backprojector: bin-window load (byte address)
+    XCT_SITE_FBP_WIN = 5,   // FBP backprojector: bin-window load pair (byte address)
+};
+#ifdef XCT_CHECKED
+int xct_check_read_tiled(XctCheckWord *out, bool reset);
+int xct_check_read_fbp(XctCheckWord *out, bool reset);
+#endif

@@ -59,3 +59,36 @@ extern "C" int xct_fp32_peak(int device, float *tflops)
     *tflops = best;
     return XCT_OK;
 }
+
+extern "C" int xct_check_report(xct_ctx *ctx, long long *count, int *site, long long *index, long long *lo,
+                                long long *hi)
+{
+    if (!ctx || !count) return xct_fail(XCT_E_INVALID, "xct_check_report: null argument");
+#ifdef XCT_CHECKED
+    XCT_CUDA_TRY(cudaSetDevice(ctx->device));
+    XCT_CUDA_TRY(cudaDeviceSynchronize());
+    int (*const readers[])(XctCheckWord *, bool) = {xct_check_read_tiled, xct_check_read_fbp};
+    long long total = 0;
+    XctCheckWord first = {};
+    for (auto rd : readers) {
+        XctCheckWord w = {};
+        if (rd(&w, true) != 0) return xct_fail(XCT_E_CUDA, "xct_check_report: reading a check word failed");
+        if (w.count != 0 && total == 0) first = w;
+        total += (long long)w.count;
+    }
+    *count = total;
+    if (site) *site = first.site;
+    if (index) *index = first.value;
+    if (lo) *lo = first.lo;
+    if (hi) *hi = first.hi;
+    return XCT_OK;
+#else
+    (void)site;
+    (void)index;
+    (void)lo;
+    (void)hi;
+    *count = -1;
+    return xct_fail(XCT_E_UNSUPPORTED, "xct_check_report: this library was built without bounds checks "
+                                       "(the checked build is libxct_checked.so)");
+#endif
+}

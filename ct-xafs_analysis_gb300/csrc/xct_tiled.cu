@@ -27,6 +27,7 @@
 //   * the multiplicative update is fused.
 #include <type_traits>
 
+#include "xct_check.cuh"
 #include "xct_device.cuh"
 #include "xct_f32x2.cuh"
 
@@ -140,9 +141,11 @@ __device__ __forceinline__ float lds_f1(unsigned addr)
 // ----------------------------------------------------------------- forward projector
 // One bilinear sample at Yc (both halves of yc2): coordinates (fma(Yc,s,ax), fma(Yc,c,ay)),
 // floor as a round-down add of 1.5*2^23 (the low mantissa bits), fraction = coordinate -
-// floor, the footprint as two 64-bit loads of (t, t[x+1] - t), three FMA lerps.
+// floor, the footprint as two 64-bit loads of (t, t[x+1] - t), three FMA lerps.  [alo, ahi]:
+// the byte addresses the first load may take (checked in the bounds-checked build only).
 template <int P>
-__device__ __forceinline__ float fwd_sample(f2x yc2, f2x sc, f2x axy, f2x MM, unsigned base2)
+__device__ __forceinline__ float fwd_sample(f2x yc2, f2x sc, f2x axy, f2x MM, unsigned base2, unsigned alo,
+                                            unsigned ahi)
 {
     const f2x xy = f2_fma(yc2, sc, axy);
     const f2x tb = f2_add_rd(xy, MM);
@@ -152,6 +155,7 @@ __device__ __forceinline__ float fwd_sample(f2x yc2, f2x sc, f2x axy, f2x MM, un
     float fx, fy;
     f2_unpack(fr, fx, fy);
     const unsigned addr = (unsigned)iyb * (unsigned)(P * 8) + (unsigned)ixb * 8u + base2;
+    if (!XCT_IN(addr, alo, ahi, XCT_SITE_FWD_TAP)) return 0.0f;
     float t00, d0, t01, d1;
     lds_f2(addr, t00, d0);
     lds_f2_next_row<P>(addr, t01, d1);
@@ -202,6 +206,8 @@ __device__ __forceinline__ void fwd_tile(const KGeom &g, const float *__restrict
     const unsigned base2 = sbase - (((bias + (unsigned)y0) * (unsigned)kFwdP + bias + (unsigned)x0) * 8u);
     const f2x MM = f2_pack(kMagic, kMagic);
     const f2x step2 = f2_pack((float)kLanesPerRay, (float)kLanesPerRay);
+    // a footprint's first element may be any but the last row's (the second load reads the row below)
+    const unsigned alo = sbase, ahi = sbase + (unsigned)((kFwdP * (kFwdRows - 1) - 1) * 8);
     const int ray = lane / kLanesPerRay;  // ray within the warp's 8
     const int ph = lane % kLanesPerRay;   // sample phase of this lane
     const int grp = lane & ~(kLanesPerRay - 1);
@@ -258,16 +264,18 @@ __device__ __forceinline__ void fwd_tile(const KGeom &g, const float *__restrict
             int i = 0;
             for (; i + 1 < n; i += 2) {
                 const f2x yb2 = f2_add(yc2, step2);
-                sum += fwd_sample<kFwdP>(yc2, sc, axy, MM, base2);
-                sum_b += fwd_sample<kFwdP>(yb2, sc, axy, MM, base2);
+                sum += fwd_sample<kFwdP>(yc2, sc, axy, MM, base2, alo, ahi);
+                sum_b += fwd_sample<kFwdP>(yb2, sc, axy, MM, base2, alo, ahi);
                 yc2 = f2_add(yb2, step2);
             }
-            if (i < n) sum += fwd_sample<kFwdP>(yc2, sc, axy, MM, base2);
+            if (i < n) sum += fwd_sample<kFwdP>(yc2, sc, axy, MM, base2, alo, ahi);
             sum += sum_b;
             // the ray's partial sum over this tile: the 4 phases, then one atomic
             sum += __shfl_xor_sync(0xffffffffu, sum, 1);
             sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-            if (ph == 0 && live && yb > ya) atomicAdd(acc + (size_t)(k0 + k) * g.px + X, (double)sum);
+            if (ph == 0 && live && yb > ya &&
+                XCT_IN((long long)(k0 + k) * g.px + X, 0, (long long)nrows * g.px - 1, XCT_SITE_FWD_ACC))
+                atomicAdd(acc + (size_t)(k0 + k) * g.px + X, (double)sum);
         }
     }
 }
@@ -349,6 +357,7 @@ __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__rest
                 const float fx = x - fi, fy = y - fj;
                 const int col = (int)fi - (x0 - 1), row = (int)fj - (y0 - 1);
                 const float gx = 1.0f - fx, gy = 1.0f - fy;
+                if (!XCT_IN(row * kAdjP + col, 0, kAdjP * kAdjP - kAdjP - 2, XCT_SITE_ADJ)) continue;
                 float *a = accs + row * kAdjP + col;
                 atomicAdd(a, gx * gy * v);
                 atomicAdd(a + 1, fx * gy * v);
@@ -453,6 +462,9 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
             win[i] = ((unsigned)bin < (unsigned)g.px) ? __ldg(rt + (size_t)th * g.px + bin) : 0.0f;
         }
         __syncthreads();
+        const unsigned wlo = wbase, whi = wbase + 4u * (unsigned)(kn * kBpW - 1);
+        (void)wlo;
+        (void)whi;
         for (int k = 0; k < kn; ++k) {
             const float c = scs[k].x;
             const float q = Yc * scs[k].y;
@@ -469,7 +481,10 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
                 const f2x t = f2_add_rd(f2_add(f2_add(f2_pack(da, db), cxp), hp), MM);
                 int b0, b1;
                 f2_unpack_bits(t, b0, b1);
-                acc2[j] = f2_add(acc2[j], f2_pack(lds_f1((unsigned)b0 * 4u + off), lds_f1((unsigned)b1 * 4u + off)));
+                const unsigned ad0 = (unsigned)b0 * 4u + off, ad1 = (unsigned)b1 * 4u + off;
+                const float v0 = XCT_IN(ad0, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad0) : 0.0f;
+                const float v1 = XCT_IN(ad1, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad1) : 0.0f;
+                acc2[j] = f2_add(acc2[j], f2_pack(v0, v1));
             }
         }
     }
@@ -758,3 +773,5 @@ int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;
 }
+
+XCT_CHECK_READER(xct_check_read_tiled)

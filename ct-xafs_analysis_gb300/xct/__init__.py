@@ -49,7 +49,7 @@ EXPORTS = (
     "xct_batch_plan_create", "xct_batch_run", "xct_batch_plan_destroy", "xct_osem_run_batched",
     "xct_fbp_filter", "xct_fbp_backproject", "xct_fbp_run_device", "xct_hybrid_run_device", "xct_fbp_run",
     "xct_hybrid_run", "xct_rot_center_shift", "xct_focus_index", "xct_rot_center_search",
-    "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_reslice_plan_set_wait_limit",
+    "xct_check_report", "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_reslice_plan_set_wait_limit",
     "xct_denoise_sinogram",
     "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
     "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume", "xct_hybrid_cs_run_device",
@@ -85,13 +85,18 @@ _lib = None
 
 
 def load():
-    """Load libxct.so (raises if it was not built: no CPU fallback exists)."""
+    """Load libxct.so (raises if it was not built: no CPU fallback exists).  With
+    XCT_LIB_VARIANT=checked the bounds-checked build libxct_checked.so is loaded instead
+    (xct.build.build_lib(checked=True) makes it; check_report reads what it found)."""
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB_PATH):
-        raise XCTError(XCT_E_UNSUPPORTED, "libxct.so not built (run __graft_entry__.build())")
-    L = ctypes.CDLL(LIB_PATH)
+    path = LIB_PATH
+    if os.environ.get("XCT_LIB_VARIANT", "") == "checked":
+        path = os.path.join(_HERE, "libxct_checked.so")
+    if not os.path.exists(path):
+        raise XCTError(XCT_E_UNSUPPORTED, "%s not built (run __graft_entry__.build())" % os.path.basename(path))
+    L = ctypes.CDLL(path)
     vp, ip, fp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)
     L.xct_ctx_create.argtypes = [ip, ctypes.POINTER(vp)]
     L.xct_ctx_destroy.argtypes = [vp]
@@ -146,6 +151,8 @@ def load():
     L.xct_batch_plan_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.xct_plan_sync.argtypes = [vp]
     L.xct_plan_last_ms.argtypes = [vp, fp]
+    L.xct_check_report.argtypes = [vp] + [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)] + \
+        [ctypes.POINTER(ctypes.c_longlong)] * 3
     L.xct_launch_count.restype = ctypes.c_longlong
     L.xct_last_error.restype = ctypes.c_char_p
     _lib = L
@@ -162,6 +169,16 @@ def subset_order(ss):
     out = (ctypes.c_int * ss)()
     _check(load().xct_subset_order(ss, out))
     return np.array(out[:], dtype=np.int32)
+
+
+def check_report(ctx):
+    """Bounds-checked build only: (skipped accesses since the last report, and the first one's
+    site code, index, lower and upper bound); resets the counts."""
+    n, site = ctypes.c_longlong(), ctypes.c_int()
+    v, lo, hi = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+    _check(load().xct_check_report(ctx.handle, ctypes.byref(n), ctypes.byref(site), ctypes.byref(v),
+                                   ctypes.byref(lo), ctypes.byref(hi)))
+    return n.value, site.value, v.value, lo.value, hi.value
 
 
 def launch_count():

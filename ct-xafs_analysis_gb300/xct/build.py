@@ -21,6 +21,7 @@ HOST = os.path.join(ROOT, "host")
 INCLUDE = os.path.join(REPO, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libxct.so")
+LIB_CHECKED = os.path.join(PKG, "libxct_checked.so")
 HOST_BIN = os.path.join(PKG, "xct_ct_reconstruction")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -49,14 +50,20 @@ def _sources():
     return cu, hdr
 
 
-def build_lib(force=False, verbose=False, extra=()):
+def build_lib(force=False, verbose=False, extra=(), checked=False):
+    """libxct.so; with checked, libxct_checked.so: the same sources with -DXCT_CHECKED (every
+    shared-memory access whose address follows from geometry is tested against its buffer,
+    see csrc/xct_check.cuh), in a build folder of its own."""
     cu, hdr = _sources()
-    os.makedirs(BUILD, exist_ok=True)
+    build_dir = BUILD + ("_checked" if checked else "")
+    lib = LIB_CHECKED if checked else LIB
+    extra = list(extra) + (["-DXCT_CHECKED"] if checked else [])
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = _nvcc()
     objs = []
     jobs = []
     for src in cu:
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if force or _newer(obj, [src] + hdr):
             jobs.append([nvcc] + NVFLAGS + list(extra) + ["-c", src, "-o", obj])
@@ -68,15 +75,15 @@ def build_lib(force=False, verbose=False, extra=()):
                 sys.stderr.write(r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
-    if force or jobs or _newer(LIB, objs):
-        tmp = LIB + ".tmp%d" % os.getpid()
+    if force or jobs or _newer(lib, objs):
+        tmp = lib + ".tmp%d" % os.getpid()
         cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed: " + " ".join(cmd))
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 def build_host(force=False):

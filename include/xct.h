@@ -285,6 +285,16 @@ int xct_reslice_plan_set_wait_limit(xct_reslice_plan *plan, long long sm_clocks)
 int xct_denoise_sinogram(int width, int n_angles, int n_rows, float threshold, const float *d_src, float *d_dst,
                          void *stream);
 
+/* Bounds-checked build (no counterpart in the reference; libxct_checked.so, the same sources
+ * compiled with -DXCT_CHECKED): every shared-memory access whose address follows from the
+ * geometry rather than from an index test -- the forward tile's footprint loads and
+ * accumulator rows, the adjoint's shared accumulator, the backprojectors' bin windows -- is
+ * tested against its buffer; one outside is skipped and recorded.  xct_check_report: on the
+ * context's device (synchronised first), the number of skipped accesses since the last
+ * report, and the first one's site code, index and bounds; resets.  The standard library
+ * returns XCT_E_UNSUPPORTED with *count = -1. */
+int xct_check_report(xct_ctx *ctx, long long *count, int *site, long long *index, long long *lo, long long *hi);
+
 /* Tracing by environment: with XCT_TRACE set to a file name (or 1 for stderr) when the
  * library is first used, every xct_osem_run_device / xct_osem_run call of a plan without a
  * sinogram correction runs with CUDA events around each launch, synchronously, and appends
