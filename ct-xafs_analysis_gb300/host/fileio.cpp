@@ -18,7 +18,13 @@ bool read_log(const std::string &path, int num, std::vector<float> &ang)
     ang.assign(num, 0.0f);
     for (int k = 0; k < num; ++k) {  // first token of each line, in degrees
         std::istringstream iss(ifs_getline(in));
-        iss >> ang[k];
+        if (!(iss >> ang[k])) {
+            // the reference keeps whatever the array held; an angle table shorter than the
+            // projection count is an error here
+            std::cerr << "angle file [" << path << "]: line " << k + 1 << " holds no angle; " << num
+                      << " projections need " << num << " angles." << std::endl;
+            return false;
+        }
     }
     return true;
 }

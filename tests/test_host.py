@@ -71,6 +71,31 @@ def test_device_list_syntax(host_bin, lst, n, want):
     assert out.stdout.strip() == want
 
 
+def test_input_failures_stop_before_any_reconstruction(host_bin, tmp_path):
+    """Missing input directory or first sinogram (main.cpp:76-108: exit 255), a missing angle
+    file, and an angle file shorter than the projection count stop the program with a
+    message before any device work."""
+    d1, d2 = tmp_path / "in", tmp_path / "out"
+    inp = tmp_path / "run.inp"
+    kw = dict(d1=str(d1), d2=str(d2), f3=str(tmp_path / "angles.log"), px=16, pa=10, n=16, it=1, ss=2)
+    write_inp(inp, **kw)
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 255 and "Directory not found" in r.stdout
+    d1.mkdir()
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 255 and "No raw file found" in r.stdout
+    for z in range(7, 10):
+        np.zeros(16 * 10, np.float32).tofile(d1 / ("s%04d.raw" % z))
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "angles.log" in r.stderr
+    with open(tmp_path / "angles.log", "w") as f:
+        for k in range(9):  # one short
+            f.write("%g\n" % (k * 18.0))
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "line 10 holds no angle" in r.stderr
+    assert not d2.exists()
+
+
 @pytest.mark.gpu
 def test_end_to_end_reconstruction_from_files(host_bin, oracle_lib, tmp_path):
     from xct import phantom as P
