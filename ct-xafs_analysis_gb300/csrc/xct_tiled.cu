@@ -18,12 +18,13 @@
 // and clears it for the next subset.
 //
 // Backprojector (OSEM2, OSEM.cl:71-105), footprint-staged:
-//   * one CTA owns a 64x32 pixel tile; per angle it stages the window of ratio bins its
+//   * one CTA owns a 64x64 pixel tile; per angle it stages the window of ratio bins its
 //     pixels hit (bin coordinates are monotone in X and in Y, so the tile corners bound the
 //     window exactly) into shared memory with coalesced loads;
-//   * each thread gathers 8 pixels per angle, in angle order, evaluating the reference's
-//     bin expression ((Xc*c - Yc*s) + cx) + 0.5 with packed f32x2 instructions (each lane
-//     rounds exactly like the scalar expression) and the nearest rule as a round-down add;
+//   * each thread gathers 8 pixels of two rows (32 apart) per angle, in angle order,
+//     evaluating the reference's bin expression ((Xc*c - Yc*s) + cx) + 0.5 -- the products
+//     Xc*c once for both rows, the rest with packed f32x2 instructions (each lane rounds
+//     exactly like the scalar expression) and the nearest rule as a round-down add;
 //   * the multiplicative update is fused.
 #include <stdint.h>
 
@@ -64,8 +65,9 @@ struct FwdTile {
 constexpr int kLanesPerRay = 4;
 constexpr int kRaysPerWarp = 32 / kLanesPerRay;
 
-constexpr int kBpTX = 64, kBpTY = 32;  // backprojection tile (pixels)
-constexpr int kBpW = 76;               // staged bins per angle (>= 63|c| + 31|s| + 3)
+constexpr int kBpTX = 64, kBpTY = 64;  // backprojection tile (pixels)
+constexpr int kBpW = 96;               // staged bins per angle (>= 63|c| + 63|s| + 3 = 92.1)
+constexpr int kBpChunk = 64;           // angles per staging pass of the backprojector
 
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 
@@ -425,10 +427,10 @@ __global__ void __launch_bounds__(256) fwd_finalize4_kernel(double *__restrict__
 
 // ------------------------------------------------------------------- backprojector
 struct BpShared {
-    float win[kAngChunk * kBpW];
-    float2 scs[kAngChunk];     // (c, s)
-    int slo[kAngChunk];        // first staged bin of the angle's window
-    unsigned soff[kAngChunk];  // byte address of window entry (bits - BIAS - lo)
+    float win[kBpChunk * kBpW];
+    float2 scs[kBpChunk];     // (c, s)
+    int slo[kBpChunk];        // first staged bin of the angle's window
+    unsigned soff[kBpChunk];  // byte address of window entry (bits - BIAS - lo)
 };
 
 // The work of one CTA: pixel tile (bx, by) of one slice (image img, ratio rt [pa][px]),
@@ -443,11 +445,12 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
     unsigned *soff = sh.soff;
     const int X0 = bx * kBpTX, Y0 = by * kBpTY;
     const int X1 = min(X0 + kBpTX, g.nx) - 1, Y1 = min(Y0 + kBpTY, g.ny) - 1;
-    const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;  // 8 threads x 8 pixels, 32 rows
-    const int Y = Y0 + ty;
+    // 8 threads x 8 pixels across, 32 threads down, each with rows ty and ty + 32
+    const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
+    const int Ya = Y0 + ty, Yb = Ya + kBpTY / 2;
     // threads past the image edge of a partial tile gather for the edge pixel (inside the
     // staged window) and write nothing
-    const float Yc = (float)min(Y, Y1) - g.hy;
+    const float Yca = (float)min(Ya, Y1) - g.hy, Ycb = (float)min(Yb, Y1) - g.hy;
     f2x xcp[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -455,16 +458,16 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
         const float b = (float)min(X0 + tx * 8 + 2 * j + 1, X1) - g.hx;
         xcp[j] = f2_pack(a, b);
     }
-    f2x acc2[4];  // pixel pairs, accumulated with packed adds (each lane an IEEE add)
+    f2x acca[4], accb[4];  // pixel pairs of the two rows, packed adds (each lane an IEEE add)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc2[j] = f2_pack(0.0f, 0.0f);
+    for (int j = 0; j < 4; ++j) acca[j] = accb[j] = f2_pack(0.0f, 0.0f);
     const f2x cxp = f2_pack(g.cx, g.cx);
     const f2x hp = f2_pack(0.5f, 0.5f);
     const f2x MM = f2_pack(kMagic, kMagic);
     const unsigned wbase = (unsigned)__cvta_generic_to_shared(win);
 
-    for (int k0 = 0; k0 < nang; k0 += kAngChunk) {
-        const int kn = min(kAngChunk, nang - k0);
+    for (int k0 = 0; k0 < nang; k0 += kBpChunk) {
+        const int kn = min(kBpChunk, nang - k0);
         __syncthreads();  // the previous chunk's gathers are done with the shared arrays
         for (int k = threadIdx.x; k < kn; k += kThreads) {
             const float2 cs = trig[sub + (k0 + k) * g.ss];
@@ -494,33 +497,43 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
         (void)wlo;
         (void)whi;
         for (int k = 0; k < kn; ++k) {
-            const float c = scs[k].x;
-            const float q = Yc * scs[k].y;
+            const float c = scs[k].x, s = scs[k].y;
+            const float qa = Yca * s, qb = Ycb * s;
             const unsigned off = soff[k];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 // Xc*c - q in scalar: ptxas contracts a packed multiply feeding a packed
                 // subtract into one fused operation whatever the rounding modifiers, and the
-                // reference rounds the product and the difference separately.  The three
-                // additions that follow are packed: ((.) + cx) + 0.5, then floor.
+                // reference rounds the product and the difference separately.  The products
+                // serve both rows; the three additions that follow are packed:
+                // ((.) + cx) + 0.5, then floor.
                 float xa, xb;
                 f2_unpack(xcp[j], xa, xb);
-                const float da = xa * c - q, db = xb * c - q;
-                const f2x t = f2_add_rd(f2_add(f2_add(f2_pack(da, db), cxp), hp), MM);
-                int b0, b1;
-                f2_unpack_bits(t, b0, b1);
-                const unsigned ad0 = (unsigned)b0 * 4u + off, ad1 = (unsigned)b1 * 4u + off;
-                const float v0 = XCT_IN(ad0, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad0) : 0.0f;
-                const float v1 = XCT_IN(ad1, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad1) : 0.0f;
-                acc2[j] = f2_add(acc2[j], f2_pack(v0, v1));
+                const float pa_ = xa * c, pb_ = xb * c;
+                const f2x ta = f2_add_rd(f2_add(f2_add(f2_pack(pa_ - qa, pb_ - qa), cxp), hp), MM);
+                const f2x tb = f2_add_rd(f2_add(f2_add(f2_pack(pa_ - qb, pb_ - qb), cxp), hp), MM);
+                int a0, a1, b0, b1;
+                f2_unpack_bits(ta, a0, a1);
+                f2_unpack_bits(tb, b0, b1);
+                const unsigned ad0 = (unsigned)a0 * 4u + off, ad1 = (unsigned)a1 * 4u + off;
+                const unsigned bd0 = (unsigned)b0 * 4u + off, bd1 = (unsigned)b1 * 4u + off;
+                const float va0 = XCT_IN(ad0, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad0) : 0.0f;
+                const float va1 = XCT_IN(ad1, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad1) : 0.0f;
+                const float vb0 = XCT_IN(bd0, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(bd0) : 0.0f;
+                const float vb1 = XCT_IN(bd1, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(bd1) : 0.0f;
+                acca[j] = f2_add(acca[j], f2_pack(va0, va1));
+                accb[j] = f2_add(accb[j], f2_pack(vb0, vb1));
             }
         }
     }
-    if (Y <= Y1) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int Y = r == 0 ? Ya : Yb;
+        if (Y > Y1) continue;
         float *row = img + (size_t)Y * g.nx;
         float acc[8];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) f2_unpack(acc2[j], acc[2 * j], acc[2 * j + 1]);
+        for (int j = 0; j < 4; ++j) f2_unpack(r == 0 ? acca[j] : accb[j], acc[2 * j], acc[2 * j + 1]);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int X = X0 + tx * 8 + i;
