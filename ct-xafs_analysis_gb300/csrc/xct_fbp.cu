@@ -35,7 +35,9 @@
 
 namespace {
 
-constexpr int kFbpTX = 64, kFbpTY = 32, kFbpThreads = 256, kFbpChunk = 128, kFbpW = 76;
+// backprojection: 64 x 64 pixel tiles (each thread 8 pixels of two rows 32 apart), windows of
+// kFbpW >= 63|c| + 63|s| + 4 bins staged kFbpChunk angles at a time
+constexpr int kFbpTX = 64, kFbpTY = 64, kFbpThreads = 256, kFbpChunk = 64, kFbpW = 96;
 
 // ------------------------------------------------------------------ ramp filter (FFT)
 __device__ __forceinline__ int fpad(int i) { return i + (i >> 4); }  // 16-entry rows + 1
@@ -236,14 +238,14 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
     const int X0 = bx * kFbpTX, Y0 = by * kFbpTY;
     const int X1 = min(X0 + kFbpTX, g.nx) - 1, Y1 = min(Y0 + kFbpTY, g.ny) - 1;
     const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
-    const int Y = Y0 + ty;
-    const float Yc = (float)min(Y, Y1) - g.hy;
+    const int Ya = Y0 + ty, Yb = Ya + kFbpTY / 2;
+    const float Yca = (float)min(Ya, Y1) - g.hy, Ycb = (float)min(Yb, Y1) - g.hy;
     float xc[8];
-    f2x acc2[4];  // pixel pairs, accumulated with packed adds (each lane an IEEE add)
+    f2x acca[4], accb[4];  // pixel pairs of the two rows, packed adds (each lane an IEEE add)
 #pragma unroll
     for (int i = 0; i < 8; ++i) xc[i] = (float)min(X0 + tx * 8 + i, X1) - g.hx;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc2[j] = f2_pack(0.0f, 0.0f);
+    for (int j = 0; j < 4; ++j) acca[j] = accb[j] = f2_pack(0.0f, 0.0f);
     const unsigned wbase = (unsigned)__cvta_generic_to_shared(sh.win);
     const f2x cxp = f2_pack(g.cx, g.cx), hp = f2_pack(0.5f, 0.5f), MM = f2_pack(12582912.0f, 12582912.0f);
     const f2x one2 = f2_pack(1.0f, 1.0f);
@@ -277,17 +279,17 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
         (void)wlo;
         (void)whi;
         for (int k = 0; k < kn; ++k) {
-            const float c = sh.scs[k].x;
-            const float q = Yc * sh.scs[k].y;
+            const float c = sh.scs[k].x, s = sh.scs[k].y;
+            const float qa = Yca * s, qb = Ycb * s;
             const unsigned off = sh.soff[k];
-#pragma unroll
-            for (int i = 0; i < 8; i += 2) {
-                // Xc*c - q in scalar (ptxas fuses a packed multiply feeding a packed subtract,
-                // and the reference rounds them separately); the additions, the round-down
-                // floor and the fraction packed over the pixel pair, each lane rounding as the
-                // scalar expression: uu = (((Xc*c - q) + cx) + 0.5) - 0.5, fi = floor(uu),
-                // a = uu - fi, then (1 - a) t[i] + a t[i+1]
-                const f2x d = f2_pack(xc[i] * c - q, xc[i + 1] * c - q);
+            // one row's pixel pair from the shared products Xc*c: the additions, the
+            // round-down floor and the fraction packed over the pair, each lane rounding as
+            // the scalar expression uu = (((Xc*c - q) + cx) + 0.5) - 0.5, fi = floor(uu),
+            // a = uu - fi; then acc += (1 - a) t[fi] + a t[fi+1] with the products in scalar
+            // (ptxas fuses a packed multiply feeding a packed add or subtract, and the
+            // reference rounds each operation)
+            auto pair = [&](float p0, float p1, float q, f2x &acc) {
+                const f2x d = f2_pack(p0 - q, p1 - q);
                 const f2x uu = f2_sub(f2_add(f2_add(d, cxp), hp), hp);
                 const f2x tb = f2_add_rd(uu, MM);
                 const f2x a2 = f2_sub(uu, f2_sub(tb, MM));
@@ -298,28 +300,36 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
                 f2_unpack(a2, a0, a1);
                 f2_unpack(w2, w0, w1);
                 const unsigned ad0 = (unsigned)e0 * 4u + off, ad1 = (unsigned)e1 * 4u + off;
-                // products in scalar (a packed multiply feeding a packed add would be fused);
-                // their sum and the accumulation packed: acc += (w t0 + a t1) per lane
                 const bool in0 = XCT_IN(ad0, wlo, whi, XCT_SITE_FBP_WIN), in1 = XCT_IN(ad1, wlo, whi, XCT_SITE_FBP_WIN);
                 const float p00 = w0 * (in0 ? fbp_lds(ad0) : 0.0f), p01 = a0 * (in0 ? fbp_lds_next(ad0) : 0.0f);
                 const float p10 = w1 * (in1 ? fbp_lds(ad1) : 0.0f), p11 = a1 * (in1 ? fbp_lds_next(ad1) : 0.0f);
-                acc2[i / 2] = f2_add(acc2[i / 2], f2_add(f2_pack(p00, p10), f2_pack(p01, p11)));
+                acc = f2_add(acc, f2_add(f2_pack(p00, p10), f2_pack(p01, p11)));
+            };
+#pragma unroll
+            for (int i = 0; i < 8; i += 2) {
+                const float p0 = xc[i] * c, p1 = xc[i + 1] * c;
+                pair(p0, p1, qa, acca[i / 2]);
+                pair(p0, p1, qb, accb[i / 2]);
             }
         }
     }
     const float two_pa = (float)g.pa * 2.0f;
     float vmin = INFINITY;
-    float acc[8];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) f2_unpack(acc2[j], acc[2 * j], acc[2 * j + 1]);
-    if (Y <= Y1) {
+    for (int r = 0; r < 2; ++r) {
+        const int Y = r == 0 ? Ya : Yb;
+        const float Yc = r == 0 ? Yca : Ycb;
+        if (Y > Y1) continue;
+        float acc[8];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) f2_unpack(r == 0 ? acca[j] : accb[j], acc[2 * j], acc[2 * j + 1]);
         float *row = img + ((size_t)z * g.ny + Y) * g.nx;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int X = X0 + tx * 8 + i;
             if (X <= X1) {
-                const float r = sqrtf(xc[i] * xc[i] + Yc * Yc);
-                const float v = (r < g.hx) ? __fdiv_rn(acc[i], two_pa) : 0.0f;
+                const float rr = sqrtf(xc[i] * xc[i] + Yc * Yc);
+                const float v = (rr < g.hx) ? __fdiv_rn(acc[i], two_pa) : 0.0f;
                 row[X] = v;
                 vmin = fminf(vmin, v);
             }
