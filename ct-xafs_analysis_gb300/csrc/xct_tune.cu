@@ -132,13 +132,23 @@ TuneChoice xct_tune_default(int sm_count, const std::function<long long(int, int
 }
 
 // Candidates worth timing: every tile side; chunks down to 16, dropping those that exceed
-// the largest subset by more than a factor of two (they launch the same CTAs as a smaller one).
+// the largest subset by more than a factor of two (they launch the same CTAs as a smaller one),
+// plus the even splits of the largest subset, ceil(rows / m) for m <= 6 (a 100-angle subset in
+// 2, 3, 4 ... equal chunks: finer steps in the grid's size, so that its last wave of resident
+// CTAs can be fuller, at the cost of staging each tile once per chunk).
 std::vector<TuneChoice> xct_tune_candidates(int max_rows)
 {
+    std::vector<int> chunks;
+    for (int c : kChunks)
+        if (c == 16 || c < 2 * max_rows) chunks.push_back(c);
+    for (int m = 1; m <= 6; ++m) {
+        const int c = (max_rows + m - 1) / m;
+        if (c >= 1 && c <= fwd_tiled_rows_cap() && std::find(chunks.begin(), chunks.end(), c) == chunks.end())
+            chunks.push_back(c);
+    }
     std::vector<TuneChoice> v;
     for (int T : kTiles)
-        for (int c : kChunks)
-            if (c == 16 || c < 2 * max_rows) v.push_back(TuneChoice{T, c, 0.0f});
+        for (int c : chunks) v.push_back(TuneChoice{T, c, 0.0f});
     return v;
 }
 
