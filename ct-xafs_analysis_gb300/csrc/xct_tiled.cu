@@ -21,9 +21,9 @@
 //   * one CTA owns a 64x64 pixel tile; per angle it stages the window of ratio bins its
 //     pixels hit (bin coordinates are monotone in X and in Y, so the tile corners bound the
 //     window exactly) into shared memory with coalesced loads;
-//   * each thread gathers 8 pixels of two rows (32 apart) per angle, in angle order,
+//   * each of 128 threads gathers 8 pixels of four rows (16 apart) per angle, in angle order,
 //     evaluating the reference's bin expression ((Xc*c - Yc*s) + cx) + 0.5 -- the products
-//     Xc*c once for both rows, the rest with packed f32x2 instructions (each lane rounds
+//     Xc*c once for the four rows, the rest with packed f32x2 instructions (each lane rounds
 //     exactly like the scalar expression) and the nearest rule as a round-down add;
 //   * the multiplicative update is fused.
 #include <stdint.h>
@@ -66,6 +66,8 @@ constexpr int kLanesPerRay = 4;
 constexpr int kRaysPerWarp = 32 / kLanesPerRay;
 
 constexpr int kBpTX = 64, kBpTY = 64;  // backprojection tile (pixels)
+constexpr int kBpRows = 4;                              // rows per thread (kBpTY / kBpRows apart)
+constexpr int kBpThreads = (kBpTX / 8) * (kBpTY / kBpRows);  // 8 pixels of kBpRows rows each
 constexpr int kBpW = 96;               // staged bins per angle (>= 63|c| + 63|s| + 3 = 92.1)
 constexpr int kBpChunk = 64;           // angles per staging pass of the backprojector
 
@@ -445,12 +447,14 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
     unsigned *soff = sh.soff;
     const int X0 = bx * kBpTX, Y0 = by * kBpTY;
     const int X1 = min(X0 + kBpTX, g.nx) - 1, Y1 = min(Y0 + kBpTY, g.ny) - 1;
-    // 8 threads x 8 pixels across, 32 threads down, each with rows ty and ty + 32
+    // 8 threads x 8 pixels across; thread row ty covers rows ty + r * (kBpTY / kBpRows)
+    constexpr int kStride = kBpTY / kBpRows;
     const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
-    const int Ya = Y0 + ty, Yb = Ya + kBpTY / 2;
     // threads past the image edge of a partial tile gather for the edge pixel (inside the
     // staged window) and write nothing
-    const float Yca = (float)min(Ya, Y1) - g.hy, Ycb = (float)min(Yb, Y1) - g.hy;
+    float Ycr[kBpRows];
+#pragma unroll
+    for (int r = 0; r < kBpRows; ++r) Ycr[r] = (float)min(Y0 + ty + r * kStride, Y1) - g.hy;
     f2x xcp[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -458,9 +462,11 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
         const float b = (float)min(X0 + tx * 8 + 2 * j + 1, X1) - g.hx;
         xcp[j] = f2_pack(a, b);
     }
-    f2x acca[4], accb[4];  // pixel pairs of the two rows, packed adds (each lane an IEEE add)
+    f2x acc[kBpRows][4];  // pixel pairs of each row, packed adds (each lane an IEEE add)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acca[j] = accb[j] = f2_pack(0.0f, 0.0f);
+    for (int r = 0; r < kBpRows; ++r)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[r][j] = f2_pack(0.0f, 0.0f);
     const f2x cxp = f2_pack(g.cx, g.cx);
     const f2x hp = f2_pack(0.5f, 0.5f);
     const f2x MM = f2_pack(kMagic, kMagic);
@@ -469,7 +475,7 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
     for (int k0 = 0; k0 < nang; k0 += kBpChunk) {
         const int kn = min(kBpChunk, nang - k0);
         __syncthreads();  // the previous chunk's gathers are done with the shared arrays
-        for (int k = threadIdx.x; k < kn; k += kThreads) {
+        for (int k = threadIdx.x; k < kn; k += kBpThreads) {
             const float2 cs = trig[sub + (k0 + k) * g.ss];
             scs[k] = cs;
             // the bin coordinate is monotone in X and in Y: the corners bound the window
@@ -486,7 +492,7 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
         }
         __syncthreads();
         // element j of angle k holds ratio[th][lo_k + j] (0 off the detector)
-        for (int i = threadIdx.x; i < kn * kBpW; i += kThreads) {
+        for (int i = threadIdx.x; i < kn * kBpW; i += kBpThreads) {
             const int k = i / kBpW, j = i - k * kBpW;
             const int bin = slo[k] + j;
             const int th = sub + (k0 + k) * g.ss;
@@ -498,53 +504,52 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
         (void)whi;
         for (int k = 0; k < kn; ++k) {
             const float c = scs[k].x, s = scs[k].y;
-            const float qa = Yca * s, qb = Ycb * s;
             const unsigned off = soff[k];
+            float q[kBpRows];
+#pragma unroll
+            for (int r = 0; r < kBpRows; ++r) q[r] = Ycr[r] * s;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 // Xc*c - q in scalar: ptxas contracts a packed multiply feeding a packed
                 // subtract into one fused operation whatever the rounding modifiers, and the
                 // reference rounds the product and the difference separately.  The products
-                // serve both rows; the three additions that follow are packed:
+                // serve every row; the three additions that follow are packed:
                 // ((.) + cx) + 0.5, then floor.
                 float xa, xb;
                 f2_unpack(xcp[j], xa, xb);
                 const float pa_ = xa * c, pb_ = xb * c;
-                const f2x ta = f2_add_rd(f2_add(f2_add(f2_pack(pa_ - qa, pb_ - qa), cxp), hp), MM);
-                const f2x tb = f2_add_rd(f2_add(f2_add(f2_pack(pa_ - qb, pb_ - qb), cxp), hp), MM);
-                int a0, a1, b0, b1;
-                f2_unpack_bits(ta, a0, a1);
-                f2_unpack_bits(tb, b0, b1);
-                const unsigned ad0 = (unsigned)a0 * 4u + off, ad1 = (unsigned)a1 * 4u + off;
-                const unsigned bd0 = (unsigned)b0 * 4u + off, bd1 = (unsigned)b1 * 4u + off;
-                const float va0 = XCT_IN(ad0, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad0) : 0.0f;
-                const float va1 = XCT_IN(ad1, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad1) : 0.0f;
-                const float vb0 = XCT_IN(bd0, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(bd0) : 0.0f;
-                const float vb1 = XCT_IN(bd1, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(bd1) : 0.0f;
-                acca[j] = f2_add(acca[j], f2_pack(va0, va1));
-                accb[j] = f2_add(accb[j], f2_pack(vb0, vb1));
+#pragma unroll
+                for (int r = 0; r < kBpRows; ++r) {
+                    const f2x t = f2_add_rd(f2_add(f2_add(f2_pack(pa_ - q[r], pb_ - q[r]), cxp), hp), MM);
+                    int b0, b1;
+                    f2_unpack_bits(t, b0, b1);
+                    const unsigned ad0 = (unsigned)b0 * 4u + off, ad1 = (unsigned)b1 * 4u + off;
+                    const float v0 = XCT_IN(ad0, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad0) : 0.0f;
+                    const float v1 = XCT_IN(ad1, wlo, whi, XCT_SITE_BP_WIN) ? lds_f1(ad1) : 0.0f;
+                    acc[r][j] = f2_add(acc[r][j], f2_pack(v0, v1));
+                }
             }
         }
     }
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int Y = r == 0 ? Ya : Yb;
+    for (int r = 0; r < kBpRows; ++r) {
+        const int Y = Y0 + ty + r * kStride;
         if (Y > Y1) continue;
         float *row = img + (size_t)Y * g.nx;
-        float acc[8];
+        float v[8];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) f2_unpack(r == 0 ? acca[j] : accb[j], acc[2 * j], acc[2 * j + 1]);
+        for (int j = 0; j < 4; ++j) f2_unpack(acc[r][j], v[2 * j], v[2 * j + 1]);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int X = X0 + tx * 8 + i;
-            if (X <= X1) row[X] = xct_update(row[X], acc[i], ssf, paf);
+            if (X <= X1) row[X] = xct_update(row[X], v[i], ssf, paf);
         }
     }
     __syncthreads();  // the shared arrays may be restaged by the caller's next tile
 }
 
 // grid: (ntx*nty tiles, 1, dN).
-__global__ void __launch_bounds__(kThreads) bp_tiled_kernel(float *__restrict__ img,
+__global__ void __launch_bounds__(kBpThreads) bp_tiled_kernel(float *__restrict__ img,
                                                             const float *__restrict__ ratio,
                                                             const float2 *__restrict__ trig, KGeom g, int sub,
                                                             int nang, int ntx, float ssf, float paf)
@@ -636,7 +641,7 @@ __global__ void fwd_finalize_batched_kernel(const XctItemDev *__restrict__ items
     }
 }
 
-__global__ void __launch_bounds__(kThreads) bp_batched_kernel(const XctItemDev *__restrict__ items,
+__global__ void __launch_bounds__(kBpThreads) bp_batched_kernel(const XctItemDev *__restrict__ items,
                                                               const int *__restrict__ base, int n, int sub,
                                                               int *queue)
 {
@@ -713,7 +718,7 @@ int xct_batched_grids(int device, int sm_count, int fwd_T, int grids[3])
     });
     if (rc) return rc;
     XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fwd_finalize_batched_kernel, 256, 0));
-    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, bp_batched_kernel, kThreads, 0));
+    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, bp_batched_kernel, kBpThreads, 0));
     grids[0] = sm_count * (a > 0 ? a : 1);
     grids[1] = sm_count * (b > 0 ? b : 1);
     grids[2] = sm_count * (c > 0 ? c : 1);
@@ -732,7 +737,7 @@ int launch_osem_step_batched(const XctItemDev *items, const int *bases /*[3][n+1
     if (rc) return rc;
     fwd_finalize_batched_kernel<<<grids[1], 256, 0, st>>>(items, bases + (n + 1), n, sub, queues + 1);
     XCT_CUDA_TRY(cudaGetLastError());
-    bp_batched_kernel<<<grids[2], kThreads, 0, st>>>(items, bases + 2 * (n + 1), n, sub, queues + 2);
+    bp_batched_kernel<<<grids[2], kBpThreads, 0, st>>>(items, bases + 2 * (n + 1), n, sub, queues + 2);
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;  // launches are counted when the captured graph is replayed
 }
@@ -816,7 +821,7 @@ int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const
     const int nang = (g.pa - sub + g.ss - 1) / g.ss;  // OSEM2's angle loop (OSEM.cl:93)
     const int ntx = (g.nx + kBpTX - 1) / kBpTX, nty = (g.ny + kBpTY - 1) / kBpTY;
     dim3 grid(ntx * nty, 1, dN);
-    bp_tiled_kernel<<<grid, kThreads, 0, st>>>(img, ratio, trig, g, sub, nang, ntx, (float)g.ss, (float)g.pa);
+    bp_tiled_kernel<<<grid, kBpThreads, 0, st>>>(img, ratio, trig, g, sub, nang, ntx, (float)g.ss, (float)g.pa);
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;
