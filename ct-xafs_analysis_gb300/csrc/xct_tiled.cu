@@ -66,8 +66,14 @@ constexpr int kLanesPerRay = 4;
 constexpr int kRaysPerWarp = 32 / kLanesPerRay;
 
 constexpr int kBpTX = 64, kBpTY = 64;  // backprojection tile (pixels)
-constexpr int kBpRows = 4;                              // rows per thread (kBpTY / kBpRows apart)
-constexpr int kBpThreads = (kBpTX / 8) * (kBpTY / kBpRows);  // 8 pixels of kBpRows rows each
+// A backprojector thread takes 8 pixels of R rows (kBpTY / R apart): R = 4 shares the
+// products Xc*c over four rows (128 threads, 80 registers); R = 2 (256 threads, 64 registers)
+// fills the SMs better when a launch has few tiles.
+template <int R>
+struct BpCfg {
+    static constexpr int Threads = (kBpTX / 8) * (kBpTY / R);
+    static constexpr int Stride = kBpTY / R;
+};
 constexpr int kBpW = 96;               // staged bins per angle (>= 63|c| + 63|s| + 3 = 92.1)
 constexpr int kBpChunk = 64;           // angles per staging pass of the backprojector
 
@@ -437,6 +443,7 @@ struct BpShared {
 
 // The work of one CTA: pixel tile (bx, by) of one slice (image img, ratio rt [pa][px]),
 // angles th = sub + k*ss for k < nang (as OSEM2 loops).  Starts/ends with threads in step.
+template <int kBpRows>
 __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img, const float *__restrict__ rt,
                                         const float2 *__restrict__ trig, int sub, int nang, int bx, int by,
                                         float ssf, float paf, BpShared &sh)
@@ -448,7 +455,7 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
     const int X0 = bx * kBpTX, Y0 = by * kBpTY;
     const int X1 = min(X0 + kBpTX, g.nx) - 1, Y1 = min(Y0 + kBpTY, g.ny) - 1;
     // 8 threads x 8 pixels across; thread row ty covers rows ty + r * (kBpTY / kBpRows)
-    constexpr int kStride = kBpTY / kBpRows;
+    constexpr int kStride = BpCfg<kBpRows>::Stride, kBpThreads = BpCfg<kBpRows>::Threads;
     const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
     // threads past the image edge of a partial tile gather for the edge pixel (inside the
     // staged window) and write nothing
@@ -549,14 +556,15 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
 }
 
 // grid: (ntx*nty tiles, 1, dN).
-__global__ void __launch_bounds__(kBpThreads) bp_tiled_kernel(float *__restrict__ img,
+template <int R>
+__global__ void __launch_bounds__(BpCfg<R>::Threads) bp_tiled_kernel(float *__restrict__ img,
                                                             const float *__restrict__ ratio,
                                                             const float2 *__restrict__ trig, KGeom g, int sub,
                                                             int nang, int ntx, float ssf, float paf)
 {
     __shared__ BpShared sh;
     const int z = blockIdx.z;
-    bp_tile(g, img + (size_t)z * g.nx * g.ny, ratio + (size_t)z * g.pa * g.px, trig, sub, nang,
+    bp_tile<R>(g, img + (size_t)z * g.nx * g.ny, ratio + (size_t)z * g.pa * g.px, trig, sub, nang,
             (int)blockIdx.x % ntx, (int)blockIdx.x / ntx, ssf, paf, sh);
 }
 
@@ -641,7 +649,7 @@ __global__ void fwd_finalize_batched_kernel(const XctItemDev *__restrict__ items
     }
 }
 
-__global__ void __launch_bounds__(kBpThreads) bp_batched_kernel(const XctItemDev *__restrict__ items,
+__global__ void __launch_bounds__(BpCfg<4>::Threads) bp_batched_kernel(const XctItemDev *__restrict__ items,
                                                               const int *__restrict__ base, int n, int sub,
                                                               int *queue)
 {
@@ -656,7 +664,7 @@ __global__ void __launch_bounds__(kBpThreads) bp_batched_kernel(const XctItemDev
         const KGeom &g = it.g;
         const int nang = (g.pa - sub + g.ss - 1) / g.ss;
         const int t = u - base[i];
-        bp_tile(g, it.img, it.ratio, it.trig, sub, nang, t % it.bp_ntx, t / it.bp_ntx, (float)g.ss, (float)g.pa,
+        bp_tile<4>(g, it.img, it.ratio, it.trig, sub, nang, t % it.bp_ntx, t / it.bp_ntx, (float)g.ss, (float)g.pa,
                 sh);
     }
 }
@@ -718,7 +726,7 @@ int xct_batched_grids(int device, int sm_count, int fwd_T, int grids[3])
     });
     if (rc) return rc;
     XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fwd_finalize_batched_kernel, 256, 0));
-    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, bp_batched_kernel, kBpThreads, 0));
+    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, bp_batched_kernel, BpCfg<4>::Threads, 0));
     grids[0] = sm_count * (a > 0 ? a : 1);
     grids[1] = sm_count * (b > 0 ? b : 1);
     grids[2] = sm_count * (c > 0 ? c : 1);
@@ -737,7 +745,7 @@ int launch_osem_step_batched(const XctItemDev *items, const int *bases /*[3][n+1
     if (rc) return rc;
     fwd_finalize_batched_kernel<<<grids[1], 256, 0, st>>>(items, bases + (n + 1), n, sub, queues + 1);
     XCT_CUDA_TRY(cudaGetLastError());
-    bp_batched_kernel<<<grids[2], kBpThreads, 0, st>>>(items, bases + 2 * (n + 1), n, sub, queues + 2);
+    bp_batched_kernel<<<grids[2], BpCfg<4>::Threads, 0, st>>>(items, bases + 2 * (n + 1), n, sub, queues + 2);
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;  // launches are counted when the captured graph is replayed
 }
@@ -814,6 +822,19 @@ int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, floa
     return XCT_OK;
 }
 
+// SM count of the current device (cached per device; a benign race fills the same value).
+static int device_sm_count()
+{
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (cache[dev] == 0) {
+        int n = 0;
+        cache[dev] = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0 ? n : 152;
+    }
+    return cache[dev];
+}
+
 int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const float *ratio, int dN, int sub,
                            cudaStream_t st)
 {
@@ -821,7 +842,13 @@ int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const
     const int nang = (g.pa - sub + g.ss - 1) / g.ss;  // OSEM2's angle loop (OSEM.cl:93)
     const int ntx = (g.nx + kBpTX - 1) / kBpTX, nty = (g.ny + kBpTY - 1) / kBpTY;
     dim3 grid(ntx * nty, 1, dN);
-    bp_tiled_kernel<<<grid, kBpThreads, 0, st>>>(img, ratio, trig, g, sub, nang, ntx, (float)g.ss, (float)g.pa);
+    // four rows per thread once the grid gives three waves of its resident CTAs (6 per SM)
+    if ((long long)ntx * nty * dN >= 3LL * 6 * device_sm_count())
+        bp_tiled_kernel<4><<<grid, BpCfg<4>::Threads, 0, st>>>(img, ratio, trig, g, sub, nang, ntx, (float)g.ss,
+                                                                (float)g.pa);
+    else
+        bp_tiled_kernel<2><<<grid, BpCfg<2>::Threads, 0, st>>>(img, ratio, trig, g, sub, nang, ntx, (float)g.ss,
+                                                                (float)g.pa);
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;
