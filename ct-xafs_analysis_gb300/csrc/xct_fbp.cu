@@ -227,10 +227,14 @@ __device__ __forceinline__ float fkey_decode(int k) { return __int_as_float(k >=
 // sampler at (u, th + 0.5): i = floor(u - 0.5), a = (u - 0.5) - i,
 // (1 - a) t[i] + a t[i+1], zero off the detector.  min_keys (optional): the per-slice
 // minimum of the written image, as keys.
-__global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__restrict__ fprj, float *__restrict__ img,
-                                                             const float2 *__restrict__ trig, KGeom g, int ntx,
-                                                             int *__restrict__ min_keys)
+// R rows per thread (kFbpTY / R apart, 512 / R threads): R = 4 shares the products Xc*c over
+// four rows; R = 2 fills the SMs better when a launch has few tiles.
+template <int R>
+__global__ void __launch_bounds__(512 / R) fbp_bp_kernel(const float *__restrict__ fprj, float *__restrict__ img,
+                                                         const float2 *__restrict__ trig, KGeom g, int ntx,
+                                                         int *__restrict__ min_keys)
 {
+    constexpr int kThr = 512 / R, kStride = kFbpTY / R;
     __shared__ FbpShared sh;
     const int z = blockIdx.z;
     const float *rt = fprj + (size_t)z * g.pa * g.px;
@@ -238,21 +242,24 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
     const int X0 = bx * kFbpTX, Y0 = by * kFbpTY;
     const int X1 = min(X0 + kFbpTX, g.nx) - 1, Y1 = min(Y0 + kFbpTY, g.ny) - 1;
     const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
-    const int Ya = Y0 + ty, Yb = Ya + kFbpTY / 2;
-    const float Yca = (float)min(Ya, Y1) - g.hy, Ycb = (float)min(Yb, Y1) - g.hy;
+    float Ycr[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) Ycr[r] = (float)min(Y0 + ty + r * kStride, Y1) - g.hy;
     float xc[8];
-    f2x acca[4], accb[4];  // pixel pairs of the two rows, packed adds (each lane an IEEE add)
+    f2x acc2[R][4];  // pixel pairs of each row, packed adds (each lane an IEEE add)
 #pragma unroll
     for (int i = 0; i < 8; ++i) xc[i] = (float)min(X0 + tx * 8 + i, X1) - g.hx;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acca[j] = accb[j] = f2_pack(0.0f, 0.0f);
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc2[r][j] = f2_pack(0.0f, 0.0f);
     const unsigned wbase = (unsigned)__cvta_generic_to_shared(sh.win);
     const f2x cxp = f2_pack(g.cx, g.cx), hp = f2_pack(0.5f, 0.5f), MM = f2_pack(12582912.0f, 12582912.0f);
     const f2x one2 = f2_pack(1.0f, 1.0f);
     for (int k0 = 0; k0 < g.pa; k0 += kFbpChunk) {
         const int kn = min(kFbpChunk, g.pa - k0);
         __syncthreads();
-        for (int k = threadIdx.x; k < kn; k += kFbpThreads) {
+        for (int k = threadIdx.x; k < kn; k += kThr) {
             const float2 cs = trig[k0 + k];
             sh.scs[k] = cs;
             // u is monotone in X and in Y (every step rounds monotonically): the corners
@@ -268,7 +275,7 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
             sh.soff[k] = wbase + 4u * (unsigned)(k * kFbpW) - 4u * (unsigned)lo;
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < kn * kFbpW; i += kFbpThreads) {
+        for (int i = threadIdx.x; i < kn * kFbpW; i += kThr) {
             const int k = i / kFbpW, j = i - k * kFbpW;
             const int bin = sh.slo[k] + j;
             sh.win[i] = ((unsigned)bin < (unsigned)g.px) ? __ldg(rt + (size_t)(k0 + k) * g.px + bin) : 0.0f;
@@ -280,16 +287,18 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
         (void)whi;
         for (int k = 0; k < kn; ++k) {
             const float c = sh.scs[k].x, s = sh.scs[k].y;
-            const float qa = Yca * s, qb = Ycb * s;
             const unsigned off = sh.soff[k];
+            float q[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) q[r] = Ycr[r] * s;
             // one row's pixel pair from the shared products Xc*c: the additions, the
             // round-down floor and the fraction packed over the pair, each lane rounding as
             // the scalar expression uu = (((Xc*c - q) + cx) + 0.5) - 0.5, fi = floor(uu),
             // a = uu - fi; then acc += (1 - a) t[fi] + a t[fi+1] with the products in scalar
             // (ptxas fuses a packed multiply feeding a packed add or subtract, and the
             // reference rounds each operation)
-            auto pair = [&](float p0, float p1, float q, f2x &acc) {
-                const f2x d = f2_pack(p0 - q, p1 - q);
+            auto pair = [&](float p0, float p1, float qq, f2x &acc) {
+                const f2x d = f2_pack(p0 - qq, p1 - qq);
                 const f2x uu = f2_sub(f2_add(f2_add(d, cxp), hp), hp);
                 const f2x tb = f2_add_rd(uu, MM);
                 const f2x a2 = f2_sub(uu, f2_sub(tb, MM));
@@ -308,21 +317,21 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
 #pragma unroll
             for (int i = 0; i < 8; i += 2) {
                 const float p0 = xc[i] * c, p1 = xc[i + 1] * c;
-                pair(p0, p1, qa, acca[i / 2]);
-                pair(p0, p1, qb, accb[i / 2]);
+#pragma unroll
+                for (int r = 0; r < R; ++r) pair(p0, p1, q[r], acc2[r][i / 2]);
             }
         }
     }
     const float two_pa = (float)g.pa * 2.0f;
     float vmin = INFINITY;
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int Y = r == 0 ? Ya : Yb;
-        const float Yc = r == 0 ? Yca : Ycb;
+    for (int r = 0; r < R; ++r) {
+        const int Y = Y0 + ty + r * kStride;
+        const float Yc = Ycr[r];
         if (Y > Y1) continue;
         float acc[8];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) f2_unpack(r == 0 ? acca[j] : accb[j], acc[2 * j], acc[2 * j + 1]);
+        for (int j = 0; j < 4; ++j) f2_unpack(acc2[r][j], acc[2 * j], acc[2 * j + 1]);
         float *row = img + ((size_t)z * g.ny + Y) * g.nx;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -342,7 +351,7 @@ __global__ void __launch_bounds__(kFbpThreads) fbp_bp_kernel(const float *__rest
         __syncthreads();
         if (threadIdx.x == 0) {
             float m = sh.red[0];
-            for (int i = 1; i < kFbpThreads / 32; ++i) m = fminf(m, sh.red[i]);
+            for (int i = 1; i < kThr / 32; ++i) m = fminf(m, sh.red[i]);
             atomicMin(min_keys + z, fkey(m));
         }
     }
@@ -433,7 +442,13 @@ int launch_fbp_bp(const KGeom &g, const float2 *trig, const float *fprj, float *
         if (e != cudaSuccess) return xct_cuda_fail(e, "fbp min reset");
     }
     dim3 grid(ntx * nty, 1, dN);
-    fbp_bp_kernel<<<grid, kFbpThreads, 0, st>>>(fprj, img, trig, g, ntx, min_keys);
+    // four rows per thread once the grid gives three waves of its resident CTAs (6 per SM)
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if ((long long)grid.x * grid.z >= 3LL * 6 * sms)
+        fbp_bp_kernel<4><<<grid, 128, 0, st>>>(fprj, img, trig, g, ntx, min_keys);
+    else
+        fbp_bp_kernel<2><<<grid, 256, 0, st>>>(fprj, img, trig, g, ntx, min_keys);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return xct_cuda_fail(e, "fbp_bp_kernel launch");
     g_xct_launches.fetch_add(1);
