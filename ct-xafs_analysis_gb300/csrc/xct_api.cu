@@ -410,6 +410,7 @@ static int check_run(xct_plan *p, int dN, const int *sub, int it)
 
 int xct_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, void *stream)
 {
+    XCT_RANGE("xct_osem_run_device");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, dN, sub, it);
     if (rc) return rc;
@@ -422,6 +423,7 @@ int xct_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, 
 
 int xct_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, const int *sub, int it)
 {
+    XCT_RANGE("xct_osem_run");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, dN, sub, it);
     if (rc) return rc;
@@ -635,6 +637,7 @@ int xct_fbp_backproject(xct_plan *p, int dN, const float *d_fprj, float *d_img, 
 
 int xct_fbp_run_device(xct_plan *p, int dN, int zp, const float *d_sino, float *d_img, void *stream)
 {
+    XCT_RANGE("xct_fbp_run_device");
     int rc = check_run(p, dN, nullptr, 0);
     if (rc) return rc;
     if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_fbp_run_device: null device pointer");
@@ -666,6 +669,7 @@ static int hybrid_device(xct_plan *p, int dN, int zp, int order, const float *d_
 int xct_hybrid_run_device(xct_plan *p, int dN, int zp, int baseup_order, const float *d_sino, float *d_img,
                           const int *sub, int it, void *stream)
 {
+    XCT_RANGE("xct_hybrid_run_device");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, dN, sub, it);
     if (rc) return rc;
@@ -707,6 +711,7 @@ static int host_run(xct_plan *p, int dN, const float *const *sino_host, float *c
 
 int xct_fbp_run(xct_plan *p, int dN, int zp, const float *const *sino_host, float *const *img_host)
 {
+    XCT_RANGE("xct_fbp_run");
     int rc = check_run(p, dN, nullptr, 0);
     if (rc) return rc;
     if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
@@ -717,6 +722,7 @@ int xct_fbp_run(xct_plan *p, int dN, int zp, const float *const *sino_host, floa
 int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *const *sino_host,
                    float *const *img_host, const int *sub, int it)
 {
+    XCT_RANGE("xct_hybrid_run");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, dN, sub, it);
     if (rc) return rc;
@@ -731,6 +737,7 @@ int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *c
 int xct_hybrid_cs_run_device(xct_plan *p, int dN, int zp, int baseup_order, const float *d_sino, float *d_img,
                              const int *sub, int it, float cs_lambda, void *stream)
 {
+    XCT_RANGE("xct_hybrid_cs_run_device");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, dN, sub, it);
     if (rc) return rc;
@@ -748,6 +755,7 @@ int xct_hybrid_cs_run_device(xct_plan *p, int dN, int zp, int baseup_order, cons
 int xct_hybrid_cs_run(xct_plan *p, int dN, int zp, int baseup_order, const float *const *sino_host,
                       float *const *img_host, const int *sub, int it, float cs_lambda)
 {
+    XCT_RANGE("xct_hybrid_cs_run");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, dN, sub, it);
     if (rc) return rc;
@@ -769,6 +777,7 @@ int xct_hybrid_cs_run(xct_plan *p, int dN, int zp, int baseup_order, const float
 int xct_osem_run_volume(xct_plan *p, int n, const float *const *sino_host, float *const *img_host, const int *sub,
                         int it)
 {
+    XCT_RANGE("xct_osem_run_volume");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, 1, sub, it);
     if (rc) return rc;
@@ -919,6 +928,7 @@ static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const
 int xct_cs_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                            float cs_lambda, void *stream)
 {
+    XCT_RANGE("xct_cs_osem_run_device");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, dN, sub, it);
     if (rc) return rc;
@@ -933,6 +943,7 @@ int xct_cs_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_im
 int xct_cs_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, const int *sub, int it,
                     float cs_lambda)
 {
+    XCT_RANGE("xct_cs_osem_run");
     if (p && it < 0) it = p->g.it;
     int rc = check_run(p, dN, sub, it);
     if (rc) return rc;
@@ -1005,6 +1016,7 @@ int xct_rot_center_search(xct_plan *p, int n, float shift_start, float shift_ste
                           float ang_fin_deg, float init_value, const float *d_sino, float *d_imgs, float *findex,
                           int *best, void *stream)
 {
+    XCT_RANGE("xct_rot_center_search");
     if (!p) return xct_fail(XCT_E_INVALID, "plan is null");
     int rc = check_shifts(n, shift_start, shift_step);
     if (rc) return rc;

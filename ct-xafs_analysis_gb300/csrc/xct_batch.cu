@@ -228,6 +228,7 @@ static int capture(xct_batch_plan *p)
 
 extern "C" int xct_batch_run(xct_batch_plan *p, const float *const *d_sino, float *const *d_img, void *stream)
 {
+    XCT_RANGE("xct_batch_run");
     if (!p || !d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_batch_run: null argument");
     for (int i = 0; i < p->n; ++i)
         if (!d_sino[i] || !d_img[i]) return xct_fail(XCT_E_INVALID, "xct_batch_run: null slice pointer");
@@ -275,6 +276,7 @@ extern "C" int xct_batch_plan_tuning(xct_batch_plan *p, int *fwd_tile, int *ang_
 // geometry only).  The choice is cached under the batch's shape key.
 extern "C" int xct_batch_plan_autotune(xct_batch_plan *p, const char *cache_path, int flags, void *stream)
 {
+    XCT_RANGE("xct_batch_plan_autotune");
     if (!p) return xct_fail(XCT_E_INVALID, "xct_batch_plan_autotune: plan is null");
     if (!cache_path) cache_path = xct_tune_env_path();
     TuneChoice best;

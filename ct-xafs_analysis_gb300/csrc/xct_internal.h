@@ -184,3 +184,16 @@ enum {
 int xct_check_read_tiled(XctCheckWord *out, bool reset);
 int xct_check_read_fbp(XctCheckWord *out, bool reset);
 #endif
+
+// ---- timeline ranges -----------------------------------------------------------------------
+// An NVTX range over a scope: the library's calls appear by name on an Nsight Systems or
+// Nsight Compute timeline.  NVTX v3 is header-only; without a tool attached a range costs a
+// pointer test.
+#include <nvtx3/nvToolsExt.h>
+struct XctRange {
+    explicit XctRange(const char *name) { nvtxRangePushA(name); }
+    ~XctRange() { nvtxRangePop(); }
+    XctRange(const XctRange &) = delete;
+    XctRange &operator=(const XctRange &) = delete;
+};
+#define XCT_RANGE(name) XctRange xct_range_guard_(name)

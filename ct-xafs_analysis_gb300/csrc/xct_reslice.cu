@@ -596,6 +596,7 @@ int xct_reslice_plan_destroy(xct_reslice_plan *p)
 
 int xct_reslice(xct_reslice_plan *p, int first_angle, int n, const float *d_proj, float *d_sino, void *stream)
 {
+    XCT_RANGE("xct_reslice");
     if (!p) return xct_fail(XCT_E_INVALID, "xct_reslice: plan is null");
     if (!d_proj || !d_sino) return xct_fail(XCT_E_INVALID, "xct_reslice: null device pointer");
     if (n <= 0 || first_angle < 0 || first_angle + n > p->A) {

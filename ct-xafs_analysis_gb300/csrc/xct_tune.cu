@@ -198,6 +198,7 @@ int xct_plan_set_tuning(xct_plan *p, int fwd_tile, int ang_chunk)
 
 int xct_plan_autotune(xct_plan *p, int dN, const char *cache_path, int flags, void *stream)
 {
+    XCT_RANGE("xct_plan_autotune");
     if (!p) return xct_fail(XCT_E_INVALID, "xct_plan_autotune: plan is null");
     if (p->g.kernels != XCT_KERNELS_TILED) return XCT_OK;  // the plain kernels have no tiles
     if (dN <= 0 || dN > p->g.max_batch) return xct_fail(XCT_E_INVALID, "xct_plan_autotune: dN outside [1, max_batch]");

@@ -77,7 +77,7 @@ def build_lib(force=False, verbose=False, extra=(), checked=False):
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _newer(lib, objs):
         tmp = lib + ".tmp%d" % os.getpid()
-        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
