@@ -443,9 +443,7 @@ int launch_fbp_bp(const KGeom &g, const float2 *trig, const float *fprj, float *
     }
     dim3 grid(ntx * nty, 1, dN);
     // four rows per thread once the grid gives three waves of its resident CTAs (6 per SM)
-    int dev = 0, sms = 152;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if ((long long)grid.x * grid.z >= 3LL * 6 * sms)
+    if ((long long)grid.x * grid.z >= 3LL * 6 * device_sm_count())
         fbp_bp_kernel<4><<<grid, 128, 0, st>>>(fprj, img, trig, g, ntx, min_keys);
     else
         fbp_bp_kernel<2><<<grid, 256, 0, st>>>(fprj, img, trig, g, ntx, min_keys);

@@ -185,6 +185,9 @@ int xct_check_read_tiled(XctCheckWord *out, bool reset);
 int xct_check_read_fbp(XctCheckWord *out, bool reset);
 #endif
 
+// SM count of the current device (cached per device).
+int device_sm_count();
+
 // ---- timeline ranges -----------------------------------------------------------------------
 // An NVTX range over a scope: the library's calls appear by name on an Nsight Systems or
 // Nsight Compute timeline.  NVTX v3 is header-only; without a tool attached a range costs a

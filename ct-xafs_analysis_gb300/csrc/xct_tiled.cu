@@ -28,6 +28,8 @@
 //   * the multiplicative update is fused.
 #include <stdint.h>
 
+#include <atomic>
+
 #include <type_traits>
 
 #include "xct_check.cuh"
@@ -822,17 +824,19 @@ int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, floa
     return XCT_OK;
 }
 
-// SM count of the current device (cached per device; a benign race fills the same value).
-static int device_sm_count()
+// SM count of the current device, cached per device (152 if it cannot be read).
+int device_sm_count()
 {
-    static int cache[64] = {0};
+    static std::atomic<int> cache[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
-    if (cache[dev] == 0) {
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
         int n = 0;
-        cache[dev] = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0 ? n : 152;
+        v = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0 ? n : 152;
+        cache[dev].store(v, std::memory_order_relaxed);
     }
-    return cache[dev];
+    return v;
 }
 
 int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const float *ratio, int dN, int sub,
