@@ -19,8 +19,9 @@
 // bins stay in place here and the filtered row is the same in exact arithmetic.  The
 // rounding differs from the reference's radix-2 float FFT at the 1e-6 relative level.
 //
-// FBP backprojection.  Same pixel tiling as the OS-EM backprojector (64 x 32 pixels, 8 per
-// thread, per-angle windows of the filtered row staged in shared memory), with the
+// FBP backprojection.  Same pixel tiling as the OS-EM backprojector (64 x 64 pixels, 8 per
+// thread in two or four rows, per-angle windows of the filtered row staged in shared
+// memory), with the
 // reference's linear sampler along the row and its per-pixel expression order, so the
 // image is bit-identical to FBP.cl's for the same filtered sinogram.
 #include <math.h>

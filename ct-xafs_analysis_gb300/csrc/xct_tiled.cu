@@ -21,15 +21,15 @@
 //   * one CTA owns a 64x64 pixel tile; per angle it stages the window of ratio bins its
 //     pixels hit (bin coordinates are monotone in X and in Y, so the tile corners bound the
 //     window exactly) into shared memory with coalesced loads;
-//   * each of 128 threads gathers 8 pixels of four rows (16 apart) per angle, in angle order,
-//     evaluating the reference's bin expression ((Xc*c - Yc*s) + cx) + 0.5 -- the products
-//     Xc*c once for the four rows, the rest with packed f32x2 instructions (each lane rounds
-//     exactly like the scalar expression) and the nearest rule as a round-down add;
+//   * each thread gathers 8 pixels of four rows (16 apart; 128 threads) or, for launches with
+//     few tiles, of two rows (32 apart; 256 threads) per angle, in angle order, evaluating the
+//     reference's bin expression ((Xc*c - Yc*s) + cx) + 0.5 -- the products Xc*c once for
+//     all its rows, the rest with packed f32x2 instructions (each lane rounds exactly like the
+//     scalar expression) and the nearest rule as a round-down add;
 //   * the multiplicative update is fused.
 #include <stdint.h>
 
 #include <atomic>
-
 #include <type_traits>
 
 #include "xct_check.cuh"
@@ -44,7 +44,7 @@ constexpr int kWarps = kThreads / 32;
 // resident warps per SM to hide the shared-memory load latency
 constexpr int kFwdThreads = 384;
 constexpr int kFwdWarps = kFwdThreads / 32;
-constexpr int kAngChunk = 128;  // angles per CTA (forward) / per staging pass (back)
+constexpr int kAngChunk = 128;  // most subset angles one forward-projector CTA serves
 
 // A warp works on 8 consecutive rays of one angle with 4 lanes per ray, the 4 lanes taking
 // every 4th sample (lane k: samples ya+k, ya+k+4, ...).  A half-warp then reads a compact
