@@ -14,9 +14,10 @@ inputs (10 sinograms + 10 images, ~290 MB) exceed the 129 MB L2, so no flush is 
 Metric: slice-iterations per second (one slice through all 15 subsets once).
   value          -- device-resident inputs, CUDA-event time over the K timed steps
                     (max over ranks), tiled kernels, batched dN = 10;
-  e2e            -- the same metric through the C ABI call with host buffers
-                    (xct_osem_run: pinned host sinograms/images copied in and out
-                    inside the timed region);
+  e2e            -- the same metric through the C ABI with host buffers, every step's
+                    copies in and out inside the timed region: xct_osem_run_volume
+                    (page-locked host sinograms/images, copies overlapped with the
+                    reconstruction), and beside it one blocking xct_osem_run per step;
   per_slice      -- the plain one-slice-per-call path (plain kernels, dN = 1) and the tiled
                     kernels at dN = 1, each on a bounded sample of slices;
   ctxafs_batched -- the CT-XAFS stack sample (uneven slices) in one autotuned batched graph
