@@ -69,6 +69,10 @@ struct xct_plan {
     int acc_rows = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // OS-EM of a batch runs its two halves on the caller's stream and on s_aux (fork/join by
+    // events), so one half's kernels fill the SMs the other half's last waves leave idle
+    cudaStream_t s_aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     float last_ms = 0.0f;
 };
 
