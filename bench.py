@@ -770,6 +770,9 @@ def main():
             "ctxafs_batched": batched, "volume_stream": volume, "next_components": nxt,
             "roofline": roofline, "cpu_baseline": cpu, "finite": finite,
             "launches_per_step": launches / max(args.steps, 1),
+            # library launches before the timed region: the skip count that makes an ncu launch
+            # list (-s) start at the first timed step
+            "launches_before_timed": l0,
         }
         print(json.dumps(line), flush=True)
     plan.close()
