@@ -89,7 +89,10 @@ int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *c
 
 /* Same on device memory: d_sino [dN][pa][px], d_img [dN][ny][nx] (in/out), enqueued on
  * `stream` (a cudaStream_t; NULL is the legacy default stream, as everywhere in CUDA).
- * Asynchronous; stream-ordered with the caller's own work on that stream. */
+ * Asynchronous; stream-ordered with the caller's own work on that stream.  A batch of two or
+ * more slices runs as two halves, the second on a stream of the plan that waits for `stream`
+ * and that `stream` waits for in turn, so the call is still ordered as one unit on `stream`;
+ * a plan serves one call at a time. */
 int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                         void *stream);
 
