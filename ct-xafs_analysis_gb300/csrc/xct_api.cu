@@ -308,28 +308,52 @@ static inline int subset_rows(const xct_plan *p, int sub)
     return p->g.subset_mode == XCT_SUBSETS_COVER ? (pa - sub + ss - 1) / ss : pa / ss;
 }
 
-// The subset/iteration loop over dN slices with the given plan buffers (ratio [dN][pa][px],
-// accumulator [dN][rows][px]) on one stream.
+// One subset step (OSEM1 then OSEM2) of dN slices with the given plan buffers (ratio
+// [dN][pa][px], accumulator [dN][rows][px]) on one stream.
+static int subset_step(xct_plan *p, int dN, const float *meas, float *d_img, float *ratio, double *acc, int s,
+                       cudaStream_t st)
+{
+    const KGeom &g = p->kg;
+    int rc;
+    if (p->g.kernels == XCT_KERNELS_TILED) {
+        rc = launch_fwd_tiled(g, p->d_trig, d_img, meas, ratio, acc, dN, s, g.ss, subset_rows(p, s), st);
+        if (rc) return rc;
+        return launch_bp_update_tiled(g, p->d_trig, d_img, ratio, dN, s, st);
+    }
+    rc = launch_fwd_plain(g, p->d_trig, d_img, meas, ratio, dN, s, g.ss, subset_rows(p, s), st);
+    if (rc) return rc;
+    return launch_bp_update_plain(g, p->d_trig, d_img, ratio, dN, s, st);
+}
+
+// The subset/iteration loop over dN slices with the given plan buffers on one stream.
 static int osem_loop_range(xct_plan *p, int dN, const float *meas, float *d_img, float *ratio, double *acc,
                            const int *sub, int it, cudaStream_t st)
 {
-    const KGeom &g = p->kg;
-    const bool tiled = p->g.kernels == XCT_KERNELS_TILED;
     for (int i = 0; i < it; ++i)
         for (int k = 0; k < p->g.ss; ++k) {
-            const int s = sub[k];
-            int rc;
-            if (tiled) {
-                rc = launch_fwd_tiled(g, p->d_trig, d_img, meas, ratio, acc, dN, s, g.ss, subset_rows(p, s), st);
-                if (rc) return rc;
-                rc = launch_bp_update_tiled(g, p->d_trig, d_img, ratio, dN, s, st);
-            } else {
-                rc = launch_fwd_plain(g, p->d_trig, d_img, meas, ratio, dN, s, g.ss, subset_rows(p, s), st);
-                if (rc) return rc;
-                rc = launch_bp_update_plain(g, p->d_trig, d_img, ratio, dN, s, st);
-            }
+            const int rc = subset_step(p, dN, meas, d_img, ratio, acc, sub[k], st);
             if (rc) return rc;
         }
+    return XCT_OK;
+}
+
+// One subset step of a batch of two or more slices as two halves on two streams (the
+// caller's and the plan's s_aux), joined back into the caller's stream.
+static int subset_step_split(xct_plan *p, int dN, const float *meas, float *d_img, int s, cudaStream_t st)
+{
+    const KGeom &g = p->kg;
+    const int d0 = (dN + 1) / 2;
+    const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
+    double *acc1 = p->d_acc ? p->d_acc + (size_t)d0 * p->acc_rows * g.px : nullptr;
+    XCT_CUDA_TRY(cudaEventRecord(p->ev_fork, st));
+    XCT_CUDA_TRY(cudaStreamWaitEvent(p->s_aux, p->ev_fork, 0));
+    int rc = subset_step(p, d0, meas, d_img, p->d_ratio, p->d_acc, s, st);
+    if (rc == XCT_OK)
+        rc = subset_step(p, dN - d0, meas + d0 * nprj, d_img + d0 * nimg, p->d_ratio + d0 * nprj, acc1, s, p->s_aux);
+    const cudaError_t e1 = cudaEventRecord(p->ev_join, p->s_aux);
+    const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(st, p->ev_join, 0) : e1;
+    if (rc) return rc;
+    if (e2 != cudaSuccess) return xct_cuda_fail(e2, "subset step: join");
     return XCT_OK;
 }
 
@@ -931,7 +955,6 @@ static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const
     }
     XCT_CUDA_TRY(cudaMemcpyAsync(w, d_img, bytes, cudaMemcpyDeviceToDevice, st));  // w = x (:344)
     XCT_CUDA_TRY(cudaMemsetAsync(beta, 0, bytes, st));                             // beta = 0 (:342)
-    const bool tiled = p->g.kernels == XCT_KERNELS_TILED;
     bool first = true;
     for (int i = 0; i < it; ++i)
         for (int k = 0; k < p->g.ss; ++k) {
@@ -941,14 +964,10 @@ static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const
                 rc = launch_ista3d(d_img, xn, g.nx, g.ny, dN, lambda, p->ctx->sm_count, st);
                 first = false;
             } else {
-                if (tiled) {
-                    rc = launch_fwd_tiled(g, p->d_trig, d_img, meas, p->d_ratio, p->d_acc, dN, s, g.ss,
-                                          subset_rows(p, s), st);
-                    if (!rc) rc = launch_bp_update_tiled(g, p->d_trig, d_img, p->d_ratio, dN, s, st);
-                } else {
-                    rc = launch_fwd_plain(g, p->d_trig, d_img, meas, p->d_ratio, dN, s, g.ss, subset_rows(p, s), st);
-                    if (!rc) rc = launch_bp_update_plain(g, p->d_trig, d_img, p->d_ratio, dN, s, st);
-                }
+                // the OS-EM step of the two halves on two streams; the proximal step after the
+                // join couples neighbouring slices
+                rc = dN >= 2 ? subset_step_split(p, dN, meas, d_img, s, st)
+                             : subset_step(p, dN, meas, d_img, p->d_ratio, p->d_acc, s, st);
                 if (!rc) rc = launch_fista3d(w, d_img, beta, xn, g.nx, g.ny, dN, lambda, p->ctx->sm_count, st);
             }
             if (rc) return rc;
