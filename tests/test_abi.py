@@ -64,3 +64,43 @@ def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
     monkeypatch.setattr(xct, "_lib", None)
     with pytest.raises(xct.XCTError):
         xct.load()
+
+
+C_CLIENT = r"""
+#include <stdio.h>
+#include <string.h>
+#include "xct.h"
+
+int main(void)
+{
+    int sub[8];
+    if (xct_abi_version() != XCT_ABI_VERSION) return 2;
+    if (xct_subset_order(8, sub) != XCT_OK) return 3;
+    if (sub[1] != 4 || sub[2] != 2 || sub[7] != 7) return 4;
+    if (xct_subset_order(0, sub) != XCT_E_INVALID) return 5;
+    if (strlen(xct_last_error()) == 0) return 6;
+    if (xct_osem_run_device(NULL, 1, NULL, NULL, NULL, 1, NULL) != XCT_E_INVALID) return 7;
+    printf("c client ok\n");
+    return 0;
+}
+"""
+
+
+def test_header_is_plain_c_and_links_from_c(xct_lib, tmp_path):
+    """The boundary is a C ABI: a C99 program includes the header (no C++ needed), links
+    against the library and calls the entry points that need no GPU."""
+    import shutil
+    import subprocess
+    from xct import build
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "client.c"
+    src.write_text(C_CLIENT)
+    exe = tmp_path / "client"
+    libdir = os.path.dirname(build.LIB)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-I" + HEADER_DIR, str(src), "-o", str(exe),
+                        "-L" + libdir, "-lxct", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and "c client ok" in r.stdout, (r.returncode, r.stdout, r.stderr)
