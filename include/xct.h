@@ -92,7 +92,9 @@ int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *c
  * Asynchronous; stream-ordered with the caller's own work on that stream.  A batch of two or
  * more slices runs as two halves, the second on a stream of the plan that waits for `stream`
  * and that `stream` waits for in turn, so the call is still ordered as one unit on `stream`;
- * a plan serves one call at a time. */
+ * a plan serves one call at a time.  The call can be captured into a CUDA graph (stream
+ * capture of `stream` takes in the second stream through the fork) and replayed; replay
+ * saves the launch overhead that dominates for small slices. */
 int xct_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
                         void *stream);
 

@@ -61,3 +61,34 @@ def test_batch_of_three_equals_single_slices(gpu_ctx, kern, correction):
         assert _rel(out[z], want[z]) <= tol, (kern, correction, z)
     plan.close()
     one.close()
+
+
+def test_device_call_captures_into_a_cuda_graph(gpu_ctx):
+    """A caller can capture xct_osem_run_device -- both halves of the batch and the fork and
+    join between its streams -- into a CUDA graph and replay it (small slices gain 10-25 % from
+    replay); each replay gives the direct call's result."""
+    import xct
+    from xct import phantom as P
+    n, pa, ss, it = 64, 45, 5, 2
+    ang = P.uniform_angles(pa)
+    plan = xct.OSEMPlan(gpu_ctx, n, n, n, ang, ss, it, max_batch=3)
+    imgs = np.stack([P.rasterize_ellipses(P.ellipse_params(n, 4, z, axes=(3, 14)), n, n) + 0.01
+                     for z in range(3)]).astype(np.float32)
+    sino = torch.empty((3, pa, n), device="cuda")
+    plan.fwd(torch.from_numpy(imgs).cuda(), sino)
+    x = torch.ones((3, n, n), device="cuda")
+    plan.run_device(sino, x)
+    torch.cuda.synchronize()
+    want = x.cpu().numpy()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        plan.run_device(sino, x, stream=s)
+    for _ in range(2):
+        x.fill_(1.0)
+        g.replay()
+        torch.cuda.synchronize()
+        assert _rel(x.cpu().numpy(), want) <= 1e-6
+    del g
+    plan.close()
