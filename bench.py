@@ -406,6 +406,8 @@ def next_components(ctx, hbm_gbs):
       fbp            -- ramp filter (zp 4096) + FBP backprojection of 10 slices (FBP.cl);
       hybrid         -- FBP + base-up + 1 OS-EM iteration (15 subsets) of 10 slices;
       cs_osem        -- compressed-sensing OS-EM (ISTA3D/FISTA3D) 1 iteration, 10 slices;
+      operators      -- the forward projector and its exact adjoint over all 1500 angles of
+                        10 slices (xct_fwd / xct_adj);
       reslice        -- 1500 projections of 2048 x 64 rows -> 64 sinograms, with drift shifts;
       rot_center     -- rotation-centre search: 16 shifts of one slice (1 OS-EM it each).
     HBM-bound kernels report GB/s of compulsory traffic against the measured HBM peak."""
@@ -452,6 +454,13 @@ def next_components(ctx, hbm_gbs):
     out["hybrid"] = {"slices_per_s": dn / (ms * 1e-3), "ms_per_10": ms, "osem_iterations": 1}
     ms = timed(lambda: (x.fill_(1.0), plan.cs_run_device(sino, x, it=1)), reps=3)
     out["cs_osem"] = {"slice_iters_per_s": dn / (ms * 1e-3), "ms_per_10": ms}
+    # the operator pair: forward projection and its exact adjoint over all angles (every
+    # bilinear sample whose footprint meets the image is one tap of each)
+    ms_a = timed(lambda: plan.fwd(x, sino), reps=3)
+    ms_t = timed(lambda: plan.adj(sino, x), reps=3)
+    out["operators"] = {"slices": dn, "fwd_ms": ms_a, "adj_ms": ms_t,
+                        "fwd_gtaps_per_s": float(np.sum(t_fwd)) * dn / (ms_a * 1e-3) / 1e9,
+                        "adj_gtaps_per_s": float(np.sum(t_fwd)) * dn / (ms_t * 1e-3) / 1e9}
     plan.close()
     # reslice: 1500 projections of 64 rows x 2048 -> 64 sinograms [1500][2048]
     H = 64
