@@ -74,6 +74,9 @@ static int batch_layout(xct_batch_plan *p, int T, int chunk)
     XCT_CUDA_TRY(cudaMemcpy(p->d_bases, p->bases.data(), sizeof(int) * p->bases.size(), cudaMemcpyHostToDevice));
     int rc = xct_batched_grids(p->ctx->device, p->ctx->sm_count, T, p->grids);
     if (rc) return rc;
+    // the finalize step runs one CTA per unit (ratio row) rather than a persistent grid: its
+    // units are short, so a device queue's per-unit latency would dominate
+    p->grids[1] = p->bases[1 * (n + 1) + n];
     p->fwd_T = T;
     p->fwd_chunk = chunk;
     if (p->exec) {

@@ -626,28 +626,25 @@ __global__ void __launch_bounds__(kFwdThreads, FwdTile<T>::MinBlocks) fwd_batche
     }
 }
 
+// grid: one CTA per finalize unit (a ratio row of an item's largest subset), base[n] of them.
 __global__ void fwd_finalize_batched_kernel(const XctItemDev *__restrict__ items, const int *__restrict__ base,
-                                            int n, int sub, int *queue)
+                                            int n, int sub)
 {
-    __shared__ int s_unit, s_item;
-    const int total = base[n];
-    for (;;) {
-        const int u = queue_take(queue, &s_unit);
-        if (u >= total) break;
-        const int i = unit_item(base, n, u, &s_item);
-        const XctItemDev &it = items[i];
-        const KGeom &g = it.g;
-        const int nrows = it.cover ? (g.pa - sub + g.ss - 1) / g.ss : g.pa / g.ss;
-        const int k = u - base[i];  // one unit per ratio row of the largest subset
-        if (k >= nrows) continue;
-        const int th = sub + k * g.ss;
-        for (int X = threadIdx.x; X < g.px; X += blockDim.x) {
-            double *a = it.acc + (size_t)k * g.px + X;
-            const float p = (float)*a;
-            *a = 0.0;
-            const float yv = xct_measured(it.sino, g.px, g.pa, X, th, g.fetch);
-            it.ratio[(size_t)th * g.px + X] = xct_ratio(yv, p);
-        }
+    __shared__ int s_item;
+    const int u = blockIdx.x;
+    const int i = unit_item(base, n, u, &s_item);
+    const XctItemDev &it = items[i];
+    const KGeom &g = it.g;
+    const int nrows = it.cover ? (g.pa - sub + g.ss - 1) / g.ss : g.pa / g.ss;
+    const int k = u - base[i];  // one unit per ratio row of the largest subset
+    if (k >= nrows) return;
+    const int th = sub + k * g.ss;
+    for (int X = threadIdx.x; X < g.px; X += blockDim.x) {
+        double *a = it.acc + (size_t)k * g.px + X;
+        const float p = (float)*a;
+        *a = 0.0;
+        const float yv = xct_measured(it.sino, g.px, g.pa, X, th, g.fetch);
+        it.ratio[(size_t)th * g.px + X] = xct_ratio(yv, p);
     }
 }
 
@@ -716,7 +713,7 @@ void xct_batched_units(const KGeom &g, int &fwd_ntx, int &fwd_nty, int &fwd_unit
 int xct_batched_grids(int device, int sm_count, int fwd_T, int grids[3])
 {
     (void)device;
-    int a = 0, b = 0, c = 0;
+    int a = 0, c = 0;
     int rc = with_tile(fwd_T, [&](auto tc) -> int {
         constexpr int T = decltype(tc)::value;
         static bool done[64] = {};
@@ -727,10 +724,9 @@ int xct_batched_grids(int device, int sm_count, int fwd_T, int grids[3])
         return XCT_OK;
     });
     if (rc) return rc;
-    XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fwd_finalize_batched_kernel, 256, 0));
     XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, bp_batched_kernel, BpCfg<4>::Threads, 0));
     grids[0] = sm_count * (a > 0 ? a : 1);
-    grids[1] = sm_count * (b > 0 ? b : 1);
+    grids[1] = 0;  // the finalize grid is the plan's unit count
     grids[2] = sm_count * (c > 0 ? c : 1);
     return XCT_OK;
 }
@@ -745,8 +741,10 @@ int launch_osem_step_batched(const XctItemDev *items, const int *bases /*[3][n+1
         return XCT_OK;
     });
     if (rc) return rc;
-    fwd_finalize_batched_kernel<<<grids[1], 256, 0, st>>>(items, bases + (n + 1), n, sub, queues + 1);
-    XCT_CUDA_TRY(cudaGetLastError());
+    if (grids[1] > 0) {
+        fwd_finalize_batched_kernel<<<grids[1], 256, 0, st>>>(items, bases + (n + 1), n, sub);
+        XCT_CUDA_TRY(cudaGetLastError());
+    }
     bp_batched_kernel<<<grids[2], BpCfg<4>::Threads, 0, st>>>(items, bases + 2 * (n + 1), n, sub, queues + 2);
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;  // launches are counted when the captured graph is replayed
