@@ -313,20 +313,38 @@ __global__ void __launch_bounds__(kFwdThreads, FwdTile<T>::MinBlocks) fwd_tiled_
 // sample's 2x2 footprint.  A CTA owns a T x T texel tile; it visits every sample whose base
 // texel lies in [x0-1, x0+T) x [y0-1, y0+T) (exactly those whose footprint touches the
 // tile), scatters its four weighted values into a shared (T+2)^2 accumulator with shared
-// atomics, and writes its own T x T texels once -- no global atomics, no overlap between
-// tiles.  grid: (ntx*nty tiles, 1, dN).
+// atomics (fixed-point integers per window of angles, below), and writes its own T x T
+// texels once -- no global atomics, no overlap between tiles.  grid: (ntx*nty tiles, 1, dN).
 constexpr int kAdjT = 64;
 constexpr int kAdjP = kAdjT + 2;
+constexpr int kAdjWarps = kThreads / 32;  // one angle per warp and window
 
+// Accumulation: the warps take one angle each per window of kAdjWarps angles; within a window
+// the contributions are scattered as 32-bit fixed-point integers (shared-memory integer atomics
+// run ~6x the rate of float ones on this GPU), with a power-of-two scale chosen from the
+// window's largest |ray value| vmax: every contribution is at most vmax * scale <= 2^22, so
+// it converts to an integer with one add of 1.5*2^23 (its low bits hold the rounded value --
+// no conversion instruction), and no texel can overflow: it receives at most six taps per
+// angle (the half-open 2x2 cell around it holds at most five samples of the rotated unit
+// lattice, one more allowed for coordinate rounding), 48 * 2^22 < 2^28 per window.  After the
+// window every thread adds its texels' integers, unscaled, to the float total in window order
+// -- so the result does not depend on the order of the atomics -- and clears them.  One
+// integer unit is at most 2^-21 of vmax, each contribution rounds by at most 2^-22 of it.  A
+// window with a non-finite ray value scatters float atomics instead.
 __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__restrict__ sino,
                                                              float *__restrict__ img,
                                                              const float2 *__restrict__ trig, KGeom g, int ntx)
 {
     __shared__ float accs[kAdjP * kAdjP];
+    __shared__ int acci[kAdjP * kAdjP];
+    __shared__ float wmax[kAdjWarps];
     const int bx = blockIdx.x % ntx, by = blockIdx.x / ntx;
     const int z = blockIdx.z;
     const int x0 = bx * kAdjT, y0 = by * kAdjT;  // owned texels [x0, x0+T) x [y0, y0+T)
-    for (int i = threadIdx.x; i < kAdjP * kAdjP; i += kThreads) accs[i] = 0.0f;
+    for (int i = threadIdx.x; i < kAdjP * kAdjP; i += kThreads) {
+        accs[i] = 0.0f;
+        acci[i] = 0;
+    }
     __syncthreads();
     const float *sn = sino + (size_t)z * g.pa * g.px;
     // base texels whose footprint touches the tile
@@ -334,53 +352,123 @@ __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__rest
     const float ylo = (float)(y0 - 1), yhi = (float)min(y0 + kAdjT, g.ny);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int D = g.depth;
-    for (int th = warp; th < g.pa; th += kWarps) {
-        const float2 cs = trig[th];
-        const float c = cs.x, s = cs.y;
-        const float inv_s = 1.0f / s, inv_c = 1.0f / c;
-        float pmin = 3.0e38f, pmax = -3.0e38f;
+    for (int w0 = 0; w0 < g.pa; w0 += kAdjWarps) {
+        const int th = w0 + warp;
+        const bool active = th < g.pa;
+        float c = 1.0f, s = 0.0f;
+        int Xlo = 0, Xhi = -1;
+        if (active) {
+            const float2 cs = trig[th];
+            c = cs.x;
+            s = cs.y;
+            float pmin = 3.0e38f, pmax = -3.0e38f;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float px_ = (q & 1) ? xhi + 2.0f : xlo - 2.0f;
-            const float py_ = (q & 2) ? yhi + 2.0f : ylo - 2.0f;
-            const float p = (px_ - g.hx) * c - (py_ - g.hy) * s + g.cx;
-            pmin = fminf(pmin, p);
-            pmax = fmaxf(pmax, p);
+            for (int q = 0; q < 4; ++q) {
+                const float px_ = (q & 1) ? xhi + 2.0f : xlo - 2.0f;
+                const float py_ = (q & 2) ? yhi + 2.0f : ylo - 2.0f;
+                const float p = (px_ - g.hx) * c - (py_ - g.hy) * s + g.cx;
+                pmin = fminf(pmin, p);
+                pmax = fmaxf(pmax, p);
+            }
+            Xlo = max(0, (int)floorf(pmin) - 1);
+            Xhi = min(g.px - 1, (int)ceilf(pmax) + 1);
         }
-        const int Xlo = max(0, (int)floorf(pmin) - 1);
-        const int Xhi = min(g.px - 1, (int)ceilf(pmax) + 1);
-        for (int base = Xlo; base <= Xhi; base += 32) {
-            const int X = base + lane;
-            int ya = 0, yb = 0;
-            float ax = 0.0f, ay = 0.0f, v = 0.0f;
-            if (X <= Xhi) {
-                v = __ldg(sn + (size_t)th * g.px + X);
+        // the window's largest |ray value| (NaN and inf make it non-finite)
+        float m = 0.0f;
+        for (int X = Xlo + lane; X <= Xhi; X += 32) {
+            const float v = fabsf(__ldg(sn + (size_t)th * g.px + X));
+            m = (v == v && m == m) ? fmaxf(m, v) : __int_as_float(0x7fc00000);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float t = __shfl_xor_sync(0xffffffffu, m, o);
+            m = (t == t && m == m) ? fmaxf(m, t) : __int_as_float(0x7fc00000);
+        }
+        if (lane == 0) wmax[warp] = m;
+        __syncthreads();
+        float vmax = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kAdjWarps; ++k) {
+            const float t = wmax[k];
+            vmax = (t == t && vmax == vmax) ? fmaxf(vmax, t) : __int_as_float(0x7fc00000);
+        }
+        const bool fixed = vmax < 1.0e30f;  // finite (false for NaN and inf)
+        // scale = 2^(22 - e) with vmax < 2^e: every contribution is below 2^22 in magnitude
+        float scale = 0.0f, inv = 0.0f;
+        if (fixed && vmax > 0.0f) {
+            int e;
+            frexpf(vmax, &e);  // vmax < 2^e
+            e = max(e, -78);   // keep the scale <= 2^100 (a finite float)
+            scale = ldexpf(1.0f, 22 - e);
+            inv = ldexpf(1.0f, e - 22);
+        }
+        if (active && (!fixed || vmax > 0.0f)) {
+            // the forward projector's lane mapping: 8 consecutive rays, 4 lanes per ray taking
+            // every 4th sample of the ray's interval in the tile, whose four limits come from
+            // one boundary search per lane -- the same samples the forward visits
+            const float inv_s = 1.0f / s, inv_c = 1.0f / c;
+            const int ray = lane / kLanesPerRay, ph = lane % kLanesPerRay, grp = lane & ~(kLanesPerRay - 1);
+            const bool bound_x = ph < 2, upper = (ph & 1) != 0;
+            for (int base = Xlo; base <= Xhi; base += kRaysPerWarp) {
+                const int X = base + ray;
+                const bool live = X <= Xhi;
+                const float v = live ? __ldg(sn + (size_t)th * g.px + X) : 0.0f;
                 const float Xc = (float)X - g.cx;
-                ax = fmaf(Xc, c, g.hx);
-                ay = fmaf(Xc, -s, g.hy);
-                int a0, a1, b0, b1;
-                coord_range(xlo, xhi, ax, s, inv_s, g.hd, D, a0, a1);
-                coord_range(ylo, yhi, ay, c, inv_c, g.hd, D, b0, b1);
-                ya = max(a0, b0);
-                yb = v != 0.0f ? min(a1, b1) : ya;  // a zero ray contributes nothing
-            }
-            for (int Y = ya; Y < yb; ++Y) {
-                const float Yc = (float)Y - g.hd;
-                const float x = fmaf(Yc, s, ax), y = fmaf(Yc, c, ay);
-                const float fi = floorf(x), fj = floorf(y);
-                const float fx = x - fi, fy = y - fj;
-                const int col = (int)fi - (x0 - 1), row = (int)fj - (y0 - 1);
-                const float gx = 1.0f - fx, gy = 1.0f - fy;
-                if (!XCT_IN(row * kAdjP + col, 0, kAdjP * kAdjP - kAdjP - 2, XCT_SITE_ADJ)) continue;
-                float *a = accs + row * kAdjP + col;
-                atomicAdd(a, gx * gy * v);
-                atomicAdd(a + 1, fx * gy * v);
-                atomicAdd(a + kAdjP, gx * fy * v);
-                atomicAdd(a + kAdjP + 1, fx * fy * v);
+                const float ax = fmaf(Xc, c, g.hx);
+                const float ay = fmaf(Xc, -s, g.hy);
+                int lim = 0;
+                if (live) {
+                    const float a = bound_x ? ax : ay, sl = bound_x ? s : c, isl = bound_x ? inv_s : inv_c;
+                    const float lo = bound_x ? xlo : ylo, hi = bound_x ? xhi : yhi;
+                    if (sl != 0.0f) {
+                        const float bnd = ((sl > 0.0f) != upper) ? lo : hi;
+                        lim = first_true(bnd, a, sl, isl, g.hd, D);
+                    } else {
+                        lim = upper ? ((a >= lo && a < hi) ? D : 0) : 0;
+                    }
+                }
+                const int l0 = __shfl_sync(0xffffffffu, lim, grp + 0), l1 = __shfl_sync(0xffffffffu, lim, grp + 1);
+                const int l2 = __shfl_sync(0xffffffffu, lim, grp + 2), l3 = __shfl_sync(0xffffffffu, lim, grp + 3);
+                const int ya = max(l0, l2);
+                const int yb = (live && v != 0.0f) ? min(l1, l3) : ya;  // a zero ray contributes nothing
+                const float vs = v * scale;
+                for (int Y = ya + ph; Y < yb; Y += kLanesPerRay) {
+                    const float Yc = (float)Y - g.hd;
+                    const float x = fmaf(Yc, s, ax), y = fmaf(Yc, c, ay);
+                    const float fi = floorf(x), fj = floorf(y);
+                    const float fx = x - fi, fy = y - fj;
+                    const int col = (int)fi - (x0 - 1), row = (int)fj - (y0 - 1);
+                    const float gx = 1.0f - fx, gy = 1.0f - fy;
+                    if (!XCT_IN(row * kAdjP + col, 0, kAdjP * kAdjP - kAdjP - 2, XCT_SITE_ADJ)) continue;
+                    const int o = row * kAdjP + col;
+                    if (fixed) {
+                        // round(x) for |x| < 2^22: the low bits of x + 1.5*2^23
+                        const float p0 = vs * gy, p1 = vs * fy;
+                        atomicAdd(acci + o, __float_as_int(gx * p0 + kMagic) - 0x4B400000);
+                        atomicAdd(acci + o + 1, __float_as_int(fx * p0 + kMagic) - 0x4B400000);
+                        atomicAdd(acci + o + kAdjP, __float_as_int(gx * p1 + kMagic) - 0x4B400000);
+                        atomicAdd(acci + o + kAdjP + 1, __float_as_int(fx * p1 + kMagic) - 0x4B400000);
+                    } else {
+                        atomicAdd(accs + o, gx * gy * v);
+                        atomicAdd(accs + o + 1, fx * gy * v);
+                        atomicAdd(accs + o + kAdjP, gx * fy * v);
+                        atomicAdd(accs + o + kAdjP + 1, fx * fy * v);
+                    }
+                }
             }
         }
+        __syncthreads();
+        if (fixed && vmax > 0.0f) {
+            for (int i = threadIdx.x; i < kAdjP * kAdjP; i += kThreads) {
+                const int q = acci[i];
+                if (q != 0) {
+                    accs[i] += (float)q * inv;
+                    acci[i] = 0;
+                }
+            }
+        }
+        __syncthreads();  // the integers are clear and wmax may be rewritten
     }
-    __syncthreads();
     float *im = img + (size_t)z * g.nx * g.ny;
     for (int i = threadIdx.x; i < kAdjT * kAdjT; i += kThreads) {
         const int r = i / kAdjT, cc = i - r * kAdjT;
