@@ -329,8 +329,11 @@ constexpr int kAdjWarps = kThreads / 32;  // one angle per warp and window
 // lattice, one more allowed for coordinate rounding), 48 * 2^22 < 2^28 per window.  After the
 // window every thread adds its texels' integers, unscaled, to the float total in window order
 // -- so the result does not depend on the order of the atomics -- and clears them.  One
-// integer unit is at most 2^-21 of vmax, each contribution rounds by at most 2^-22 of it.  A
-// window with a non-finite ray value scatters float atomics instead.
+// integer unit is at most 2^-21 of vmax, each contribution rounds by at most 2^-22 of it; only
+// rays with |value| >= vmax * 2^-6 take the integer path (so each of their contributions
+// rounds by at most 2^-16 of the ray's value, below the weight error of float32 sample
+// coordinates), smaller ones -- and every ray of a window with a non-finite value -- scatter
+// float atomics, which keep full relative precision.
 __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__restrict__ sino,
                                                              float *__restrict__ img,
                                                              const float2 *__restrict__ trig, KGeom g, int ntx)
@@ -432,6 +435,7 @@ __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__rest
                 const int ya = max(l0, l2);
                 const int yb = (live && v != 0.0f) ? min(l1, l3) : ya;  // a zero ray contributes nothing
                 const float vs = v * scale;
+                const bool as_int = fixed && fabsf(v) >= vmax * 0.015625f;  // |v| >= vmax * 2^-6
                 for (int Y = ya + ph; Y < yb; Y += kLanesPerRay) {
                     const float Yc = (float)Y - g.hd;
                     const float x = fmaf(Yc, s, ax), y = fmaf(Yc, c, ay);
@@ -441,7 +445,7 @@ __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__rest
                     const float gx = 1.0f - fx, gy = 1.0f - fy;
                     if (!XCT_IN(row * kAdjP + col, 0, kAdjP * kAdjP - kAdjP - 2, XCT_SITE_ADJ)) continue;
                     const int o = row * kAdjP + col;
-                    if (fixed) {
+                    if (as_int) {
                         // round(x) for |x| < 2^22: the low bits of x + 1.5*2^23
                         const float p0 = vs * gy, p1 = vs * fy;
                         atomicAdd(acci + o, __float_as_int(gx * p0 + kMagic) - 0x4B400000);

@@ -3,8 +3,11 @@
 * dot-product test <A x, y> = <x, A^T y> on 32 seeded (x, y) pairs, 1024^2 image, 720
   angles, 1024 bins, to 1e-5 relative (inner products accumulated in float64);
 * A^T against the oracle's scatter adjoint (rel-L2 1e-5: the GPU sums fixed-point
-  contributions per window of angles, each rounded at 2^-22 of the window's largest value);
-  and two runs give identical bits (integer sums do not depend on the atomics' order);
+  contributions per window of angles, each rounded at 2^-22 of the window's largest value),
+  also for a sinogram of 1e-6-scale values whose centre ray is 1.0 at every angle (rays far
+  below their window's largest value keep float precision: checked by linearity on the GPU);
+  two runs give identical bits when every ray of a window is within 2^6 of its largest
+  (integer sums do not depend on the atomics' order);
 * gradient of the Poisson log-likelihood against central finite differences of an FP64
   model (64^2, 90 angles);
 * a 50-step unrolled reconstruction: gradients with per-iteration checkpointing equal the
@@ -119,8 +122,8 @@ def test_unrolled_reconstruction_checkpointing_and_reference_gradient(gpu_ctx, o
         loss.backward()
         grads.append((float(st.grad), yy.grad.clone()))
     (g1, gy1), (g2, gy2) = grads
-    # recomputation repeats the forward pass; the adjoint's shared-memory float atomics sum
-    # in a run-dependent order, so the two graphs agree to rounding, not bit for bit
+    # recomputation repeats the forward pass; the adjoint's float atomics (rays far below their
+    # window's largest value) sum in a run-dependent order, so the two graphs agree to rounding
     assert abs(g1 - g2) <= 1e-3 * abs(g2)
     assert float((gy1 - gy2).norm() / gy2.norm()) <= 1e-3
 
@@ -136,16 +139,62 @@ def test_unrolled_reconstruction_checkpointing_and_reference_gradient(gpu_ctx, o
     plan.close()
 
 
+def test_adjoint_high_dynamic_range(gpu_ctx, oracle_lib):
+    """One bright ray (1.0) per angle, through the image centre, among rays of ~1e-6: the
+    tiles round the centre see a bright ray in every window of angles.  Rounding the small
+    rays to the bright window's fixed-point unit (2^-21) puts texels off the bright lines ~20%
+    off; the small rays keep float precision instead.
+
+    Geometry-free check: adj(y) = adj(bright rays) + adj(small rays) texel by texel, all three
+    on the GPU, to float summation noise (the bright taps round identically in the first two,
+    so only mixing magnitudes in one window could break it).  Against the float64 oracle the
+    texels off the blob agree to 2e-3: the float32 sample coordinates alone move them by up to
+    ~6e-4 (a plain float scatter measures the same on this input)."""
+    import xct
+    from xct import phantom as P
+    O = oracle_lib
+    n, px, pa = 128, 128, 720
+    ang = P.uniform_angles(pa)
+    plan = xct.OSEMPlan(gpu_ctx, n, n, px, ang, 1, 1)
+    rng = np.random.default_rng(21)
+    y = (rng.uniform(1.0, 2.0, (pa, px)) * 1e-6).astype(np.float32)
+    bright = np.zeros_like(y)
+    bright[:, px // 2] = 1.0
+    small = y.copy()
+    small[:, px // 2] = 0.0
+    y[:, px // 2] = 1.0
+
+    def adj(v):
+        out = torch.empty((1, n, n), device="cuda")
+        plan.adj(torch.from_numpy(v).cuda().reshape(1, pa, px).contiguous(), out)
+        torch.cuda.synchronize()
+        return out[0].cpu().numpy().astype(np.float64)
+
+    got, got_b, got_s = adj(y), adj(bright), adj(small)
+    yy, xx = np.mgrid[0:n, 0:n]
+    far = np.hypot(xx + 0.5 - n / 2, yy + 0.5 - n / 2) > 6  # off the bright blob
+    # the small rays of adj(y) go through float atomics into the running total: ~3600 rounded
+    # adds per texel at 2^-24 each bound the difference by ~2e-4 (measured 4e-5 at most)
+    lin = np.abs(got - (got_b + got_s))[far] / np.abs(got)[far]
+    assert lin.max() <= 2e-4, lin.max()
+    want = O.adjoint(y, ang, n, n, dtype=np.float64)
+    rel = np.abs(got - want)[far] / np.abs(want)[far]
+    assert rel.max() <= 2e-3, rel.max()
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) <= 2e-5
+    plan.close()
+
+
 def test_adjoint_is_deterministic(gpu_ctx):
-    """Integer accumulation per window: the same input gives the same bits every run, on an
-    odd shape with an off-centre axis."""
+    """Integer accumulation per window: with every ray within 2^6 of its window's largest
+    value, the same input gives the same bits every run, on an odd shape with an off-centre
+    axis."""
     import xct
     nx, ny, px, pa = 150, 97, 170, 61
     ang = np.sort(np.random.default_rng(8).uniform(0, 180, pa)).astype(np.float32)
     plan = xct.OSEMPlan(gpu_ctx, nx, ny, px, ang, 1, 1, center_bin=px * 0.5 + 2.25, max_batch=2)
     g = torch.Generator(device="cuda")
     g.manual_seed(4)
-    y = torch.randn((2, pa, px), device="cuda", generator=g)
+    y = torch.rand((2, pa, px), device="cuda", generator=g) + 1.0  # in [1, 2)
     a = torch.empty((2, ny, nx), device="cuda")
     b = torch.empty_like(a)
     plan.adj(y, a)
