@@ -187,7 +187,12 @@ int xct_osem2(xct_plan *plan, int dN, int sub, float *d_img, const float *d_rati
  *              bilinear ray sums, d_sino[dN][pa][px] = A d_img.
  * xct_bp_ref : the reference plain backprojector `backProjection`
  *              (reconstShare.cl:245-275) with ss = 1, sub = 0 (all angles).
- * xct_adj    : the exact adjoint A^T of xct_fwd (d_img = A^T d_sino).               */
+ * xct_adj    : the exact adjoint A^T of xct_fwd (d_img = A^T d_sino): the same samples
+ *              and bilinear weights, scattered.  Per window of 8 angles, the rays within
+ *              2^6 of the window's largest |value| are summed as fixed-point integers (each
+ *              contribution rounded by at most 2^-16 of its ray's value); smaller rays, and
+ *              windows holding a NaN or an infinity, use float atomics.  Results repeat bit
+ *              for bit when every window takes the integer path only.                      */
 int xct_fwd(xct_plan *plan, int dN, const float *d_img, float *d_sino, void *stream);
 int xct_bp_ref(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
 int xct_adj(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
