@@ -104,3 +104,32 @@ def test_header_is_plain_c_and_links_from_c(xct_lib, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0 and "c client ok" in r.stdout, (r.returncode, r.stdout, r.stderr)
+
+
+def test_last_error_is_per_thread(xct_lib):
+    """xct_last_error() is per thread: a failing call in one thread leaves another thread's
+    message alone (the reference runs one reconstruction thread per device beside its input
+    and output threads, CT_reconstruction/GPU.cpp:629-658)."""
+    import threading
+    seen = {}
+    step = threading.Barrier(2, timeout=30)
+
+    def first():
+        xct_lib.xct_subset_order(0, None)  # fails: ss must be > 0
+        step.wait()                        # the other thread fails now
+        step.wait()
+        seen["first"] = xct_lib.xct_last_error()
+
+    def second():
+        step.wait()
+        xct_lib.xct_osem_plan_create(None, None, ctypes.byref(ctypes.c_void_p()))
+        seen["second"] = xct_lib.xct_last_error()
+        step.wait()
+
+    ts = [threading.Thread(target=f) for f in (first, second)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(timeout=60)
+    assert b"xct_subset_order" in seen["first"], seen
+    assert b"xct_osem_plan_create" in seen["second"], seen
