@@ -332,8 +332,8 @@ constexpr int kAdjWarps = kThreads / 32;  // one angle per warp and window
 // integer unit is at most 2^-21 of vmax, each contribution rounds by at most 2^-22 of it; only
 // rays with |value| >= vmax * 2^-6 take the integer path (so each of their contributions
 // rounds by at most 2^-16 of the ray's value, below the weight error of float32 sample
-// coordinates), smaller ones -- and every ray of a window with a non-finite value -- scatter
-// float atomics, which keep full relative precision.
+// coordinates), smaller ones -- and every ray of a window with a non-finite value or one above
+// 1e30 -- scatter float atomics, which keep full relative precision.
 __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__restrict__ sino,
                                                              float *__restrict__ img,
                                                              const float2 *__restrict__ trig, KGeom g, int ntx)
@@ -395,7 +395,8 @@ __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__rest
             const float t = wmax[k];
             vmax = (t == t && vmax == vmax) ? fmaxf(vmax, t) : __int_as_float(0x7fc00000);
         }
-        const bool fixed = vmax < 1.0e30f;  // finite (false for NaN and inf)
+        // false for NaN and inf, and for finite windows above 1e30: those scatter float atomics
+        const bool fixed = vmax < 1.0e30f;
         // scale = 2^(22 - e) with vmax < 2^e: every contribution is below 2^22 in magnitude
         float scale = 0.0f, inv = 0.0f;
         if (fixed && vmax > 0.0f) {
