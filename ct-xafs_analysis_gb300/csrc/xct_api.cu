@@ -477,6 +477,72 @@ int xct_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, 
                                   "xct_osem_run_device");
 }
 
+// xct_osem_run for a batch of two or more slices: the batch's two halves each carry their own
+// copies and kernels on their own stream (the plan's stream and s_aux), enqueued so that one
+// half's uploads and downloads overlap the other half's kernels.  Copies from pageable host
+// memory return only when done, so the host order is: upload A, kernels A, upload B (while A
+// runs), kernels B, download A (while B runs), download B.  ev0..ev1 spans the first kernel to
+// the later half's last (ev_fork, after its first use for the fork, marks the end of A).
+static int osem_host_split(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host,
+                           const int *sub, int it)
+{
+    const KGeom &g = p->kg;
+    const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
+    const int d0 = (dN + 1) / 2;
+    const int first[2] = {0, d0}, count[2] = {d0, dN - d0};
+    cudaStream_t sts[2] = {p->stream, p->s_aux};
+    double *accs[2] = {p->d_acc, p->d_acc ? p->d_acc + (size_t)d0 * p->acc_rows * g.px : nullptr};
+    XCT_CUDA_TRY(cudaEventRecord(p->ev_fork, sts[0]));
+    XCT_CUDA_TRY(cudaStreamWaitEvent(sts[1], p->ev_fork, 0));
+    auto upload_and_run = [&](int h) -> int {
+        cudaStream_t st = sts[h];
+        cudaError_t e;
+        for (int i = first[h]; i < first[h] + count[h]; ++i) {
+            if ((e = cudaMemcpyAsync(p->d_sino + i * nprj, sino_host[i], sizeof(float) * nprj, cudaMemcpyHostToDevice,
+                                     st)) != cudaSuccess)
+                return xct_cuda_fail(e, "xct_osem_run: upload sinogram");
+            if ((e = cudaMemcpyAsync(p->d_img + i * nimg, img_host[i], sizeof(float) * nimg, cudaMemcpyHostToDevice,
+                                     st)) != cudaSuccess)
+                return xct_cuda_fail(e, "xct_osem_run: upload image");
+        }
+        if (h == 0 && (e = cudaEventRecord(p->ev0, st)) != cudaSuccess) return xct_cuda_fail(e, "xct_osem_run: event");
+        const float *meas = p->d_sino + first[h] * nprj;
+        if (p->g.correction_mode > 0) {
+            const int r = launch_sino_correction(g, meas, p->d_corr + first[h] * nprj, p->d_corr_ang, p->d_corr_bin,
+                                                 p->g.correction_mode, count[h], st);
+            if (r) return r;
+            meas = p->d_corr + first[h] * nprj;
+        }
+        const int r = osem_loop_range(p, count[h], meas, p->d_img + first[h] * nimg, p->d_ratio + first[h] * nprj,
+                                      accs[h], sub, it, st);
+        if (r) return r;
+        if (h == 0) e = cudaEventRecord(p->ev_fork, st);
+        else if ((e = cudaStreamWaitEvent(st, p->ev_fork, 0)) == cudaSuccess) e = cudaEventRecord(p->ev1, st);
+        return e == cudaSuccess ? XCT_OK : xct_cuda_fail(e, "xct_osem_run: event");
+    };
+    auto download = [&](int h) -> int {
+        for (int i = first[h]; i < first[h] + count[h]; ++i) {
+            const cudaError_t e = cudaMemcpyAsync(img_host[i], p->d_img + i * nimg, sizeof(float) * nimg,
+                                                  cudaMemcpyDeviceToHost, sts[h]);
+            if (e != cudaSuccess) return xct_cuda_fail(e, "xct_osem_run: download image");
+        }
+        return XCT_OK;
+    };
+    int rc = upload_and_run(0);
+    if (rc == XCT_OK) rc = upload_and_run(1);
+    if (rc == XCT_OK) rc = download(0);
+    if (rc == XCT_OK) rc = download(1);
+    // join in every case, so that nothing of this call is still queued when it returns
+    const cudaError_t e1 = cudaEventRecord(p->ev_join, sts[1]);
+    const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(sts[0], p->ev_join, 0) : e1;
+    const cudaError_t e3 = cudaStreamSynchronize(sts[0]);
+    if (rc) return rc;
+    if (e2 != cudaSuccess) return xct_cuda_fail(e2, "xct_osem_run: join");
+    if (e3 != cudaSuccess) return xct_cuda_fail(e3, "xct_osem_run: synchronize");
+    XCT_CUDA_TRY(cudaEventElapsedTime(&p->last_ms, p->ev0, p->ev1));
+    return XCT_OK;
+}
+
 int xct_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, const int *sub, int it)
 {
     XCT_RANGE("xct_osem_run");
@@ -487,6 +553,11 @@ int xct_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *cons
     for (int i = 0; i < dN; ++i)
         if (!sino_host[i] || !img_host[i]) return xct_fail(XCT_E_INVALID, "xct_osem_run: null slice pointer");
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    // two or more slices: halves with their own copies on two streams (a traced call keeps
+    // the one-stream order below, whose launches the trace times)
+    const bool traced = trace_file() != nullptr && p->g.correction_mode == 0;
+    if (dN >= 2 && it > 0 && !traced)
+        return osem_host_split(p, dN, sino_host, img_host, sub ? sub : p->sub_default.data(), it);
     const size_t nimg = (size_t)p->g.nx * p->g.ny, nprj = (size_t)p->g.px * p->g.pa;
     cudaStream_t st = p->stream;
     // host -> device (OSEM_thread, GPU.cpp:440-445)

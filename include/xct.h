@@ -83,7 +83,10 @@ int xct_subset_order(int ss, int *sub);
 /* ---- OS-EM: replaces OSEM_execution (GPU.cpp:125-240) + the host<->device image copies
  * of OSEM_thread (GPU.cpp:440-445, 460-463).  sino_host[i] is slice i's [pa][px]
  * sinogram, img_host[i] its [ny][nx] image (initial image in, reconstruction out).
- * Blocking.  sub may be NULL (the plan's subset order).  it < 0 uses the plan's it. */
+ * Blocking.  sub may be NULL (the plan's subset order).  it < 0 uses the plan's it.  A batch
+ * of two or more slices runs as two halves, each with its own copies on its own stream, so
+ * one half's uploads and downloads overlap the other half's kernels (page-locked host
+ * buffers overlap fully; pageable ones as far as their synchronous copies allow). */
 int xct_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *const *img_host, const int *sub,
                  int it);
 

@@ -2,7 +2,8 @@
 half on the plan's own stream, with offset views of the plan's ratio, accumulator and
 corrected-sinogram buffers).  A batch of 3 (halves of 2 and 1) equals the three slices run
 one per call, for both kernel families, with and without a sinogram correction, through the
-device and the host-buffer forms; and the caller's stream sees the finished result."""
+device and the host-buffer forms (the latter with each half's copies on its own stream); and
+the caller's stream sees the finished result."""
 import numpy as np
 import pytest
 
