@@ -493,6 +493,15 @@ def next_components(ctx, hbm_gbs):
     out["fbp"] = {"slices_per_s": dn / (ms * 1e-3), "ms_per_10": ms, "filter_ms": ms_f, "backproject_ms": ms_b,
                   "filter_hbm_gbs": 2 * dn * PA * PX * 4 / (ms_f * 1e-3) / 1e9, "hbm_peak_gbs": hbm_gbs,
                   "backproject_tflops": bp_flop / (ms_b * 1e-3) / 1e12}
+    # the same FBP through the blocking host-buffer call (pageable arrays, as the drop-in host
+    # program passes them): copies in and out included, wall time
+    host_s = [sino[z].cpu().numpy() for z in range(dn)]
+    host_x = [np.empty((NY, NX), np.float32) for _ in range(dn)]
+    plan.fbp_run(host_s, host_x, zp=4096)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        plan.fbp_run(host_s, host_x, zp=4096)
+    out["fbp"]["host_slices_per_s"] = 3 * dn / (time.perf_counter() - t0)
     ms = timed(lambda: (x.fill_(0.0), plan.hybrid(sino, x, zp=4096, it=1)), reps=3)
     out["hybrid"] = {"slices_per_s": dn / (ms * 1e-3), "ms_per_10": ms, "osem_iterations": 1}
     ms = timed(lambda: (x.fill_(1.0), plan.cs_run_device(sino, x, it=1)), reps=3)

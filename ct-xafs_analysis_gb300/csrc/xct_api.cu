@@ -477,21 +477,21 @@ int xct_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, 
                                   "xct_osem_run_device");
 }
 
-// xct_osem_run for a batch of two or more slices: the batch's two halves each carry their own
-// copies and kernels on their own stream (the plan's stream and s_aux), enqueued so that one
-// half's uploads and downloads overlap the other half's kernels.  Copies from pageable host
-// memory return only when done, so the host order is: upload A, kernels A, upload B (while A
-// runs), kernels B, download A (while B runs), download B.  ev0..ev1 spans the first kernel to
-// the later half's last (ev_fork, after its first use for the fork, marks the end of A).
-static int osem_host_split(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host,
-                           const int *sub, int it)
+// A blocking host-buffer call on a batch of two or more independent slices: the batch's two
+// halves each carry their own copies and kernels (run_half(first, count, stream), using the
+// plan's work buffers from slice `first` on) on their own stream -- the plan's stream and
+// s_aux -- enqueued so that one half's uploads and downloads overlap the other half's kernels.
+// Copies from pageable host memory return only when done, so the host order is: upload A,
+// kernels A, upload B (while A runs), kernels B, download A (while B runs), download B.
+// ev0..ev1 spans the first kernel to the later half's last (ev_fork, after its first use for
+// the fork, marks the end of A).
+static int host_run_split(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host,
+                          bool upload_img, const std::function<int(int, int, cudaStream_t)> &run_half)
 {
-    const KGeom &g = p->kg;
-    const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
+    const size_t nimg = (size_t)p->g.nx * p->g.ny, nprj = (size_t)p->g.px * p->g.pa;
     const int d0 = (dN + 1) / 2;
     const int first[2] = {0, d0}, count[2] = {d0, dN - d0};
     cudaStream_t sts[2] = {p->stream, p->s_aux};
-    double *accs[2] = {p->d_acc, p->d_acc ? p->d_acc + (size_t)d0 * p->acc_rows * g.px : nullptr};
     XCT_CUDA_TRY(cudaEventRecord(p->ev_fork, sts[0]));
     XCT_CUDA_TRY(cudaStreamWaitEvent(sts[1], p->ev_fork, 0));
     auto upload_and_run = [&](int h) -> int {
@@ -500,31 +500,23 @@ static int osem_host_split(xct_plan *p, int dN, const float *const *sino_host, f
         for (int i = first[h]; i < first[h] + count[h]; ++i) {
             if ((e = cudaMemcpyAsync(p->d_sino + i * nprj, sino_host[i], sizeof(float) * nprj, cudaMemcpyHostToDevice,
                                      st)) != cudaSuccess)
-                return xct_cuda_fail(e, "xct_osem_run: upload sinogram");
-            if ((e = cudaMemcpyAsync(p->d_img + i * nimg, img_host[i], sizeof(float) * nimg, cudaMemcpyHostToDevice,
-                                     st)) != cudaSuccess)
-                return xct_cuda_fail(e, "xct_osem_run: upload image");
+                return xct_cuda_fail(e, "upload sinogram");
+            if (upload_img && (e = cudaMemcpyAsync(p->d_img + i * nimg, img_host[i], sizeof(float) * nimg,
+                                                   cudaMemcpyHostToDevice, st)) != cudaSuccess)
+                return xct_cuda_fail(e, "upload image");
         }
-        if (h == 0 && (e = cudaEventRecord(p->ev0, st)) != cudaSuccess) return xct_cuda_fail(e, "xct_osem_run: event");
-        const float *meas = p->d_sino + first[h] * nprj;
-        if (p->g.correction_mode > 0) {
-            const int r = launch_sino_correction(g, meas, p->d_corr + first[h] * nprj, p->d_corr_ang, p->d_corr_bin,
-                                                 p->g.correction_mode, count[h], st);
-            if (r) return r;
-            meas = p->d_corr + first[h] * nprj;
-        }
-        const int r = osem_loop_range(p, count[h], meas, p->d_img + first[h] * nimg, p->d_ratio + first[h] * nprj,
-                                      accs[h], sub, it, st);
+        if (h == 0 && (e = cudaEventRecord(p->ev0, st)) != cudaSuccess) return xct_cuda_fail(e, "event");
+        const int r = run_half(first[h], count[h], st);
         if (r) return r;
         if (h == 0) e = cudaEventRecord(p->ev_fork, st);
         else if ((e = cudaStreamWaitEvent(st, p->ev_fork, 0)) == cudaSuccess) e = cudaEventRecord(p->ev1, st);
-        return e == cudaSuccess ? XCT_OK : xct_cuda_fail(e, "xct_osem_run: event");
+        return e == cudaSuccess ? XCT_OK : xct_cuda_fail(e, "event");
     };
     auto download = [&](int h) -> int {
         for (int i = first[h]; i < first[h] + count[h]; ++i) {
             const cudaError_t e = cudaMemcpyAsync(img_host[i], p->d_img + i * nimg, sizeof(float) * nimg,
                                                   cudaMemcpyDeviceToHost, sts[h]);
-            if (e != cudaSuccess) return xct_cuda_fail(e, "xct_osem_run: download image");
+            if (e != cudaSuccess) return xct_cuda_fail(e, "download image");
         }
         return XCT_OK;
     };
@@ -537,10 +529,30 @@ static int osem_host_split(xct_plan *p, int dN, const float *const *sino_host, f
     const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(sts[0], p->ev_join, 0) : e1;
     const cudaError_t e3 = cudaStreamSynchronize(sts[0]);
     if (rc) return rc;
-    if (e2 != cudaSuccess) return xct_cuda_fail(e2, "xct_osem_run: join");
-    if (e3 != cudaSuccess) return xct_cuda_fail(e3, "xct_osem_run: synchronize");
+    if (e2 != cudaSuccess) return xct_cuda_fail(e2, "join");
+    if (e3 != cudaSuccess) return xct_cuda_fail(e3, "synchronize");
     XCT_CUDA_TRY(cudaEventElapsedTime(&p->last_ms, p->ev0, p->ev1));
     return XCT_OK;
+}
+
+// xct_osem_run's halves: the sinogram correction (if any) and the subset/iteration loop on
+// the plan's buffers from slice `first` on.
+static int osem_host_split(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host,
+                           const int *sub, int it)
+{
+    const KGeom &g = p->kg;
+    const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
+    return host_run_split(p, dN, sino_host, img_host, true, [&](int first, int count, cudaStream_t st) {
+        const float *meas = p->d_sino + first * nprj;
+        if (p->g.correction_mode > 0) {
+            const int r = launch_sino_correction(g, meas, p->d_corr + first * nprj, p->d_corr_ang, p->d_corr_bin,
+                                                 p->g.correction_mode, count, st);
+            if (r) return r;
+            meas = p->d_corr + first * nprj;
+        }
+        double *acc = p->d_acc ? p->d_acc + (size_t)first * p->acc_rows * g.px : nullptr;
+        return osem_loop_range(p, count, meas, p->d_img + first * nimg, p->d_ratio + first * nprj, acc, sub, it, st);
+    });
 }
 
 int xct_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, const int *sub, int it)
@@ -723,22 +735,26 @@ int xct_osem_profile(xct_plan *p, int dN, const float *d_sino, float *d_img, con
 // correction when it has one (GPU.cpp:711-723, applied into the correction buffer), the
 // ramp filter into the ratio buffer, backProjectionFBP into d_img.  The ratio buffer is
 // cleared afterwards: OS-EM relies on the rows it never writes being 0.
+// FBP of dN slices; the plan's work buffers (corrected sinograms, filtered sinograms, minima)
+// are used from slice `first` on, so the halves of a batch can run side by side.
 static int fbp_device(xct_plan *p, int dN, int zp, const float *d_sino, float *d_img, bool with_min,
-                      const float **meas_out, cudaStream_t st)
+                      const float **meas_out, cudaStream_t st, int first = 0)
 {
     const KGeom &g = p->kg;
+    const size_t nprj = (size_t)g.pa * g.px;
+    float *fprj = p->d_ratio + first * nprj;
     const float *meas = d_sino;
     if (p->g.correction_mode > 0) {
-        int rc = launch_sino_correction(g, d_sino, p->d_corr, p->d_corr_ang, p->d_corr_bin, p->g.correction_mode, dN,
-                                        st);
+        int rc = launch_sino_correction(g, d_sino, p->d_corr + first * nprj, p->d_corr_ang, p->d_corr_bin,
+                                        p->g.correction_mode, dN, st);
         if (rc) return rc;
-        meas = p->d_corr;
+        meas = p->d_corr + first * nprj;
     }
-    int rc = launch_fbp_filter(g, meas, p->d_ratio, dN, zp, st);
+    int rc = launch_fbp_filter(g, meas, fprj, dN, zp, st);
     if (rc) return rc;
-    rc = launch_fbp_bp(g, p->d_trig, p->d_ratio, d_img, dN, with_min ? p->d_min_keys : nullptr, st);
+    rc = launch_fbp_bp(g, p->d_trig, fprj, d_img, dN, with_min ? p->d_min_keys + first : nullptr, st);
     if (rc) return rc;
-    XCT_CUDA_TRY(cudaMemsetAsync(p->d_ratio, 0, sizeof(float) * dN * (size_t)g.pa * g.px, st));
+    XCT_CUDA_TRY(cudaMemsetAsync(fprj, 0, sizeof(float) * dN * nprj, st));
     if (meas_out) *meas_out = meas;
     return XCT_OK;
 }
@@ -842,6 +858,14 @@ int xct_fbp_run(xct_plan *p, int dN, int zp, const float *const *sino_host, floa
     int rc = check_run(p, dN, nullptr, 0);
     if (rc) return rc;
     if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    if (dN >= 2) {  // halves with their own copies on two streams
+        const size_t nimg = (size_t)p->g.nx * p->g.ny, nprj = (size_t)p->g.px * p->g.pa;
+        return host_run_split(p, dN, sino_host, img_host, false, [&](int first, int count, cudaStream_t st) {
+            return fbp_device(p, count, zp, p->d_sino + first * nprj, p->d_img + first * nimg, false, nullptr, st,
+                              first);
+        });
+    }
     return host_run(p, dN, sino_host, img_host, false,
                     [&](cudaStream_t st) { return fbp_device(p, dN, zp, p->d_sino, p->d_img, false, nullptr, st); });
 }
