@@ -9,7 +9,9 @@ phantom leaves empty rays, so OSEM1's small-projection branch (ratio = measured 
 * OSEM1's ratio rows are bit-identical for the plain kernels and within 5e-6 rel-L2 (1e-4 per
   bin) for the tiled ones, whose per-tile partial ray sums meet in double; rows outside the
   subset stay untouched;
-* the FBP backprojector on the same geometries is bit-identical to backProjectionFBP.
+* the FBP backprojector on the same geometries is bit-identical to backProjectionFBP;
+* the exact adjoint passes the dot-product test against the forward projector and matches
+  the oracle's scatter adjoint.
 """
 import numpy as np
 import pytest
@@ -112,4 +114,29 @@ def test_random_geometry_fbp_backprojection(gpu_ctx, oracle_lib, seed):
         want = O.bp_fbp(fprj[z], ang, nx, ny, cx=cx)
         bad = np.argwhere(got != want)
         assert bad.size == 0, "case %d slice %d: %d pixels differ, first %s" % (seed, z, len(bad), bad[:5].tolist())
+    plan.close()
+
+
+@pytest.mark.parametrize("seed", range(CASES))
+def test_random_geometry_adjoint(gpu_ctx, oracle_lib, seed):
+    """The exact adjoint on the same random geometries: <A x, y> = <x, A^T y> to 1e-5 (inner
+    products in float64) with the forward projector, and A^T y against the oracle's scatter
+    adjoint to 1e-5 rel-L2."""
+    import xct
+    O = oracle_lib
+    nx, ny, px, pa, ss, ang, cx, tile, chunk, subs, rng = _geometry(seed)
+    plan = xct.OSEMPlan(gpu_ctx, nx, ny, px, ang, 1, 1, center_bin=cx)
+    x = rng.uniform(0.0, 1.0, (1, ny, nx)).astype(np.float32)
+    y = rng.uniform(0.0, 1.0, (1, pa, px)).astype(np.float32)
+    ax = torch.empty((1, pa, px), device="cuda")
+    aty = torch.empty((1, ny, nx), device="cuda")
+    plan.fwd(_dev(x), ax)
+    plan.adj(_dev(y), aty)
+    torch.cuda.synchronize()
+    ax, aty = ax.cpu().numpy().astype(np.float64), aty.cpu().numpy().astype(np.float64)
+    lhs = float(np.sum(ax * y))
+    rhs = float(np.sum(x * aty))
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs), (seed, lhs, rhs)
+    want = O.adjoint(y[0], ang, nx, ny, cx=cx, dtype=np.float64)
+    assert np.linalg.norm(aty[0] - want) / np.linalg.norm(want) <= 1e-5, seed
     plan.close()
