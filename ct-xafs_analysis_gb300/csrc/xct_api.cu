@@ -809,6 +809,25 @@ static int hybrid_device(xct_plan *p, int dN, int zp, int order, const float *d_
     return osem_loop(p, dN, meas, d_img, sub ? sub : p->sub_default.data(), it, st, false);
 }
 
+// One half of a host-buffer hybrid batch: FBP, base-up and OS-EM of `count` slices on the
+// plan's buffers from slice `first` on, on one stream (no inner split: the halves already
+// run side by side).
+static int hybrid_half(xct_plan *p, int first, int count, int zp, int order, const int *sub, int it,
+                       cudaStream_t st)
+{
+    const KGeom &g = p->kg;
+    const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
+    float *img = p->d_img + first * nimg;
+    const float *meas = nullptr;
+    int rc = fbp_device(p, count, zp, p->d_sino + first * nprj, img, true, &meas, st, first);
+    if (rc) return rc;
+    rc = launch_base_up(g, img, count, order, p->d_min_keys + first, p->ctx->sm_count, st);
+    if (rc) return rc;
+    double *acc = p->d_acc ? p->d_acc + (size_t)first * p->acc_rows * g.px : nullptr;
+    return osem_loop_range(p, count, meas, img, p->d_ratio + first * nprj, acc, sub ? sub : p->sub_default.data(), it,
+                           st);
+}
+
 int xct_hybrid_run_device(xct_plan *p, int dN, int zp, int baseup_order, const float *d_sino, float *d_img,
                           const int *sub, int it, void *stream)
 {
@@ -879,6 +898,11 @@ int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *c
     if (rc) return rc;
     if (baseup_order < 0 || baseup_order > 64) return xct_fail(XCT_E_INVALID, "xct_hybrid_run: order 0..64");
     if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    if (dN >= 2)  // halves with their own copies on two streams
+        return host_run_split(p, dN, sino_host, img_host, false, [&](int first, int count, cudaStream_t st) {
+            return hybrid_half(p, first, count, zp, baseup_order, sub, it, st);
+        });
     return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
         return hybrid_device(p, dN, zp, baseup_order, p->d_sino, p->d_img, sub, it, st);
     });

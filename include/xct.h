@@ -219,9 +219,9 @@ int xct_adj(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *str
  *                       the corrected sinogram (it < 0: the plan's; sub NULL: plan order).
  * xct_fbp_run / xct_hybrid_run : the same from host buffers (FBP_thread, GPU.cpp:822-893):
  *                       sinograms in, images out (the images' initial contents are not
- *                       read: the backprojection writes every pixel).  Blocking.  xct_fbp_run
- *                       runs a batch of two or more slices as two halves, each with its own
- *                       copies on its own stream, as xct_osem_run does. */
+ *                       read: the backprojection writes every pixel).  Blocking.  Both run a
+ *                       batch of two or more slices as two halves, each with its own copies
+ *                       on its own stream, as xct_osem_run does. */
 int xct_fbp_filter(xct_plan *plan, int dN, int zp, const float *d_sino, float *d_fprj, void *stream);
 int xct_fbp_backproject(xct_plan *plan, int dN, const float *d_fprj, float *d_img, void *stream);
 int xct_fbp_run_device(xct_plan *plan, int dN, int zp, const float *d_sino, float *d_img, void *stream);
