@@ -26,7 +26,7 @@ Metric: slice-iterations per second (one slice through all 15 subsets once).
                     10 slices per call, beside the CPU oracle's full run of one slice;
   next_components-- throughput of FBP, the hybrid, the compressed-sensing OS-EM, reslice,
                     denoise and the rotation-centre search (HBM-bound ones against the
-                    measured HBM peak);
+                    measured HBM peak), with the CPU oracle on bounded samples beside them;
   volume_stream  -- a sample of the full-volume workload (2048^2, 1800 angles, 20 subsets x 3
                     it, rotation centre +3.5 bins, I0 = 2e4) streamed from page-locked host
                     memory by xct_osem_run_volume, against blocking per-batch calls and the
@@ -256,6 +256,49 @@ def cpu_baseline_sample(nsub=3):
     dt = time.perf_counter() - t0
     return {"value": nsub / SS / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
             "sample": "%d subsets (OSEM1+OSEM2) of one 2048^2 slice, 1500 angles, OpenMP" % nsub}
+
+
+def next_cpu_baselines():
+    """The CPU oracle (OpenMP, all host cores) on bounded samples of the next_components
+    workloads, each scaled to the unit of its GPU figure: FBP of one 2048^2 slice with 300 of
+    the 1500 angles (work is linear in the angle count), the compressed-sensing OS-EM of one
+    slice for one iteration, reslice and denoise of 16 of the 64 rows, and the exact adjoint
+    of one slice over 20 angles."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from xct import phantom
+    oracle.build()
+    rng = np.random.default_rng(11)
+    ang = phantom.uniform_angles(PA)
+    out = {"cores": os.cpu_count(), "kind": "port"}
+    samp = ang[::5]  # 300 angles
+    sino = rng.uniform(0.0, 1.0, (len(samp), PX)).astype(np.float32)
+    t0 = time.perf_counter()
+    oracle.fbp(sino, samp, NX, NY, 4096)
+    out["fbp_slices_per_s"] = (len(samp) / PA) / (time.perf_counter() - t0)
+    # positive random measurements: the oracle's work does not depend on the values
+    meas = rng.uniform(0.05, 1.0, (1, PA, PX)).astype(np.float32)
+    t0 = time.perf_counter()
+    oracle.cs_osem_run(np.ones((1, NY, NX), np.float32), meas, ang, SS, 1)
+    out["cs_osem_slice_iters_per_s"] = 1 / (time.perf_counter() - t0)
+    H = 16
+    mt = rng.uniform(0.5, 1.5, (PA, H, PX)).astype(np.float32)
+    xs, ys = rng.uniform(-2, 2, PA).astype(np.float32), rng.uniform(-1, 1, PA).astype(np.float32)
+    t0 = time.perf_counter()
+    r = oracle.reslice(mt, xs, ys, 0.0, 1)
+    out["reslice_gbs"] = 2 * mt.nbytes / (time.perf_counter() - t0) / 1e9
+    t0 = time.perf_counter()
+    oracle.denoise_sinogram(r, 0.1)
+    out["denoise_gbs"] = 2 * r.nbytes / (time.perf_counter() - t0) / 1e9
+    samp = ang[::75]  # 20 angles
+    y = rng.uniform(0.0, 1.0, (len(samp), PX)).astype(np.float32)
+    t_fwd, _ = algorithmic_counts(samp, NX, NY, PX)
+    t0 = time.perf_counter()
+    oracle.adjoint(y, samp, NX, NY)
+    out["adj_gtaps_per_s"] = float(np.sum(t_fwd)) / (time.perf_counter() - t0) / 1e9
+    out["samples"] = ("FBP: one 2048^2 slice, 300 of 1500 angles, zp 4096; CS OS-EM: one slice, 15 subsets x 1 "
+                      "it; reslice/denoise: 1500 x 16 x 2048; adjoint: one slice, 20 angles")
+    return out
 
 
 def small_case_256(ctx, reps=5):
@@ -824,6 +867,11 @@ def main():
             cpu = cpu_baseline_sample()
         except Exception as e:  # reported, never fatal
             cpu = {"value": None, "error": str(e)[:200]}
+        if isinstance(nxt, dict) and "error" not in nxt:
+            try:
+                nxt["cpu_oracle"] = next_cpu_baselines()
+            except Exception as e:  # reported, never fatal
+                nxt["cpu_oracle"] = {"error": str(e)[:200]}
 
     if rank == 0:
         line = {
