@@ -39,7 +39,6 @@
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
 // forward projector: 12 warps per CTA so that 3 CTAs (3 x 69 KB of shared memory) give 36
 // resident warps per SM to hide the shared-memory load latency
 constexpr int kFwdThreads = 384;
@@ -117,23 +116,6 @@ __device__ __forceinline__ int first_true(float b, float a, float sl, float inv_
     const bool ph = (Y >= D) || (up ? (uh >= b) : (uh < b));
     if (!pl && ph) return Y;
     return first_true_search(b, a, sl, hd, D);
-}
-
-// Y range [ya, yb) of samples whose coordinate u lies in [lo, hi).
-__device__ __forceinline__ void coord_range(float lo, float hi, float a, float sl, float inv_sl, float hd, int D,
-                                            int &ya, int &yb)
-{
-    if (sl > 0.0f) {
-        ya = first_true(lo, a, sl, inv_sl, hd, D);
-        yb = first_true(hi, a, sl, inv_sl, hd, D);
-    } else if (sl < 0.0f) {
-        ya = first_true(hi, a, sl, inv_sl, hd, D);
-        yb = first_true(lo, a, sl, inv_sl, hd, D);
-    } else {  // constant coordinate: fma(Yc, 0, a) == a for every Y
-        const bool in = (a >= lo) && (a < hi);
-        ya = 0;
-        yb = in ? D : 0;
-    }
 }
 
 __device__ __forceinline__ void lds_f2(unsigned addr, float &a, float &b)
