@@ -38,7 +38,9 @@ namespace {
 
 // backprojection: 64 x 64 pixel tiles (each thread 8 pixels of two rows 32 apart), windows of
 // kFbpW >= 63|c| + 63|s| + 4 bins staged kFbpChunk angles at a time
-constexpr int kFbpTX = 64, kFbpTY = 64, kFbpThreads = 256, kFbpChunk = 64, kFbpW = 96;
+// (40 angles of 96 bin pairs: 31 KB of shared memory, so the register-limited six CTAs of the
+// four-row kernel still fit on an SM)
+constexpr int kFbpTX = 64, kFbpTY = 64, kFbpThreads = 256, kFbpChunk = 40, kFbpW = 96;
 
 // ------------------------------------------------------------------ ramp filter (FFT)
 __device__ __forceinline__ int fpad(int i) { return i + (i >> 4); }  // 16-entry rows + 1
@@ -195,24 +197,16 @@ __global__ void __launch_bounds__(1024) fbp_filter_kernel(const float *__restric
 
 // ------------------------------------------------------------ FBP backprojection
 struct FbpShared {
-    float win[kFbpChunk * kFbpW];
+    float2 win[kFbpChunk * kFbpW];  // entry j of angle k: (t[lo+j], t[lo+j+1]), the lerp's two bins
     float2 scs[kFbpChunk];
     int slo[kFbpChunk];
-    unsigned soff[kFbpChunk];  // shared address of angle k's entry for floor bits fb: soff[k] + 4*fb
+    unsigned soff[kFbpChunk];  // shared address of angle k's entry for floor bits fb: soff[k] + 8*fb
     float red[kFbpThreads / 32];
 };
 
-__device__ __forceinline__ float fbp_lds(unsigned addr)
+__device__ __forceinline__ void fbp_lds2(unsigned addr, float &t0, float &t1)
 {
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
-    return v;
-}
-__device__ __forceinline__ float fbp_lds_next(unsigned addr)
-{
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1+4];" : "=f"(v) : "r"(addr));
-    return v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(t0), "=f"(t1) : "r"(addr));
 }
 
 // Monotone integer key of a float (atomicMin on keys orders as the floats do).
@@ -231,7 +225,7 @@ __device__ __forceinline__ float fkey_decode(int k) { return __int_as_float(k >=
 // R rows per thread (kFbpTY / R apart, 512 / R threads): R = 4 shares the products Xc*c over
 // four rows; R = 2 fills the SMs better when a launch has few tiles.
 template <int R>
-__global__ void __launch_bounds__(512 / R) fbp_bp_kernel(const float *__restrict__ fprj, float *__restrict__ img,
+__global__ void __launch_bounds__(512 / R, R == 4 ? 6 : 4) fbp_bp_kernel(const float *__restrict__ fprj, float *__restrict__ img,
                                                          const float2 *__restrict__ trig, KGeom g, int ntx,
                                                          int *__restrict__ min_keys)
 {
@@ -242,6 +236,8 @@ __global__ void __launch_bounds__(512 / R) fbp_bp_kernel(const float *__restrict
     const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
     const int X0 = bx * kFbpTX, Y0 = by * kFbpTY;
     const int X1 = min(X0 + kFbpTX, g.nx) - 1, Y1 = min(Y0 + kFbpTY, g.ny) - 1;
+    // thread tx takes the pixels X0 + tx + 8i (i < 8): the 8 lanes of a row read neighbouring
+    // bins and write neighbouring pixels
     const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
     float Ycr[R];
 #pragma unroll
@@ -249,7 +245,7 @@ __global__ void __launch_bounds__(512 / R) fbp_bp_kernel(const float *__restrict
     float xc[8];
     f2x acc2[R][4];  // pixel pairs of each row, packed adds (each lane an IEEE add)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) xc[i] = (float)min(X0 + tx * 8 + i, X1) - g.hx;
+    for (int i = 0; i < 8; ++i) xc[i] = (float)min(X0 + tx + 8 * i, X1) - g.hx;
 #pragma unroll
     for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -272,18 +268,20 @@ __global__ void __launch_bounds__(512 / R) fbp_bp_kernel(const float *__restrict
             lo = min(lo, xct_floor_bits(xct_bin_coord(xa, cs.x, qb, g.cx) - 0.5f));
             lo = min(lo, xct_floor_bits(xct_bin_coord(xb, cs.x, qb, g.cx) - 0.5f));
             sh.slo[k] = lo - XCT_FLOOR_BIAS;
-            // entry for floor bits fb: k*W + fb - lo  (mod 2^32)
-            sh.soff[k] = wbase + 4u * (unsigned)(k * kFbpW) - 4u * (unsigned)lo;
+            // entry for floor bits fb: k*W + fb - lo  (mod 2^32), 8 bytes each
+            sh.soff[k] = wbase + 8u * (unsigned)(k * kFbpW) - 8u * (unsigned)lo;
         }
         __syncthreads();
         for (int i = threadIdx.x; i < kn * kFbpW; i += kThr) {
             const int k = i / kFbpW, j = i - k * kFbpW;
             const int bin = sh.slo[k] + j;
-            sh.win[i] = ((unsigned)bin < (unsigned)g.px) ? __ldg(rt + (size_t)(k0 + k) * g.px + bin) : 0.0f;
+            const float *rk = rt + (size_t)(k0 + k) * g.px;
+            sh.win[i] = make_float2(((unsigned)bin < (unsigned)g.px) ? __ldg(rk + bin) : 0.0f,
+                                    ((unsigned)(bin + 1) < (unsigned)g.px) ? __ldg(rk + bin + 1) : 0.0f);
         }
         __syncthreads();
-        // a pair's first entry may be any but the window's last (the pair reads the next one)
-        const unsigned wlo = wbase, whi = wbase + 4u * (unsigned)(kn * kFbpW - 2);
+        // any entry of the staged windows (each holds both bins of its lerp)
+        const unsigned wlo = wbase, whi = wbase + 8u * (unsigned)(kn * kFbpW - 1);
         (void)wlo;
         (void)whi;
         for (int k = 0; k < kn; ++k) {
@@ -309,10 +307,13 @@ __global__ void __launch_bounds__(512 / R) fbp_bp_kernel(const float *__restrict
                 float a0, a1, w0, w1;
                 f2_unpack(a2, a0, a1);
                 f2_unpack(w2, w0, w1);
-                const unsigned ad0 = (unsigned)e0 * 4u + off, ad1 = (unsigned)e1 * 4u + off;
+                const unsigned ad0 = (unsigned)e0 * 8u + off, ad1 = (unsigned)e1 * 8u + off;
                 const bool in0 = XCT_IN(ad0, wlo, whi, XCT_SITE_FBP_WIN), in1 = XCT_IN(ad1, wlo, whi, XCT_SITE_FBP_WIN);
-                const float p00 = w0 * (in0 ? fbp_lds(ad0) : 0.0f), p01 = a0 * (in0 ? fbp_lds_next(ad0) : 0.0f);
-                const float p10 = w1 * (in1 ? fbp_lds(ad1) : 0.0f), p11 = a1 * (in1 ? fbp_lds_next(ad1) : 0.0f);
+                float t00 = 0.0f, t01 = 0.0f, t10 = 0.0f, t11 = 0.0f;
+                if (in0) fbp_lds2(ad0, t00, t01);
+                if (in1) fbp_lds2(ad1, t10, t11);
+                const float p00 = w0 * t00, p01 = a0 * t01;
+                const float p10 = w1 * t10, p11 = a1 * t11;
                 acc = f2_add(acc, f2_add(f2_pack(p00, p10), f2_pack(p01, p11)));
             };
 #pragma unroll
@@ -336,7 +337,7 @@ __global__ void __launch_bounds__(512 / R) fbp_bp_kernel(const float *__restrict
         float *row = img + ((size_t)z * g.ny + Y) * g.nx;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const int X = X0 + tx * 8 + i;
+            const int X = X0 + tx + 8 * i;
             if (X <= X1) {
                 const float rr = sqrtf(xc[i] * xc[i] + Yc * Yc);
                 const float v = (rr < g.hx) ? __fdiv_rn(acc[i], two_pa) : 0.0f;
