@@ -531,7 +531,9 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
     unsigned *soff = sh.soff;
     const int X0 = bx * kBpTX, Y0 = by * kBpTY;
     const int X1 = min(X0 + kBpTX, g.nx) - 1, Y1 = min(Y0 + kBpTY, g.ny) - 1;
-    // 8 threads x 8 pixels across; thread row ty covers rows ty + r * (kBpTY / kBpRows)
+    // 8 threads x 8 pixels across, thread tx taking X0 + tx + 8i (the 8 lanes of a row read
+    // neighbouring bins and write neighbouring pixels); thread row ty covers rows
+    // ty + r * (kBpTY / kBpRows)
     constexpr int kStride = BpCfg<kBpRows>::Stride, kBpThreads = BpCfg<kBpRows>::Threads;
     const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
     // threads past the image edge of a partial tile gather for the edge pixel (inside the
@@ -542,8 +544,8 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
     f2x xcp[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const float a = (float)min(X0 + tx * 8 + 2 * j, X1) - g.hx;
-        const float b = (float)min(X0 + tx * 8 + 2 * j + 1, X1) - g.hx;
+        const float a = (float)min(X0 + tx + 16 * j, X1) - g.hx;
+        const float b = (float)min(X0 + tx + 16 * j + 8, X1) - g.hx;
         xcp[j] = f2_pack(a, b);
     }
     f2x acc[kBpRows][4];  // pixel pairs of each row, packed adds (each lane an IEEE add)
@@ -625,7 +627,7 @@ __device__ __forceinline__ void bp_tile(const KGeom &g, float *__restrict__ img,
         for (int j = 0; j < 4; ++j) f2_unpack(acc[r][j], v[2 * j], v[2 * j + 1]);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const int X = X0 + tx * 8 + i;
+            const int X = X0 + tx + 8 * i;
             if (X <= X1) row[X] = xct_update(row[X], v[i], ssf, paf);
         }
     }
