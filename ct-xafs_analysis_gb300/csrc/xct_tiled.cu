@@ -21,7 +21,7 @@
 //   * one CTA owns a 64x64 pixel tile; per angle it stages the window of ratio bins its
 //     pixels hit (bin coordinates are monotone in X and in Y, so the tile corners bound the
 //     window exactly) into shared memory with coalesced loads;
-//   * each thread gathers 8 pixels of four rows (16 apart; 128 threads) or, for launches with
+//   * each thread gathers 8 pixels (8 apart) of four rows (16 apart; 128 threads) or, for launches with
 //     few tiles, of two rows (32 apart; 256 threads) per angle, in angle order, evaluating the
 //     reference's bin expression ((Xc*c - Yc*s) + cx) + 0.5 -- the products Xc*c once for
 //     all its rows, the rest with packed f32x2 instructions (each lane rounds exactly like the
