@@ -128,6 +128,15 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def _int_range(a, sl, t0, lo_v, hi_v):
+    """The integers t with lo_v <= a + sl * (t - t0) < hi_v, as [start, end) (arrays over a;
+    sl != 0).  A falling coordinate turns the lower bound into an inclusive upper bound on t
+    and the strict upper bound into a strict lower bound."""
+    if sl > 0:
+        return np.ceil((lo_v - a) / sl + t0), np.ceil((hi_v - a) / sl + t0)
+    return np.floor((hi_v - a) / sl + t0) + 1, np.floor((lo_v - a) / sl + t0) + 1
+
+
 def algorithmic_counts(angles, nx, ny, px, cx=None):
     """T_fwd: bilinear samples whose 2x2 footprint meets the image (base texel in
     [-1, nx-1] x [-1, ny-1]), per angle, from the exact chord of each ray; T_bp: (pixel,
@@ -139,35 +148,32 @@ def algorithmic_counts(angles, nx, ny, px, cx=None):
     t_bp = np.zeros(len(angles))
     Xc = np.arange(px) - cx
     Yc = np.arange(ny) - ny * 0.5
-    Xp = np.arange(nx) - nx * 0.5
     for k, (c, s) in enumerate(zip(np.cos(phi), np.sin(phi))):
+        # a direction cosine below 1e-12 (cos 90, sin 180 in float64) is exactly 0: the rays
+        # are axis-aligned, and every term below uses the same snapped values
+        c = 0.0 if abs(c) < 1e-12 else float(c)
+        s = 0.0 if abs(s) < 1e-12 else float(s)
+        # sample Y of ray X: x = (Y - D/2) s + ax, y = (Y - D/2) c + ay
         ax = Xc * c + nx * 0.5
         ay = -Xc * s + ny * 0.5
-        lo = np.full(px, -np.inf)
-        hi = np.full(px, np.inf)
+        lo = np.zeros(px)
+        hi = np.full(px, float(D))
         for a, sl, n in ((ax, s, nx), (ay, c, ny)):
-            if abs(sl) < 1e-12:
-                inside = (a >= -1) & (a < n)
-                lo = np.where(inside, lo, np.inf)
+            if sl == 0.0:
+                hi = np.where((a >= -1) & (a < n), hi, 0.0)
                 continue
-            y1 = (-1 - a) / sl + D * 0.5
-            y2 = (n - a) / sl + D * 0.5
-            lo = np.maximum(lo, np.minimum(y1, y2))
-            hi = np.minimum(hi, np.maximum(y1, y2))
-        lo = np.clip(np.ceil(lo), 0, D)
-        hi = np.clip(np.ceil(hi), 0, D)
+            l, h = _int_range(a, sl, D * 0.5, -1.0, float(n))
+            lo = np.maximum(lo, l)
+            hi = np.minimum(hi, h)
         t_fwd[k] = np.maximum(hi - lo, 0).sum()
-        # bins of row Y are floor(Xp*c - Yc*s + cx + 0.5): count X in [0, nx) with
-        # 0 <= Xp*c + off < px, an interval in X per row
+        # bins of row Y are floor((X - nx/2) c + off), off = cx + 0.5 - Yc s: count X in
+        # [0, nx) with 0 <= (X - nx/2) c + off < px
         off = cx + 0.5 - Yc * s
-        if abs(c) < 1e-12:
+        if c == 0.0:
             t_bp[k] = nx * np.count_nonzero((off >= 0) & (off < px))
             continue
-        x1 = (0 - off) / c + nx * 0.5
-        x2 = (px - off) / c + nx * 0.5
-        a = np.clip(np.ceil(np.minimum(x1, x2)), 0, nx)
-        b = np.clip(np.ceil(np.maximum(x1, x2)), 0, nx)
-        t_bp[k] = np.maximum(b - a, 0).sum()
+        l, h = _int_range(off, c, nx * 0.5, 0.0, float(px))
+        t_bp[k] = np.maximum(np.minimum(h, nx) - np.maximum(l, 0), 0).sum()
     return t_fwd, t_bp
 
 
