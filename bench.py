@@ -326,7 +326,7 @@ def small_case_256(ctx, reps=5):
     out = {"workload": "256^2, 180 angles, 256 bins, 10 subsets x 5 iterations"}
     for dn in (1, 10):
         plan = xct.OSEMPlan(ctx, n, n, n, ang, ss, it, max_batch=dn)
-        sino = torch.from_numpy(np.array(np.broadcast_to(meas, (dn, pa, n)))).cuda()
+        sino = torch.from_numpy(np.repeat(meas[None], dn, axis=0)).cuda()  # C-contiguous copy
         x = torch.empty((dn, n, n), device="cuda")
         for _ in range(2):
             plan.run_device(sino, x.fill_(1.0), dN=dn)
