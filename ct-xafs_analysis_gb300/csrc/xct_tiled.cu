@@ -297,8 +297,9 @@ __global__ void __launch_bounds__(kFwdThreads, FwdTile<T>::MinBlocks) fwd_tiled_
 // tile), scatters its four weighted values into a shared (T+2)^2 accumulator with shared
 // atomics (fixed-point integers per window of angles, below), and writes its own T x T
 // texels once -- no global atomics, no overlap between tiles.  grid: (ntx*nty tiles, 1, dN).
-constexpr int kAdjT = 64;
-constexpr int kAdjP = kAdjT + 2;
+// tile side: 64, or 32 when a launch of 64-texel tiles would leave fewer than three CTAs per
+// SM (one slice of 1024^2 makes only 256 tiles of 64)
+constexpr int kAdjT = 64, kAdjTSmall = 32;
 constexpr int kAdjWarps = kThreads / 32;  // one angle per warp and window
 
 // Accumulation: the warps take one angle each per window of kAdjWarps angles; within a window
@@ -316,10 +317,12 @@ constexpr int kAdjWarps = kThreads / 32;  // one angle per warp and window
 // rounds by at most 2^-16 of the ray's value, below the weight error of float32 sample
 // coordinates), smaller ones -- and every ray of a window with a non-finite value or one above
 // 1e30 -- scatter float atomics, which keep full relative precision.
+template <int T>
 __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__restrict__ sino,
                                                              float *__restrict__ img,
                                                              const float2 *__restrict__ trig, KGeom g, int ntx)
 {
+    constexpr int kAdjT = T, kAdjP = T + 2;  // this launch's tile side and pitch
     __shared__ float accs[kAdjP * kAdjP];
     __shared__ int acci[kAdjP * kAdjP];
     __shared__ float wmax[kAdjWarps];
@@ -891,9 +894,14 @@ int launch_fwd_tiled(const KGeom &g, const float2 *trig, const float *img, const
 int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, cudaStream_t st)
 {
     if (dN <= 0) return XCT_OK;
-    const int ntx = (g.nx + kAdjT - 1) / kAdjT, nty = (g.ny + kAdjT - 1) / kAdjT;
-    dim3 grid(ntx * nty, 1, dN);
-    adj_tiled_kernel<<<grid, kThreads, 0, st>>>(sino, img, trig, g, ntx);
+    const long long big = (long long)((g.nx + kAdjT - 1) / kAdjT) * ((g.ny + kAdjT - 1) / kAdjT) * dN;
+    if (big >= 3LL * device_sm_count()) {
+        const int ntx = (g.nx + kAdjT - 1) / kAdjT, nty = (g.ny + kAdjT - 1) / kAdjT;
+        adj_tiled_kernel<kAdjT><<<dim3(ntx * nty, 1, dN), kThreads, 0, st>>>(sino, img, trig, g, ntx);
+    } else {
+        const int ntx = (g.nx + kAdjTSmall - 1) / kAdjTSmall, nty = (g.ny + kAdjTSmall - 1) / kAdjTSmall;
+        adj_tiled_kernel<kAdjTSmall><<<dim3(ntx * nty, 1, dN), kThreads, 0, st>>>(sino, img, trig, g, ntx);
+    }
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;
