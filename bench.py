@@ -651,6 +651,29 @@ def profile_case():
     print(json.dumps({"profile_case": "ok", "mean": float(x.mean())}))
 
 
+def profile_case_slices(n=8):
+    """Small case for profilers, the slice-interleaved forward projector: n slices of the
+    workload (sinograms made with the per-slice forward projector, one launch per 128 angles),
+    then one OS-EM iteration (15 subsets) of the n slices in one call.  ~0.3 GB on the device."""
+    import torch
+    import xct
+    from xct import phantom
+    ang = phantom.uniform_angles(PA)
+    ctx = xct.Context(0)
+    plan = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, 1, max_batch=n)
+    pars = phantom.ellipsoid_params(NX, NSLICES, 30, 2, mu=(0.005, 0.1))
+    img = torch.stack([phantom.ellipsoid_slice(pars, z, NX, NY, torch_device="cuda") for z in range(n)]).contiguous()
+    sino = torch.empty((n, PA, PX), device="cuda")
+    ms = plan.multislice()
+    plan.set_multislice(0)
+    plan.fwd(img, sino)
+    plan.set_multislice(ms if ms > 0 else 128)
+    x = torch.ones((n, NY, NX), device="cuda")
+    plan.run_device(sino, x, it=1)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "slices", "n": n, "multislice": plan.multislice(), "mean": float(x.mean())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -658,12 +681,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", nargs="?", const="osem", choices=["osem", "next"],
-                    help="run a small profiling case and exit: osem (one slice, one OS-EM iteration) or next "
+    ap.add_argument("--profile-case", nargs="?", const="osem", choices=["osem", "slices", "next"],
+                    help="run a small profiling case and exit: osem (one slice, one OS-EM iteration), slices "
+                         "(eight slices, one OS-EM iteration, slice-interleaved forward projector) or next "
                          "(the components either side of the path, each once)")
     args = ap.parse_args()
     if args.profile_case == "osem":
         profile_case()
+        return
+    if args.profile_case == "slices":
+        profile_case_slices()
         return
     if args.profile_case == "next":
         profile_case_next()

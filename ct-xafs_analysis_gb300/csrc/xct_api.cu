@@ -52,22 +52,22 @@ void xct_trig_table(const float *ang_deg, int pa, std::vector<float2> &cs)
 }
 
 // Subset order of OSEM_ocl (GPU.cpp:564-582): a power-of-two ss gives the bit-reversal
-// permutation (0, ss/2, ss/4, 3ss/4, ...); any other ss the identity.
+// permutation (0, ss/2, ss/4, 3ss/4, ...); any other ss the identity.  Entry k alone:
+int xct_subset_at(int ss, int k)
+{
+    if (ss <= 0 || (ss & (ss - 1)) != 0) return k;
+    int bits = 0;
+    while ((1 << bits) < ss) ++bits;
+    int r = 0;
+    for (int b = 0; b < bits; ++b)
+        if (k & (1 << b)) r |= 1 << (bits - 1 - b);
+    return r;
+}
+
+// ... and the whole order.
 void xct_subset_order_host(int ss, int *sub)
 {
-    if (ss <= 0) return;
-    if ((ss & (ss - 1)) == 0) {
-        int bits = 0;
-        while ((1 << bits) < ss) ++bits;
-        for (int j = 0; j < ss; ++j) {
-            int r = 0;
-            for (int b = 0; b < bits; ++b)
-                if (j & (1 << b)) r |= 1 << (bits - 1 - b);
-            sub[j] = r;
-        }
-    } else {
-        for (int j = 0; j < ss; ++j) sub[j] = j;
-    }
+    for (int j = 0; j < ss; ++j) sub[j] = xct_subset_at(ss, j);
 }
 
 extern "C" {
@@ -308,6 +308,17 @@ static inline int subset_rows(const xct_plan *p, int sub)
     return p->g.subset_mode == XCT_SUBSETS_COVER ? (pa - sub + ss - 1) / ss : pa / ss;
 }
 
+// First-half size of a batch that runs as two halves on two streams.  With the
+// slice-interleaved forward projector on, the cut falls on a multiple of its slice group, so
+// that each half keeps whole groups (10 slices: 8 | 2; 16: 8 | 8; 20: 8 | 12; 8: 8 | 0, no
+// split); otherwise in the middle.
+static int xct_osem_split(const xct_plan *p, int dN)
+{
+    const int G = fwd_ms_slices();
+    if (p->g.kernels == XCT_KERNELS_TILED && p->kg.ms_chunk > 0 && dN >= G) return G * ((dN / G + 1) / 2);
+    return (dN + 1) / 2;
+}
+
 // One subset step (OSEM1 then OSEM2) of dN slices with the given plan buffers (ratio
 // [dN][pa][px], accumulator [dN][rows][px]) on one stream.
 static int subset_step(xct_plan *p, int dN, const float *meas, float *d_img, float *ratio, double *acc, int s,
@@ -342,7 +353,8 @@ static int osem_loop_range(xct_plan *p, int dN, const float *meas, float *d_img,
 static int subset_step_split(xct_plan *p, int dN, const float *meas, float *d_img, int s, cudaStream_t st)
 {
     const KGeom &g = p->kg;
-    const int d0 = (dN + 1) / 2;
+    const int d0 = xct_osem_split(p, dN);
+    if (d0 >= dN) return subset_step(p, dN, meas, d_img, p->d_ratio, p->d_acc, s, st);
     const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
     double *acc1 = p->d_acc ? p->d_acc + (size_t)d0 * p->acc_rows * g.px : nullptr;
     XCT_CUDA_TRY(cudaEventRecord(p->ev_fork, st));
@@ -375,8 +387,8 @@ static int osem_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, con
         if (rc) return rc;
         meas = p->d_corr;
     }
-    if (dN < 2 || it == 0) return osem_loop_range(p, dN, meas, d_img, p->d_ratio, p->d_acc, sub, it, st);
-    const int d0 = (dN + 1) / 2, d1 = dN - d0;
+    const int d0 = xct_osem_split(p, dN), d1 = dN - d0;
+    if (dN < 2 || it == 0 || d1 == 0) return osem_loop_range(p, dN, meas, d_img, p->d_ratio, p->d_acc, sub, it, st);
     const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
     double *acc1 = p->d_acc ? p->d_acc + (size_t)d0 * p->acc_rows * g.px : nullptr;
     XCT_CUDA_TRY(cudaEventRecord(p->ev_fork, st));
@@ -485,11 +497,10 @@ int xct_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, 
 // kernels A, upload B (while A runs), kernels B, download A (while B runs), download B.
 // ev0..ev1 spans the first kernel to the later half's last (ev_fork, after its first use for
 // the fork, marks the end of A).
-static int host_run_split(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host,
+static int host_run_split(xct_plan *p, int dN, int d0, const float *const *sino_host, float *const *img_host,
                           bool upload_img, const std::function<int(int, int, cudaStream_t)> &run_half)
 {
     const size_t nimg = (size_t)p->g.nx * p->g.ny, nprj = (size_t)p->g.px * p->g.pa;
-    const int d0 = (dN + 1) / 2;
     const int first[2] = {0, d0}, count[2] = {d0, dN - d0};
     cudaStream_t sts[2] = {p->stream, p->s_aux};
     XCT_CUDA_TRY(cudaEventRecord(p->ev_fork, sts[0]));
@@ -542,7 +553,8 @@ static int osem_host_split(xct_plan *p, int dN, const float *const *sino_host, f
 {
     const KGeom &g = p->kg;
     const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
-    return host_run_split(p, dN, sino_host, img_host, true, [&](int first, int count, cudaStream_t st) {
+    return host_run_split(p, dN, xct_osem_split(p, dN), sino_host, img_host, true,
+                          [&](int first, int count, cudaStream_t st) {
         const float *meas = p->d_sino + first * nprj;
         if (p->g.correction_mode > 0) {
             const int r = launch_sino_correction(g, meas, p->d_corr + first * nprj, p->d_corr_ang, p->d_corr_bin,
@@ -880,7 +892,8 @@ int xct_fbp_run(xct_plan *p, int dN, int zp, const float *const *sino_host, floa
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
     if (dN >= 2) {  // halves with their own copies on two streams
         const size_t nimg = (size_t)p->g.nx * p->g.ny, nprj = (size_t)p->g.px * p->g.pa;
-        return host_run_split(p, dN, sino_host, img_host, false, [&](int first, int count, cudaStream_t st) {
+        return host_run_split(p, dN, (dN + 1) / 2, sino_host, img_host, false,
+                              [&](int first, int count, cudaStream_t st) {
             return fbp_device(p, count, zp, p->d_sino + first * nprj, p->d_img + first * nimg, false, nullptr, st,
                               first);
         });
@@ -900,7 +913,8 @@ int xct_hybrid_run(xct_plan *p, int dN, int zp, int baseup_order, const float *c
     if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
     if (dN >= 2)  // halves with their own copies on two streams
-        return host_run_split(p, dN, sino_host, img_host, false, [&](int first, int count, cudaStream_t st) {
+        return host_run_split(p, dN, (dN + 1) / 2, sino_host, img_host, false,
+                              [&](int first, int count, cudaStream_t st) {
             return hybrid_half(p, first, count, zp, baseup_order, sub, it, st);
         });
     return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {

@@ -22,6 +22,8 @@ struct KGeom {
     int fetch;       // XCT_FETCH_*
     int fwd_T;       // tiled forward projector: tile side (44, 60, 76, 92)
     int fwd_chunk;   // tiled forward projector: subset angles per CTA (1..128)
+    int ms_chunk = 0;  // slice-interleaved forward projector: subset angles per CTA (1..128);
+                       // 0 = off (groups of eight slices then use the per-slice kernel)
 };
 
 // One slice of a batched launch (device-side descriptor).
@@ -90,6 +92,7 @@ extern std::atomic<long long> g_xct_launches;
 // ---- host-side tables (identical to the oracle's) ----
 void xct_trig_table(const float *ang_deg, int pa, std::vector<float2> &cs);
 void xct_subset_order_host(int ss, int *sub);
+int xct_subset_at(int ss, int k);  // entry k of that order
 
 // ---- kernel launchers (xct_plain.cu / xct_tiled.cu / xct_misc.cu) ----
 // Forward projection of rows th = sub + k*step, k < nrows, for dN slices.
@@ -111,6 +114,12 @@ int launch_fwd_tiled(const KGeom &g, const float2 *trig, const float *img, const
 // The two halves of launch_fwd_tiled (timed separately by xct_osem_profile).
 int launch_fwd_tiled_main(const KGeom &g, const float2 *trig, const float *img, double *acc, int dN, int sub, int step,
                           int nrows, cudaStream_t st);
+// The slice-interleaved forward projector alone over groups x 8 slices (part of
+// launch_fwd_tiled_main when g.ms_chunk > 0); its slice group size and tile side.
+int launch_fwd_ms(const KGeom &g, const float2 *trig, const float *img, double *acc, int groups, int sub, int step,
+                  int nrows, int chunk, cudaStream_t st);
+int fwd_ms_slices();
+int fwd_ms_tile();
 int launch_fwd_finalize(const KGeom &g, const float *meas, float *out, double *acc, int dN, int sub, int step,
                         int nrows, cudaStream_t st);
 // Tiled OSEM2 backprojection + update, in place (same contract as the plain one).
@@ -146,6 +155,7 @@ int launch_base_up(const KGeom &g, float *img, int dN, int order, const int *min
 struct TuneChoice {
     int T, chunk;
     float ms;
+    int ms_chunk = 0;  // slice-interleaved forward projector's angle chunk; 0 = off
 };
 std::string xct_tune_key(const char *device, int nx, int ny, int px, int pa, int ss, int dN);
 bool xct_tune_lookup(const std::string &key, const char *path, TuneChoice &c);
@@ -183,6 +193,7 @@ enum {
     XCT_SITE_ADJ = 3,       // adjoint tile: shared accumulator element
     XCT_SITE_BP_WIN = 4,    // OS-EM backprojector: bin-window load (byte address)
     XCT_SITE_FBP_WIN = 5,   // FBP backprojector: bin-window load pair (byte address)
+    XCT_SITE_FWD_MS_TAP = 6,  // slice-interleaved forward tile: footprint load (byte address)
 };
 #ifdef XCT_CHECKED
 int xct_check_read_tiled(XctCheckWord *out, bool reset);

@@ -12,6 +12,13 @@
 // In host code the array's name is only a host-side stand-in for the symbol, not a device
 // address: its device address is fetched with cudaGetSymbolAddress once per device (with
 // that device current) on the first call made on that device, and passed to the kernels.
+// That address belongs to the device's current context: after a cudaDeviceReset the module
+// is loaded anew and the cached address is stale, so this entry point must not be used on a
+// device after it has been reset.
+//
+// The (cos, sin) table is uploaded on every call from a stack buffer (pageable memory), so a
+// call cannot be captured into a CUDA graph: a replay would read a stack buffer that no
+// longer exists.  Calls made while the stream is capturing are rejected.
 #include <math.h>
 #include <stdio.h>
 
@@ -43,24 +50,12 @@ int scratch_address(int dev, unsigned char **out)
     return XCT_OK;
 }
 
-// Entry k of the subset order of OSEM_ocl (CT_reconstruction/GPU.cpp:564-582), computed
-// directly: bit reversal of k for a power-of-two ss, k otherwise.
-int subset_at(int ss, int k)
-{
-    if ((ss & (ss - 1)) != 0) return k;
-    int bits = 0;
-    while ((1 << bits) < ss) ++bits;
-    int r = 0;
-    for (int b = 0; b < bits; ++b)
-        if (k & (1 << b)) r |= 1 << (bits - 1 - b);
-    return r;
-}
-
 }  // namespace
 
 extern "C" int xct_osem_run_static(const xct_geom *g, int dN, const float *d_sino, float *d_img, const int *sub,
                                    int it, void *stream)
 {
+    XCT_RANGE("xct_osem_run_static");
     if (!g || !d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_osem_run_static: null argument");
     if (g->nx <= 0 || g->ny <= 0 || g->px <= 0 || g->pa <= 0 || g->ss <= 0 || g->ss > g->pa || !g->angles_deg)
         return xct_fail(XCT_E_INVALID, "xct_osem_run_static: invalid geometry");
@@ -100,6 +95,17 @@ extern "C" int xct_osem_run_static(const xct_geom *g, int dN, const float *d_sin
         return xct_fail(XCT_E_INVALID, b);
     }
 
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
+    // the per-call pageable upload of the angle table cannot be replayed from a graph
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t ce = cudaStreamIsCapturing(st, &cap);
+    if (ce != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        if (ce != cudaSuccess) (void)cudaGetLastError();  // not a sticky error: clear it
+        return xct_fail(XCT_E_UNSUPPORTED,
+                        "xct_osem_run_static: the stream is being captured; this entry point uploads its angle table "
+                        "from host memory on every call and cannot be captured into a CUDA graph (use a plan)");
+    }
+
     int dev = 0;
     XCT_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return xct_fail(XCT_E_INVALID, "xct_osem_run_static: device index too large");
@@ -109,8 +115,6 @@ extern "C" int xct_osem_run_static(const xct_geom *g, int dN, const float *d_sin
     float2 *d_trig = reinterpret_cast<float2 *>(base);
     double *d_acc = reinterpret_cast<double *>(base + trig_bytes);
     float *d_ratio = reinterpret_cast<float *>(base + trig_bytes + acc_bytes);
-    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
-
     // (cos, sin) table, computed exactly as for a plan, staged through a small stack buffer
     // (a pageable copy returns once the source has been read)
     float2 chunk[256];
@@ -145,7 +149,7 @@ extern "C" int xct_osem_run_static(const xct_geom *g, int dN, const float *d_sin
 
     for (int i = 0; i < it; ++i)
         for (int kk = 0; kk < g->ss; ++kk) {
-            const int s = sub ? sub[kk] : subset_at(g->ss, kk);
+            const int s = sub ? sub[kk] : xct_subset_at(g->ss, kk);
             const int nrows = g->subset_mode == XCT_SUBSETS_COVER ? (g->pa - s + g->ss - 1) / g->ss : g->pa / g->ss;
             rc = launch_fwd_tiled(k, d_trig, d_img, d_sino, d_ratio, d_acc, dN, s, g->ss, nrows, st);
             if (rc) return rc;

@@ -289,6 +289,231 @@ __global__ void __launch_bounds__(kFwdThreads, FwdTile<T>::MinBlocks) fwd_tiled_
                 (int)blockIdx.x % ntx, (int)blockIdx.x / ntx, (int)blockIdx.y * g.fwd_chunk, g.fwd_chunk, smem_raw);
 }
 
+// ------------------------------------------- forward projector, eight slices per tile
+// For a batch of slices of one geometry (the reference's dN image-array layers, OSEM1 over
+// global size (px, pa/ss, dN)), eight slices share every sample position.  A CTA of 16 warps
+// owns a T x T tile of base texels of eight slices; shared memory holds, per base texel, one
+// 16-byte element per slice -- (t00, t10 - t00, t01 - t00, (t11 - t01) - (t10 - t00)), the
+// whole 2x2 footprint -- and a texel's eight elements are one 128-byte record.  A warp takes
+// four rays of one angle, a quarter-warp (eight lanes) per ray, lane p of a quarter taking
+// every eighth sample from phase p.  For each sample a lane finds the coordinates, floor and
+// record once and then reads the eight slices' elements starting at slot p and wrapping, so
+// at every load the quarter's eight lanes read eight different 16-byte bank groups: no load
+// has a bank conflict whatever the geometry, the coordinate work is spread over eight
+// slice-samples, and a quarter whose ray is done costs no shared-memory wavefronts.  Slot r
+// of lane p accumulates slice (r + p) mod 8; eight shuffles give lane p the quarter's total
+// for slice p, which it adds to the double accumulator with one atomic.  Work items (angle,
+// four rays) are taken from a shared counter, so warps finish within one item of each other.
+constexpr int kMsSlices = 8;
+constexpr int kMsThreads = 512;
+constexpr int kMsRays = 32 / kMsSlices;  // rays per warp (one per quarter-warp)
+constexpr int kMsTile = 42;              // base texels per tile side: 42^2 x 128 B = 221 KB
+
+template <int T>
+struct FwdMsTile {
+    static constexpr size_t TileBytes = (size_t)T * T * kMsSlices * sizeof(float4);
+    // per chunk angle: (c, s), (1/c, 1/s), first and last ray, ray-group prefix; then the
+    // group total and the work counter
+    static constexpr size_t Smem = TileBytes + (size_t)kAngChunk * (2 * sizeof(float2) + 3 * sizeof(int)) + 16;
+    static_assert(Smem <= 227u * 1024u, "eight-slice tile exceeds shared memory");
+};
+
+__device__ __forceinline__ float4 lds_f4(unsigned addr)
+{
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+    return v;
+}
+
+// float -> double for the accumulator without the FP64 pipe (GB300 runs FP64 at a small
+// fraction of the FP32 rate): normal numbers and zero by re-biasing the exponent in integer
+// arithmetic, the rare others through the conversion instruction.
+__device__ __forceinline__ double f32_to_f64(float v)
+{
+    const unsigned u = __float_as_uint(v);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e - 1u < 254u) {
+        const unsigned hi = (u & 0x80000000u) | ((e + (1023u - 127u)) << 20) | ((u >> 3) & 0xfffffu);
+        return __hiloint2double((int)hi, (int)(u << 29));
+    }
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)v;
+}
+
+// grid: (ntx*nty tiles, angle chunks, dN / 8 slice groups); acc [dN][nrows][px] doubles.
+template <int T>
+__global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__restrict__ img,
+                                                               double *__restrict__ acc,
+                                                               const float2 *__restrict__ trig, KGeom g, int sub,
+                                                               int step, int nrows, int ntx, int chunk)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float4 *tile = reinterpret_cast<float4 *>(smem_raw);
+    float2 *scs = reinterpret_cast<float2 *>(smem_raw + FwdMsTile<T>::TileBytes);
+    float2 *inv_s = scs + kAngChunk;
+    int *xlo_s = reinterpret_cast<int *>(inv_s + kAngChunk);
+    int *xhi_s = xlo_s + kAngChunk;
+    int *gpre = xhi_s + kAngChunk;
+    int *tail = gpre + kAngChunk;  // [0] ray groups of the chunk, [1] work counter
+    const int k0 = (int)blockIdx.y * chunk;
+    const int kn = min(chunk, nrows - k0);
+    if (kn <= 0) return;
+    const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
+    const int x0 = -1 + bx * T, y0 = -1 + by * T;
+    const int z0 = (int)blockIdx.z * kMsSlices;
+    const size_t nimg = (size_t)g.nx * g.ny;
+    const float *im0 = img + (size_t)z0 * nimg;
+
+    // element (c, r) of slice z at tile[(r*T + c)*8 + z]; texels outside the image are 0
+    for (int i = threadIdx.x; i < T * T * kMsSlices; i += kMsThreads) {
+        const int z = i & (kMsSlices - 1), e = i >> 3;
+        const int r = e / T, c = e - r * T;
+        const int gx = x0 + c, gy = y0 + r;
+        const float *im = im0 + (size_t)z * nimg;
+        const bool c0 = (unsigned)gx < (unsigned)g.nx, c1 = (unsigned)(gx + 1) < (unsigned)g.nx;
+        const bool r0 = (unsigned)gy < (unsigned)g.ny, r1 = (unsigned)(gy + 1) < (unsigned)g.ny;
+        const long long o = (long long)gy * g.nx + gx;
+        const float t00 = (r0 && c0) ? __ldg(im + o) : 0.0f;
+        const float t10 = (r0 && c1) ? __ldg(im + o + 1) : 0.0f;
+        const float t01 = (r1 && c0) ? __ldg(im + o + g.nx) : 0.0f;
+        const float t11 = (r1 && c1) ? __ldg(im + o + g.nx + 1) : 0.0f;
+        const float d0 = t10 - t00, d1 = t11 - t01;
+        tile[i] = make_float4(t00, d0, t01 - t00, d1 - d0);
+    }
+    // owned base-texel ranges (the union over tiles is [-1, n-1])
+    const float xlo = (float)x0, xhi = (float)min(x0 + T, g.nx);
+    const float ylo = (float)y0, yhi = (float)min(y0 + T, g.ny);
+    for (int k = threadIdx.x; k < kn; k += kMsThreads) {
+        const float2 cs = trig[sub + (k0 + k) * step];
+        scs[k] = cs;
+        inv_s[k] = make_float2(1.0f / cs.x, 1.0f / cs.y);
+        // rays that can reach the tile: the (expanded) tile corners on the detector axis
+        float pmin = 3.0e38f, pmax = -3.0e38f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float px_ = (q & 1) ? xhi + 2.0f : xlo - 2.0f;
+            const float py_ = (q & 2) ? yhi + 2.0f : ylo - 2.0f;
+            const float p = (px_ - g.hx) * cs.x - (py_ - g.hy) * cs.y + g.cx;
+            pmin = fminf(pmin, p);
+            pmax = fmaxf(pmax, p);
+        }
+        xlo_s[k] = max(0, (int)floorf(pmin) - 1);
+        xhi_s[k] = min(g.px - 1, (int)ceilf(pmax) + 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive prefix of the ray groups per angle (warp 0)
+        const int lane = threadIdx.x;
+        int carry = 0;
+        for (int b = 0; b < kn; b += 32) {
+            const int k = b + lane;
+            const int n = k < kn ? max(0, (xhi_s[k] - xlo_s[k] + kMsRays) / kMsRays) : 0;
+            int v = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += t;
+            }
+            if (k < kn) gpre[k] = carry + v - n;
+            carry += __shfl_sync(0xffffffffu, v, 31);
+        }
+        if (lane == 0) {
+            tail[0] = carry;
+            tail[1] = 0;
+        }
+    }
+    __syncthreads();
+
+    const int total = tail[0];
+    const int lane = threadIdx.x & 31;
+    const int ph = lane & (kMsSlices - 1);  // sample phase; also this lane's first slot
+    const int qb = lane & ~(kMsSlices - 1);  // first lane of the quarter
+    const int ray = lane >> 3;               // ray of the warp's four
+    const int D = g.depth;
+    // byte address of the record of base texel (col, row) from the floor bits:
+    // (iy_bits * T + ix_bits) * 128 + base2, the biases folded into base2 (mod 2^32)
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(tile);
+    const unsigned bias = (unsigned)XCT_FLOOR_BIAS;
+    const unsigned base2 =
+        sbase - ((bias + (unsigned)y0) * (unsigned)T + bias + (unsigned)x0) * (unsigned)(kMsSlices * 16);
+    const unsigned alo = sbase, ahi = sbase + (unsigned)((T * T - 1) * kMsSlices * 16);
+    // slot r of this lane holds slice (r + ph) mod 8, read at byte offset 16 * that
+    unsigned off[kMsSlices];
+#pragma unroll
+    for (int r = 0; r < kMsSlices; ++r) off[r] = 16u * (unsigned)((r + ph) & (kMsSlices - 1));
+    const f2x MM = f2_pack(kMagic, kMagic);
+    const f2x step2 = f2_pack((float)kMsSlices, (float)kMsSlices);
+    // lanes 0..3 of a quarter find the ray's interval limits: the lower (even) or upper (odd)
+    // Y limit from the x (0, 1) or the y coordinate (2, 3)
+    const bool bound_x = ph < 2;
+    const bool upper = (ph & 1) != 0;
+    int *counter = tail + 1;
+    int k = 0;  // the warp's current angle: items only grow, so the search runs forward
+
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(counter, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        while (k + 1 < kn && gpre[k + 1] <= item) ++k;  // the last k with gpre[k] <= item
+        const float c = scs[k].x, s = scs[k].y;
+        const int X = xlo_s[k] + (item - gpre[k]) * kMsRays + ray;
+        const bool live = X <= xhi_s[k];
+        const float Xc = (float)X - g.cx;
+        const float ax = fmaf(Xc, c, g.hx);
+        const float ay = fmaf(Xc, -s, g.hy);
+        int v = 0;
+        if (live && ph < 4) {
+            const float a = bound_x ? ax : ay, sl = bound_x ? s : c;
+            const float isl = bound_x ? inv_s[k].y : inv_s[k].x;
+            const float lo_ = bound_x ? xlo : ylo, hi_ = bound_x ? xhi : yhi;
+            if (sl != 0.0f) {
+                // sl > 0: [first(u >= lo), first(u >= hi)); sl < 0: [first(u < hi), first(u < lo))
+                const float b = ((sl > 0.0f) != upper) ? lo_ : hi_;
+                v = first_true(b, a, sl, isl, g.hd, D);
+            } else {  // constant coordinate: all samples or none
+                v = upper ? ((a >= lo_ && a < hi_) ? D : 0) : 0;
+            }
+        }
+        const int v0 = __shfl_sync(0xffffffffu, v, qb + 0), v1 = __shfl_sync(0xffffffffu, v, qb + 1);
+        const int v2 = __shfl_sync(0xffffffffu, v, qb + 2), v3 = __shfl_sync(0xffffffffu, v, qb + 3);
+        const int ya = max(v0, v2), yb = min(v1, v3);
+        const int n = (live && yb - ya > ph) ? (yb - ya - ph + kMsSlices - 1) / kMsSlices : 0;
+        const float yc0 = (float)(ya + ph) - g.hd;
+        f2x yc2 = f2_pack(yc0, yc0);
+        const f2x sc = f2_pack(s, c);
+        const f2x axy = f2_pack(ax, ay);
+        float sum[kMsSlices];
+#pragma unroll
+        for (int r = 0; r < kMsSlices; ++r) sum[r] = 0.0f;
+        for (int i = 0; i < n; ++i) {
+            const f2x xy = f2_fma(yc2, sc, axy);
+            const f2x tb = f2_add_rd(xy, MM);
+            const f2x fr = f2_sub(xy, f2_sub(tb, MM));
+            yc2 = f2_add(yc2, step2);
+            int ixb, iyb;
+            f2_unpack_bits(tb, ixb, iyb);
+            float fx, fy;
+            f2_unpack(fr, fx, fy);
+            const unsigned rec = ((unsigned)iyb * (unsigned)T + (unsigned)ixb) * (unsigned)(kMsSlices * 16) + base2;
+            if (!XCT_IN(rec, alo, ahi, XCT_SITE_FWD_MS_TAP)) continue;
+#pragma unroll
+            for (int r = 0; r < kMsSlices; ++r) {
+                const float4 e = lds_f4(rec + off[r]);
+                sum[r] += fmaf(fy, fmaf(fx, e.w, e.z), fmaf(fx, e.y, e.x));
+            }
+        }
+        // lane p's slot d holds slice (d + p) mod 8: lane p gathers slice p's partial sums from
+        // lanes (p - d) mod 8 of its quarter, slot d
+        float tot = 0.0f;
+#pragma unroll
+        for (int d = 0; d < kMsSlices; ++d)
+            tot += __shfl_sync(0xffffffffu, sum[d], qb + ((ph - d) & (kMsSlices - 1)));
+        if (live && yb > ya &&
+            XCT_IN((long long)k * g.px + X, 0, (long long)(nrows - k0) * g.px - 1, XCT_SITE_FWD_ACC))
+            atomicAdd(acc + ((size_t)(z0 + ph) * nrows + k0 + k) * g.px + X, f32_to_f64(tot));
+    }
+}
+
 // ------------------------------------------------------------------- exact adjoint
 // A^T of the forward projector: img[t] = sum over samples of w_t(sample) * sino[th][X], with
 // the bilinear weights w00 = (1-fx)(1-fy), w10 = fx(1-fy), w01 = (1-fx)fy, w11 = fx fy of the
@@ -753,14 +978,18 @@ __global__ void __launch_bounds__(BpCfg<4>::Threads) bp_batched_kernel(const Xct
 // ---------------------------------------------------------------- tile-size dispatch
 bool xct_fwd_tile_valid(int T) { return T == 44 || T == 60 || T == 76 || T == 92; }
 
+// Raises a kernel's dynamic shared-memory limit once per device.  Host threads may race on
+// the first call of a device: the flags are atomic, and setting the attribute twice is
+// harmless.  Devices beyond the table set it on every call.
 template <int T>
-static int fwd_smem_attr(const void *fn, bool *done)
+static int fwd_smem_attr(const void *fn, std::atomic<bool> *done)
 {
     int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !done[dev]) {
+    XCT_CUDA_TRY(cudaGetDevice(&dev));
+    const bool cached = dev >= 0 && dev < 64;
+    if (!cached || !done[dev].load(std::memory_order_acquire)) {
         XCT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FwdTile<T>::Smem));
-        done[dev] = true;
+        if (cached) done[dev].store(true, std::memory_order_release);
     }
     return XCT_OK;
 }
@@ -796,7 +1025,7 @@ int xct_batched_grids(int device, int sm_count, int fwd_T, int grids[3])
     int a = 0, c = 0;
     int rc = with_tile(fwd_T, [&](auto tc) -> int {
         constexpr int T = decltype(tc)::value;
-        static bool done[64] = {};
+        static std::atomic<bool> done[64];
         int r = fwd_smem_attr<T>((const void *)fwd_batched_kernel<T>, done);
         if (r) return r;
         XCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fwd_batched_kernel<T>, kFwdThreads,
@@ -844,14 +1073,54 @@ int launch_fwd_batched(const XctItemDev *items, const int *bases, int n, int sub
 
 int fwd_tiled_rows_cap() { return kAngChunk; }
 
+int fwd_ms_slices() { return kMsSlices; }
+int fwd_ms_tile() { return kMsTile; }
+
+// The slice-interleaved forward projector over groups*8 slices (slice-group g of the grid is
+// slices 8g .. 8g+7 of img / acc).
+int launch_fwd_ms(const KGeom &g, const float2 *trig, const float *img, double *acc, int groups, int sub, int step,
+                  int nrows, int chunk, cudaStream_t st)
+{
+    if (nrows <= 0 || groups <= 0) return XCT_OK;
+    if (chunk <= 0 || chunk > kAngChunk) return xct_fail(XCT_E_INVALID, "slice-interleaved angle chunk out of range");
+    constexpr int T = kMsTile;
+    static std::atomic<bool> done[64];
+    int dev = 0;
+    XCT_CUDA_TRY(cudaGetDevice(&dev));
+    const bool cached = dev >= 0 && dev < 64;
+    if (!cached || !done[dev].load(std::memory_order_acquire)) {
+        XCT_CUDA_TRY(cudaFuncSetAttribute((const void *)fwd_ms_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)FwdMsTile<T>::Smem));
+        if (cached) done[dev].store(true, std::memory_order_release);
+    }
+    const int ntx = (g.nx + 1 + T - 1) / T, nty = (g.ny + 1 + T - 1) / T;
+    const int nch = (nrows + chunk - 1) / chunk;
+    dim3 grid(ntx * nty, nch, groups);
+    fwd_ms_kernel<T><<<grid, kMsThreads, FwdMsTile<T>::Smem, st>>>(img, acc, trig, g, sub, step, nrows, ntx, chunk);
+    g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+    XCT_CUDA_TRY(cudaGetLastError());
+    return XCT_OK;
+}
+
+// The forward projection of dN slices into the accumulator: with the slice-interleaved
+// kernel enabled (g.ms_chunk > 0), its groups of eight slices first, then the rest with the
+// per-slice tiled kernel.
 int launch_fwd_tiled_main(const KGeom &g, const float2 *trig, const float *img, double *acc, int dN, int sub, int step,
                           int nrows, cudaStream_t st)
 {
     if (nrows <= 0 || dN <= 0) return XCT_OK;
+    const int ms = g.ms_chunk > 0 ? (dN / kMsSlices) * kMsSlices : 0;
+    if (ms > 0) {
+        const int rc = launch_fwd_ms(g, trig, img, acc, ms / kMsSlices, sub, step, nrows, g.ms_chunk, st);
+        if (rc || ms == dN) return rc;
+        img += (size_t)ms * g.nx * g.ny;
+        acc += (size_t)ms * nrows * g.px;
+        dN -= ms;
+    }
     if (g.fwd_chunk <= 0 || g.fwd_chunk > kAngChunk) return xct_fail(XCT_E_INVALID, "forward angle chunk out of range");
     return with_tile(g.fwd_T, [&](auto tc) -> int {
         constexpr int T = decltype(tc)::value;
-        static bool done[64] = {};
+        static std::atomic<bool> done[64];
         int r = fwd_smem_attr<T>((const void *)fwd_tiled_kernel<T>, done);
         if (r) return r;
         const int ntx = (g.nx + 1 + T - 1) / T;  // base texels -1 .. nx-1

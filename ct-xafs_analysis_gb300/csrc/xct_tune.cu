@@ -165,14 +165,29 @@ static long long plan_ctas(const xct_plan *p, int dN, int T, int c)
     return (long long)((p->g.nx + T) / T) * ((p->g.ny + T) / T) * ((rows + c - 1) / c) * dN;
 }
 
+// The slice-interleaved forward projector by default: on (all subset angles per CTA) when a
+// plan's full batch holds a group of eight slices whose tiles give at least two waves of
+// CTAs (one per SM); smaller problems keep the per-slice kernel, whose smaller CTAs fill
+// the SMs better.
+static int plan_default_ms_chunk(const xct_plan *p)
+{
+    const int G = fwd_ms_slices(), T = fwd_ms_tile();
+    if (p->g.kernels != XCT_KERNELS_TILED || p->g.max_batch < G) return 0;
+    const long long tiles = (long long)((p->g.nx + T) / T) * ((p->g.ny + T) / T);
+    return tiles * (p->g.max_batch / G) >= 2LL * p->ctx->sm_count ? fwd_tiled_rows_cap() : 0;
+}
+
 void xct_plan_default_tuning(xct_plan *p)
 {
     TuneChoice c;
     const std::string key = xct_tune_key(p->ctx->name, p->g.nx, p->g.ny, p->g.px, p->g.pa, p->g.ss, p->g.max_batch);
-    if (!xct_tune_lookup(key, xct_tune_env_path(), c))
+    if (!xct_tune_lookup(key, xct_tune_env_path(), c)) {
         c = xct_tune_default(p->ctx->sm_count, [&](int T, int ch) { return plan_ctas(p, p->g.max_batch, T, ch); });
+        c.ms_chunk = plan_default_ms_chunk(p);
+    }
     p->kg.fwd_T = c.T;
     p->kg.fwd_chunk = c.chunk;
+    p->kg.ms_chunk = c.ms_chunk;
 }
 
 extern "C" {
@@ -193,6 +208,24 @@ int xct_plan_set_tuning(xct_plan *p, int fwd_tile, int ang_chunk)
         return xct_fail(XCT_E_INVALID, "ang_chunk must be in 1..128");
     p->kg.fwd_T = fwd_tile;
     p->kg.fwd_chunk = ang_chunk;
+    return XCT_OK;
+}
+
+int xct_plan_multislice(xct_plan *p, int *ang_chunk)
+{
+    if (!p || !ang_chunk) return xct_fail(XCT_E_INVALID, "xct_plan_multislice: null argument");
+    *ang_chunk = p->kg.ms_chunk;
+    return XCT_OK;
+}
+
+int xct_plan_set_multislice(xct_plan *p, int ang_chunk)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "xct_plan_set_multislice: plan is null");
+    if (ang_chunk < 0 || ang_chunk > fwd_tiled_rows_cap())
+        return xct_fail(XCT_E_INVALID, "xct_plan_set_multislice: ang_chunk must be 0 (off) or in 1..128");
+    if (ang_chunk > 0 && p->g.kernels != XCT_KERNELS_TILED)
+        return xct_fail(XCT_E_UNSUPPORTED, "xct_plan_set_multislice: the plain kernels have no slice-interleaved form");
+    p->kg.ms_chunk = ang_chunk;
     return XCT_OK;
 }
 

@@ -52,6 +52,7 @@ EXPORTS = (
     "xct_check_report", "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_reslice_plan_set_wait_limit",
     "xct_denoise_sinogram",
     "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
+    "xct_plan_multislice", "xct_plan_set_multislice",
     "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume", "xct_hybrid_cs_run_device",
     "xct_hybrid_cs_run",
 )
@@ -147,6 +148,8 @@ def load():
     L.xct_plan_autotune.argtypes = [vp, ip, ctypes.c_char_p, ip, vp]
     L.xct_plan_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.xct_plan_set_tuning.argtypes = [vp, ip, ip]
+    L.xct_plan_multislice.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    L.xct_plan_set_multislice.argtypes = [vp, ip]
     L.xct_batch_plan_autotune.argtypes = [vp, ctypes.c_char_p, ip, vp]
     L.xct_batch_plan_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.xct_plan_sync.argtypes = [vp]
@@ -512,6 +515,17 @@ class OSEMPlan:
 
     def set_tuning(self, fwd_tile, ang_chunk):
         _check(self._lib.xct_plan_set_tuning(self.handle, fwd_tile, ang_chunk))
+
+    def multislice(self):
+        """Angle chunk of the slice-interleaved forward projector (0 = off)."""
+        v = ctypes.c_int()
+        _check(self._lib.xct_plan_multislice(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def set_multislice(self, ang_chunk):
+        """Turn the slice-interleaved forward projector on (subset angles per CTA, 1..128) or
+        off (0) for calls of eight or more slices."""
+        _check(self._lib.xct_plan_set_multislice(self.handle, int(ang_chunk)))
 
     def profile(self, d_sino, d_img, dN=None, sub=None, it=-1, stream=None):
         """Run OS-EM with CUDA events around every launch; returns a dict of summed device

@@ -149,8 +149,12 @@ int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, const float
  *     XCT_E_INVALID with the byte counts in the message.  Sinogram correction modes are not
  *     available here (XCT_E_UNSUPPORTED).
  *   - Runs on the CURRENT device.  The first call on a device looks up the array's device
- *     address (cudaGetSymbolAddress) for that device; make that first call before any
- *     stream capture.
+ *     address (cudaGetSymbolAddress) for that device and keeps it; after a cudaDeviceReset
+ *     of that device the kept address is stale, so do not use this entry point on a device
+ *     that has been reset.
+ *   - Cannot be captured into a CUDA graph: every call uploads its angle table from host
+ *     memory on the stack, which a replay could not read.  A call on a stream that is being
+ *     captured returns XCT_E_UNSUPPORTED and enqueues nothing.
  *   - Every call uses the same array and it keeps the last call's contents (each call clears
  *     what must start at zero).  Calls whose GPU work overlaps -- on different streams or
  *     host threads -- race on the array and give wrong results: serialise them.
@@ -344,6 +348,21 @@ int xct_plan_tuning(xct_plan *plan, int *fwd_tile, int *ang_chunk);
 int xct_plan_set_tuning(xct_plan *plan, int fwd_tile, int ang_chunk);
 int xct_batch_plan_autotune(xct_batch_plan *plan, const char *cache_path, int flags, void *stream);
 int xct_batch_plan_tuning(xct_batch_plan *plan, int *fwd_tile, int *ang_chunk);
+
+/* ---- slice-interleaved forward projector -------------------------------------------------
+ * No counterpart in the reference (its OSEM1 work-items each sum one ray of one slice).  The
+ * slices of one OS-EM call share their geometry, so a plan can forward-project them in
+ * groups of eight: a CTA stages one tile of eight slices, and the eight lanes of each
+ * quarter-warp take the same sample of one ray in the eight slices (one shared-memory line,
+ * no bank conflict; the ray's interval and coordinates are found once for all eight).  With
+ * it on, a call's slices go in groups of eight through it and the rest through the per-slice
+ * tiled kernel, and a call that runs as two halves cuts them at a multiple of eight.  The
+ * value is the number of subset angles one CTA serves (1..128); 0 turns it off.  Plans start
+ * with the cached or autotuned choice, else on (128) when max_batch >= 8 and the tiles of one
+ * group give at least two CTAs per SM.  Results agree with the per-slice kernel to float
+ * rounding of the partial ray sums. */
+int xct_plan_multislice(xct_plan *plan, int *ang_chunk);
+int xct_plan_set_multislice(xct_plan *plan, int ang_chunk);
 
 /* FP32 FMA throughput of a device (TFLOP/s), measured by a dependent-chain-free FMA
  * kernel: the roofline denominator for the projectors. */

@@ -23,7 +23,8 @@ import subprocess
 import hashlib
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("XCT_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: XCT_REFERENCE_ROOT, else a sibling directory "reference" of the repository
+REF_ROOT = os.environ.get("XCT_REFERENCE_ROOT") or os.path.join(os.path.dirname(HERE), "..", "reference")
 OUT = os.path.join(HERE, "_ref")
 KERNELS = ("CT_reconstruction/FBP.cl", "CT_reconstruction/OSEM.cl", "CT_reconstruction/FISTA.cl",
            "CT_reconstruction/reconstShare.cl")

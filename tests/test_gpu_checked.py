@@ -1,6 +1,6 @@
 """The bounds-checked build (libxct_checked.so, -DXCT_CHECKED): every shared-memory access
 whose address the kernels derive from geometry -- the forward tile's footprint loads and
-accumulator rows, the adjoint's shared accumulator, the OS-EM and FBP backprojectors' bin
+accumulator rows (per-slice and slice-interleaved tiles), the adjoint's shared accumulator, the OS-EM and FBP backprojectors' bin
 windows -- is tested against its buffer.  A child process runs those kernels through the
 checked library on awkward shapes (every forward tile size, odd sizes, an off-centre
 rotation axis, a 360-degree scan, batched mixed shapes) and must report no skipped access;
@@ -54,6 +54,18 @@ for ci, (nx, ny, px, pa, ss, span, off) in enumerate(CASES):
     plan.fbp_backproject(y, f)
     out["fbpbp_%%d" %% ci] = f.cpu().numpy()
     plan.close()
+    # the slice-interleaved forward projector: nine slices (a group of eight, then one)
+    plan9 = xct.OSEMPlan(ctx, nx, ny, px, ang, ss, 2, center_bin=px * 0.5 + off, max_batch=9)
+    img9 = torch.cat([img * (1.0 + 0.1 * j) for j in range(9)]).contiguous()
+    for chunk in (16, 128):
+        plan9.set_multislice(chunk)
+        s9 = torch.empty((9, pa, px), device="cuda")
+        plan9.fwd(img9, s9)
+        out["msfwd_%%d_%%d" %% (ci, chunk)] = s9.cpu().numpy()
+        x = torch.ones((9, ny, nx), device="cuda")
+        plan9.run_device(s9, x)
+        out["msosem_%%d_%%d" %% (ci, chunk)] = x.cpu().numpy()
+    plan9.close()
 # batched mixed shapes
 geoms, sinos, imgs = [], [], []
 for ci, (nx, ny, px, pa, ss, span, off) in enumerate(CASES):
