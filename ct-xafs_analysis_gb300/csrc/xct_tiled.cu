@@ -295,19 +295,23 @@ __global__ void __launch_bounds__(kFwdThreads, FwdTile<T>::MinBlocks) fwd_tiled_
 // owns a T x T tile of base texels of eight slices; shared memory holds, per base texel, one
 // 16-byte element per slice -- (t00, t10 - t00, t01 - t00, (t11 - t01) - (t10 - t00)), the
 // whole 2x2 footprint -- and a texel's eight elements are one 128-byte record.  A warp takes
-// four rays of one angle, a quarter-warp (eight lanes) per ray, lane p of a quarter taking
-// every eighth sample from phase p.  For each sample a lane finds the coordinates, floor and
+// eight rays of one angle, a quarter-warp (eight lanes) per pair of consecutive rays A, B:
+// the pair's samples form one stream (A's interval in the tile, then B's), lane p taking
+// stream positions p, p + 8, ...  For each sample a lane finds the coordinates, floor and
 // record once and then reads the eight slices' elements starting at slot p and wrapping, so
 // at every load the quarter's eight lanes read eight different 16-byte bank groups: no load
 // has a bank conflict whatever the geometry, the coordinate work is spread over eight
-// slice-samples, and a quarter whose ray is done costs no shared-memory wavefronts.  Slot r
-// of lane p accumulates slice (r + p) mod 8; eight shuffles give lane p the quarter's total
-// for slice p, which it adds to the double accumulator with one atomic.  Work items (angle,
-// four rays) are taken from a shared counter, so warps finish within one item of each other.
+// slice-samples, a quarter whose stream is done costs no shared-memory wavefronts, and only
+// the stream's last pass leaves lanes idle (one pass per two rays).  Slot r of lane p
+// accumulates slice (r + p) mod 8, separately for A and B; eight shuffles give lane p the
+// quarter's totals for slice p, which it adds to the double accumulator with one atomic per
+// ray.  Work items (angle, eight rays) are taken from a shared counter, so warps finish
+// within one item of each other.
 constexpr int kMsSlices = 8;
 constexpr int kMsThreads = 512;
-constexpr int kMsRays = 32 / kMsSlices;  // rays per warp (one per quarter-warp)
+constexpr int kMsRays = 2 * 32 / kMsSlices;  // rays per warp (a pair per quarter-warp)
 constexpr int kMsTile = 42;              // base texels per tile side: 42^2 x 128 B = 221 KB
+constexpr int kMsStageRows = 6;          // element rows per staging strip
 
 template <int T>
 struct FwdMsTile {
@@ -340,6 +344,49 @@ __device__ __forceinline__ double f32_to_f64(float v)
     return (double)v;
 }
 
+// Pass i of a quarter's ray-pair stream for lane ph: the sample (stream position 8i + ph,
+// of ray A below LA), its fractions and the byte address of its base texel's record.
+__device__ __forceinline__ unsigned ms_locate(int i, int ph, int LA, float ycA, float ycB, f2x sc, f2x axyA,
+                                              f2x axyB, f2x MM, unsigned base2, int T, float &fx, float &fy,
+                                              bool &onA)
+{
+    onA = kMsSlices * i + ph < LA;
+    const float yc = (onA ? ycA : ycB) + (float)(kMsSlices * i);
+    const f2x xy = f2_fma(f2_pack(yc, yc), sc, onA ? axyA : axyB);
+    const f2x tb = f2_add_rd(xy, MM);
+    const f2x fr = f2_sub(xy, f2_sub(tb, MM));
+    int ixb, iyb;
+    f2_unpack_bits(tb, ixb, iyb);
+    f2_unpack(fr, fx, fy);
+    return ((unsigned)iyb * (unsigned)T + (unsigned)ixb) * (unsigned)(kMsSlices * 16) + base2;
+}
+
+// The eight slices' elements of one record, slot r from byte offset off[r].
+__device__ __forceinline__ void ms_load(float4 (&e)[kMsSlices], unsigned rec, const unsigned (&off)[kMsSlices],
+                                        unsigned alo, unsigned ahi)
+{
+    if (!XCT_IN(rec, alo, ahi, XCT_SITE_FWD_MS_TAP)) {
+#pragma unroll
+        for (int r = 0; r < kMsSlices; ++r) e[r] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < kMsSlices; ++r) e[r] = lds_f4(rec + off[r]);
+}
+
+// The bilinear values of one record's eight slices, added to ray A's or B's slot sums
+// (predicated adds: a non-finite sample stays in its own ray).
+__device__ __forceinline__ void ms_accumulate(const float4 (&e)[kMsSlices], float fx, float fy, bool onA,
+                                              float (&sumA)[kMsSlices], float (&sumB)[kMsSlices])
+{
+#pragma unroll
+    for (int r = 0; r < kMsSlices; ++r) {
+        const float val = fmaf(fy, fmaf(fx, e[r].w, e[r].z), fmaf(fx, e[r].y, e[r].x));
+        if (onA) sumA[r] += val;
+        else sumB[r] += val;
+    }
+}
+
 // grid: (ntx*nty tiles, angle chunks, dN / 8 slice groups); acc [dN][nrows][px] doubles.
 template <int T>
 __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__restrict__ img,
@@ -364,21 +411,37 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
     const size_t nimg = (size_t)g.nx * g.ny;
     const float *im0 = img + (size_t)z0 * nimg;
 
-    // element (c, r) of slice z at tile[(r*T + c)*8 + z]; texels outside the image are 0
-    for (int i = threadIdx.x; i < T * T * kMsSlices; i += kMsThreads) {
-        const int z = i & (kMsSlices - 1), e = i >> 3;
-        const int r = e / T, c = e - r * T;
-        const int gx = x0 + c, gy = y0 + r;
+    // element (c, r) of slice z at tile[(r*T + c)*8 + z]; texels outside the image are 0.
+    // A warp stages a strip of four columns x eight slices (lane 8*cl + z: column 4u + cl of
+    // slice z) over kMsStageRows element rows, walking down the texel rows: each texel is
+    // loaded once, its right neighbour comes from the next column's lane (the strip's last
+    // column loads it), and the quarter-warps store whole records (no bank conflict).
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int cl = lane >> 3, z = lane & (kMsSlices - 1);
         const float *im = im0 + (size_t)z * nimg;
-        const bool c0 = (unsigned)gx < (unsigned)g.nx, c1 = (unsigned)(gx + 1) < (unsigned)g.nx;
-        const bool r0 = (unsigned)gy < (unsigned)g.ny, r1 = (unsigned)(gy + 1) < (unsigned)g.ny;
-        const long long o = (long long)gy * g.nx + gx;
-        const float t00 = (r0 && c0) ? __ldg(im + o) : 0.0f;
-        const float t10 = (r0 && c1) ? __ldg(im + o + 1) : 0.0f;
-        const float t01 = (r1 && c0) ? __ldg(im + o + g.nx) : 0.0f;
-        const float t11 = (r1 && c1) ? __ldg(im + o + g.nx + 1) : 0.0f;
-        const float d0 = t10 - t00, d1 = t11 - t01;
-        tile[i] = make_float4(t00, d0, t01 - t00, d1 - d0);
+        constexpr int kStrips = (T + 3) / 4, kBands = (T + kMsStageRows - 1) / kMsStageRows;
+        for (int u = warp; u < kStrips * kBands; u += kMsThreads / 32) {
+            const int c = (u % kStrips) * 4 + cl, r0 = (u / kStrips) * kMsStageRows;
+            const int gx = x0 + c;
+            const bool c0 = (unsigned)gx < (unsigned)g.nx, c1 = (unsigned)(gx + 1) < (unsigned)g.nx;
+            float tp = 0.0f, trp = 0.0f;
+#pragma unroll
+            for (int j = 0; j <= kMsStageRows; ++j) {
+                const int r = r0 + j, gy = y0 + r;
+                const bool rv = (unsigned)gy < (unsigned)g.ny && r <= T;
+                const long long o = (long long)gy * g.nx + gx;
+                const float t = (rv && c0) ? __ldg(im + o) : 0.0f;
+                float tr = __shfl_down_sync(0xffffffffu, t, 8);
+                if (cl == 3) tr = (rv && c1) ? __ldg(im + o + 1) : 0.0f;
+                if (j > 0 && c < T && r - 1 < T) {
+                    const float d0 = trp - tp, d1 = tr - t;
+                    tile[((r - 1) * T + c) * kMsSlices + z] = make_float4(tp, d0, t - tp, d1 - d0);
+                }
+                tp = t;
+                trp = tr;
+            }
+        }
     }
     // owned base-texel ranges (the union over tiles is [-1, n-1])
     const float xlo = (float)x0, xhi = (float)min(x0 + T, g.nx);
@@ -425,9 +488,9 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
 
     const int total = tail[0];
     const int lane = threadIdx.x & 31;
-    const int ph = lane & (kMsSlices - 1);  // sample phase; also this lane's first slot
-    const int qb = lane & ~(kMsSlices - 1);  // first lane of the quarter
-    const int ray = lane >> 3;               // ray of the warp's four
+    const int ph = lane & (kMsSlices - 1);    // stream phase; also this lane's first slot
+    const int qb = lane & ~(kMsSlices - 1);   // first lane of the quarter
+    const int pair = lane >> 3;               // ray pair of the warp's four
     const int D = g.depth;
     // byte address of the record of base texel (col, row) from the floor bits:
     // (iy_bits * T + ix_bits) * 128 + base2, the biases folded into base2 (mod 2^32)
@@ -441,11 +504,11 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
 #pragma unroll
     for (int r = 0; r < kMsSlices; ++r) off[r] = 16u * (unsigned)((r + ph) & (kMsSlices - 1));
     const f2x MM = f2_pack(kMagic, kMagic);
-    const f2x step2 = f2_pack((float)kMsSlices, (float)kMsSlices);
-    // lanes 0..3 of a quarter find the ray's interval limits: the lower (even) or upper (odd)
-    // Y limit from the x (0, 1) or the y coordinate (2, 3)
-    const bool bound_x = ph < 2;
+    // lane ph of a quarter finds one interval limit of ray A (ph < 4) or B (ph >= 4): the
+    // lower (even) or upper (odd) Y limit from the x (ph & 3 < 2) or the y coordinate
+    const bool bound_x = (ph & 3) < 2;
     const bool upper = (ph & 1) != 0;
+    const bool of_b = ph >= 4;
     int *counter = tail + 1;
     int k = 0;  // the warp's current angle: items only grow, so the search runs forward
 
@@ -456,13 +519,15 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
         if (item >= total) break;
         while (k + 1 < kn && gpre[k + 1] <= item) ++k;  // the last k with gpre[k] <= item
         const float c = scs[k].x, s = scs[k].y;
-        const int X = xlo_s[k] + (item - gpre[k]) * kMsRays + ray;
-        const bool live = X <= xhi_s[k];
-        const float Xc = (float)X - g.cx;
+        // the quarter's two consecutive rays A = XA and B = XA + 1
+        const int XA = xlo_s[k] + (item - gpre[k]) * kMsRays + 2 * pair;
+        const int Xhi = xhi_s[k];
+        const int Xl = XA + (of_b ? 1 : 0);
+        const float Xc = (float)Xl - g.cx;
         const float ax = fmaf(Xc, c, g.hx);
         const float ay = fmaf(Xc, -s, g.hy);
         int v = 0;
-        if (live && ph < 4) {
+        if (Xl <= Xhi) {
             const float a = bound_x ? ax : ay, sl = bound_x ? s : c;
             const float isl = bound_x ? inv_s[k].y : inv_s[k].x;
             const float lo_ = bound_x ? xlo : ylo, hi_ = bound_x ? xhi : yhi;
@@ -474,43 +539,55 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
                 v = upper ? ((a >= lo_ && a < hi_) ? D : 0) : 0;
             }
         }
-        const int v0 = __shfl_sync(0xffffffffu, v, qb + 0), v1 = __shfl_sync(0xffffffffu, v, qb + 1);
-        const int v2 = __shfl_sync(0xffffffffu, v, qb + 2), v3 = __shfl_sync(0xffffffffu, v, qb + 3);
-        const int ya = max(v0, v2), yb = min(v1, v3);
-        const int n = (live && yb - ya > ph) ? (yb - ya - ph + kMsSlices - 1) / kMsSlices : 0;
-        const float yc0 = (float)(ya + ph) - g.hd;
-        f2x yc2 = f2_pack(yc0, yc0);
+        // this lane's ray's limits: lower ones (even ph) max-combined, upper ones min-combined
+        // across the x and y limits (xor 2), then exchanged within the pair of lanes (xor 1)
+        // and with the other ray's lanes (xor 4)
+        const int w = __shfl_xor_sync(0xffffffffu, v, 2);
+        const int m = upper ? min(v, w) : max(v, w);
+        const int u = __shfl_xor_sync(0xffffffffu, m, 1);
+        const int ya_own = upper ? u : m, yb_own = upper ? m : u;
+        const int ya_oth = __shfl_xor_sync(0xffffffffu, ya_own, 4);
+        const int yb_oth = __shfl_xor_sync(0xffffffffu, yb_own, 4);
+        const int yaA = of_b ? ya_oth : ya_own, ybA = of_b ? yb_oth : yb_own;
+        const int yaB = of_b ? ya_own : ya_oth, ybB = of_b ? yb_own : yb_oth;
+        const int LA = max(ybA - yaA, 0), LB = max(ybB - yaB, 0);
+        // the ray parameters of A and B
+        const float XcA = (float)XA - g.cx, XcB = (float)(XA + 1) - g.cx;
+        const float axA = fmaf(XcA, c, g.hx), ayA = fmaf(XcA, -s, g.hy);
+        const float axB = fmaf(XcB, c, g.hx), ayB = fmaf(XcB, -s, g.hy);
+        // stream position t = 8i + ph: sample yaA + t of A for t < LA, else sample
+        // yaB + t - LA of B; Yc = Y - hd is tracked as a float (exact small integers)
+        const int n = (LA + LB > ph) ? (LA + LB - ph + kMsSlices - 1) / kMsSlices : 0;
+        const float ycA = (float)(yaA + ph) - g.hd, ycB = (float)(yaB - LA + ph) - g.hd;
         const f2x sc = f2_pack(s, c);
-        const f2x axy = f2_pack(ax, ay);
-        float sum[kMsSlices];
+        const f2x axyA = f2_pack(axA, ayA), axyB = f2_pack(axB, ayB);
+        float sumA[kMsSlices], sumB[kMsSlices];
 #pragma unroll
-        for (int r = 0; r < kMsSlices; ++r) sum[r] = 0.0f;
+        for (int r = 0; r < kMsSlices; ++r) {
+            sumA[r] = 0.0f;
+            sumB[r] = 0.0f;
+        }
         for (int i = 0; i < n; ++i) {
-            const f2x xy = f2_fma(yc2, sc, axy);
-            const f2x tb = f2_add_rd(xy, MM);
-            const f2x fr = f2_sub(xy, f2_sub(tb, MM));
-            yc2 = f2_add(yc2, step2);
-            int ixb, iyb;
-            f2_unpack_bits(tb, ixb, iyb);
             float fx, fy;
-            f2_unpack(fr, fx, fy);
-            const unsigned rec = ((unsigned)iyb * (unsigned)T + (unsigned)ixb) * (unsigned)(kMsSlices * 16) + base2;
-            if (!XCT_IN(rec, alo, ahi, XCT_SITE_FWD_MS_TAP)) continue;
-#pragma unroll
-            for (int r = 0; r < kMsSlices; ++r) {
-                const float4 e = lds_f4(rec + off[r]);
-                sum[r] += fmaf(fy, fmaf(fx, e.w, e.z), fmaf(fx, e.y, e.x));
-            }
+            bool onA;
+            float4 e[kMsSlices];
+            ms_load(e, ms_locate(i, ph, LA, ycA, ycB, sc, axyA, axyB, MM, base2, T, fx, fy, onA), off, alo, ahi);
+            ms_accumulate(e, fx, fy, onA, sumA, sumB);
         }
         // lane p's slot d holds slice (d + p) mod 8: lane p gathers slice p's partial sums from
-        // lanes (p - d) mod 8 of its quarter, slot d
-        float tot = 0.0f;
+        // lanes (p - d) mod 8 of its quarter, slot d -- for A and for B
+        float totA = 0.0f, totB = 0.0f;
 #pragma unroll
-        for (int d = 0; d < kMsSlices; ++d)
-            tot += __shfl_sync(0xffffffffu, sum[d], qb + ((ph - d) & (kMsSlices - 1)));
-        if (live && yb > ya &&
-            XCT_IN((long long)k * g.px + X, 0, (long long)(nrows - k0) * g.px - 1, XCT_SITE_FWD_ACC))
-            atomicAdd(acc + ((size_t)(z0 + ph) * nrows + k0 + k) * g.px + X, f32_to_f64(tot));
+        for (int d = 0; d < kMsSlices; ++d) {
+            const int src = qb + ((ph - d) & (kMsSlices - 1));
+            totA += __shfl_sync(0xffffffffu, sumA[d], src);
+            totB += __shfl_sync(0xffffffffu, sumB[d], src);
+        }
+        double *accz = acc + ((size_t)(z0 + ph) * nrows + k0 + k) * g.px;
+        if (LA > 0 && XCT_IN((long long)k * g.px + XA, 0, (long long)(nrows - k0) * g.px - 1, XCT_SITE_FWD_ACC))
+            atomicAdd(accz + XA, f32_to_f64(totA));
+        if (LB > 0 && XCT_IN((long long)k * g.px + XA + 1, 0, (long long)(nrows - k0) * g.px - 1, XCT_SITE_FWD_ACC))
+            atomicAdd(accz + XA + 1, f32_to_f64(totB));
     }
 }
 
