@@ -3,8 +3,9 @@
 TEST INFRASTRUCTURE ONLY.  The reference (NozomuIshiguro/CT-XAFS_analysis) has no tests
 and no CPU build; its kernels are OpenCL C JIT-compiled at run time with the problem shape
 as -D macros (CT_reconstruction/GPU.cpp:537-550).  This recipe compiles
-CT_reconstruction/FBP.cl, OSEM.cl, FISTA.cl and reconstShare.cl (OSEM_programBuild builds the
-last three as one program, GPU.cpp:527-535), where they lie in the reference checkout, with g++ against oracle/ref_shim/cl_shim.hpp (an
+CT_reconstruction/FBP.cl, OSEM.cl, FISTA.cl, AART.cl and reconstShare.cl (OSEM_programBuild builds
+OSEM, FISTA and reconstShare as one program, GPU.cpp:527-535; FISTA_programBuild AART, FISTA and
+reconstShare, GPU.cpp:2032-2047), where they lie in the reference checkout, with g++ against oracle/ref_shim/cl_shim.hpp (an
 OpenCL-C environment written for this project).  The only changes to the kernel text are
 mechanical and happen in the build output: OpenCL vector literals ``(float4)(a,b,c,d)``
 become constructor calls ``float4(a,b,c,d)`` (C++ would parse the former as a comma
@@ -27,7 +28,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_ROOT = os.environ.get("XCT_REFERENCE_ROOT") or os.path.join(os.path.dirname(HERE), "..", "reference")
 OUT = os.path.join(HERE, "_ref")
 KERNELS = ("CT_reconstruction/FBP.cl", "CT_reconstruction/OSEM.cl", "CT_reconstruction/FISTA.cl",
-           "CT_reconstruction/reconstShare.cl")
+           "CT_reconstruction/AART.cl", "CT_reconstruction/reconstShare.cl")
 _VEC = re.compile(r"\((float|int|uint)([234])\)\s*\(")
 _SWZ = re.compile(r"\.(xx|yy|yx)\b")
 _GLOBAL = re.compile(r"(?<![_\w])global(?=\s)")

@@ -76,6 +76,9 @@ def lib():
             getattr(L, "xo_sino_correction" + sfx).argtypes = [p, p, fp, gp, ctypes.c_int]
             getattr(L, "xo_adjoint" + sfx).argtypes = [p, p, gp, p]
             getattr(L, "xo_osem_run" + sfx).argtypes = [p, p, p, gp, ip, ctypes.c_int, ctypes.c_int]
+        L.xo_power_iteration_f32.argtypes = [fp, gp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp]
+        L.xo_fista_run_f32.argtypes = [fp, fp, fp, fp, gp, ctypes.c_int, ip, ctypes.c_int, ctypes.c_float, fp,
+                                       ctypes.c_double, ctypes.c_int]
         L.xo_fbp_filter_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp]
         L.xo_fbp_filter_f64.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
         L.xo_base_up_f32.argtypes = [fp, ctypes.c_longlong, ctypes.c_int, fp]
@@ -308,6 +311,50 @@ def cs_lambda(cs_lambda_f32):
     return float(np.float32(d / float(np.float32(0.5)) * 0.5))
 
 
+def lambda_literal(cs_lambda_f32):
+    """The value of -D LAMBDA_FISTA: the float CSlambda streamed with six significant digits
+    (GPU.cpp:549, FISTA_programBuild likewise), read back as a double literal."""
+    return float("%g" % np.float32(cs_lambda_f32))
+
+
+def power_iteration(angles_deg, nx, ny, px, ss, trials=30, work_group=1024, fetch_mode=0, layer_mode=0):
+    """powerIteration (GPU.cpp:2079-2188): L[ss], the squared norm of (B A) applied to the
+    normalised estimate after `trials` rounds, per subset, in the kernels' float order.
+    layer_mode 0: powerIter1 projects layer 0 for every subset (its sampling coordinate's
+    layer is never set, FISTA.cl:60); 1: each subset's own layer."""
+    pa = len(angles_deg)
+    g = make_geom(nx, ny, px, pa, ss, None, ORDER_LITERAL, fetch_mode)
+    cs = trig(angles_deg, np.float32)
+    out = np.zeros(ss, np.float32)
+    lib().xo_power_iteration_f32(_p(cs), ctypes.byref(g), trials, work_group, layer_mode, _p(out))
+    return out
+
+
+def fista_run(imgs, meas, angles_deg, ss, it, L, alpha=1.0, cs_lambda_f32=1.0e-4, correction_mode=0,
+              sub_order=None, flags=0, order=ORDER_LITERAL):
+    """FISTA_execution (GPU.cpp:1755-1924) on a batch meas [dN][pa][px]: the initial image is
+    the subset-0 backprojection (imgs only gives the shape), then per subset AART1,
+    FISTAbackProjection and ISTA3D (first cycle) / FISTA3D.  flags & 1 stores FISTA3D's
+    x_{t+1} as the next image (the reference discards it)."""
+    meas = np.ascontiguousarray(meas, dtype=np.float32)
+    dN, pa, px = meas.shape
+    ny, nx = np.asarray(imgs).shape[-2:]
+    g = make_geom(nx, ny, px, pa, ss, None, order)
+    cs = trig(angles_deg, np.float32)
+    if correction_mode > 0:
+        used = np.stack([sino_correction(m, angles_deg, correction_mode) for m in meas])
+        res0 = meas.copy()
+    else:
+        used = meas
+        res0 = np.zeros_like(meas)
+    so = subset_order(ss) if sub_order is None else np.ascontiguousarray(sub_order, dtype=np.int32)
+    out = np.zeros((dN, ny, nx), np.float32)
+    Lf = np.ascontiguousarray(L, dtype=np.float32)
+    lib().xo_fista_run_f32(_p(out), _p(np.ascontiguousarray(used)), _p(res0), _p(cs), ctypes.byref(g), dN, _p(so),
+                           it, float(alpha), _p(Lf), lambda_literal(cs_lambda_f32), int(flags))
+    return out
+
+
 def ista3d(v, lam):
     v = np.ascontiguousarray(v, dtype=np.float32)
     dN, ny, nx = v.shape
@@ -393,10 +440,10 @@ def osem_run(img0, meas, angles_deg, ss, it, sub_order=None, cx=None, order=ORDE
 class RefKernels:
     """The reference's OSEM.cl/reconstShare.cl compiled for one shape (see build_ref.py)."""
 
-    def __init__(self, nx, ny, px, pa, ss, zp=None):
+    def __init__(self, nx, ny, px, pa, ss, zp=None, cs_lambda="0.0001"):
         import build_ref  # noqa: local module beside this file
         self.shape = (nx, ny, px, pa, ss)
-        self.lib = ctypes.CDLL(build_ref.build(nx, ny, px, pa, ss, zp))
+        self.lib = ctypes.CDLL(build_ref.build(nx, ny, px, pa, ss, zp, cs_lambda=cs_lambda))
         self.zp = self.lib.ref_zp_size()
         fp = ctypes.POINTER(ctypes.c_float)
         ip = ctypes.POINTER(ctypes.c_int)
@@ -408,6 +455,27 @@ class RefKernels:
         self.lib.ref_bp_fbp.argtypes = [fp, fp, ctypes.c_int, fp]
         self.lib.ref_base_up.argtypes = [fp, ctypes.c_int, ctypes.c_int, fp]
         self.lib.ref_fista_osem_execution.argtypes = [fp, fp, fp, ip, ctypes.c_int, ctypes.c_int]
+        self.lib.ref_power_iteration.argtypes = [fp, ctypes.c_int, ctypes.c_int, fp, ctypes.c_int]
+        self.lib.ref_fista_execution.argtypes = [fp, fp, fp, ip, ctypes.c_int, ctypes.c_int, ctypes.c_float, fp,
+                                                 ctypes.c_int, ctypes.c_int]
+
+    def power_iteration(self, angles_deg, trials=30, work_group=1024, fetch_mode=0):
+        ss = self.shape[4]
+        out = np.zeros(ss, np.float32)
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        self.lib.ref_power_iteration(_p(ang), trials, work_group, _p(out), fetch_mode)
+        return out
+
+    def fista_execution(self, prjs, angles_deg, sub_order, it, L, alpha=1.0, correction_mode=0, fetch_mode=0):
+        nx, ny, px, pa, ss = self.shape
+        prjs = np.ascontiguousarray(prjs, dtype=np.float32)
+        imgs = np.zeros((prjs.shape[0], ny, nx), np.float32)
+        ang = np.ascontiguousarray(angles_deg, dtype=np.float32)
+        so = np.ascontiguousarray(sub_order, dtype=np.int32)
+        Lf = np.ascontiguousarray(L, dtype=np.float32)
+        self.lib.ref_fista_execution(_p(imgs), _p(prjs), _p(ang), _p(so), prjs.shape[0], it, float(alpha), _p(Lf),
+                                     correction_mode, fetch_mode)
+        return imgs
 
     def fista_osem_execution(self, imgs, prjs, angles_deg, sub_order, it):
         imgs = np.array(imgs, dtype=np.float32, copy=True, order="C")

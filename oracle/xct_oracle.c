@@ -570,3 +570,194 @@ void xo_fista3d_f32(const float *x_in, const float *v, const float *beta, int nx
                 w_new[i] = (w != w) ? 1.0e-6f : w;
             }
 }
+
+/* ------------------------------------------------------------ FISTA with compressed sensing
+ * The Lipschitz estimate of the subset operators (powerIteration, GPU.cpp:2079-2188, over
+ * the kernels powerIter1/2/3, imageL2AbsX/Y of FISTA.cl:50-208) and FISTA_execution
+ * (GPU.cpp:1755-1924), float, in the kernels' literal order. */
+
+/* Bilinear read with the linear sampler at unnormalised (u, v) on one [h][w] image, zero
+ * border: texel coordinates (u - 0.5, v - 0.5), weights as the OpenCL 1.2 specification
+ * writes them. */
+static float xo_linear_(const float *img, int w, int h, float u, float v)
+{
+    const float uu = u - 0.5f, vv = v - 0.5f;
+    const float fi = floorf(uu), fj = floorf(vv);
+    const float a = uu - fi, b = vv - fj;
+    const int i = (int)fi, j = (int)fj;
+    const float t00 = xo_tex__f32(img, w, h, i, j), t10 = xo_tex__f32(img, w, h, i + 1, j);
+    const float t01 = xo_tex__f32(img, w, h, i, j + 1), t11 = xo_tex__f32(img, w, h, i + 1, j + 1);
+    return (1.0f - a) * (1.0f - b) * t00 + a * (1.0f - b) * t10 + (1.0f - a) * b * t01 + a * b * t11;
+}
+
+/* A linear-sampler read at INTEGER coordinates (undefined in OpenCL 1.2): the exact texel
+ * (fetch_mode 0) or the 2x2 average of texels (X-1..X, Y-1..Y) (fetch_mode 1). */
+static float xo_int_linear_(const float *img, int w, int h, int X, int Y, int fetch_mode)
+{
+    if (fetch_mode == 0) return xo_tex__f32(img, w, h, X, Y);
+    return 0.25f * (((xo_tex__f32(img, w, h, X - 1, Y - 1) + xo_tex__f32(img, w, h, X, Y - 1)) +
+                     xo_tex__f32(img, w, h, X - 1, Y)) +
+                    xo_tex__f32(img, w, h, X, Y));
+}
+
+/* imageL2AbsX then imageL2AbsY of one [ny][nx] image with work-groups of wg items: each item
+ * sums the squares at X = lid + i*wg, i < nx/wg (then Y likewise), then the tree
+ * loc[lid] += loc[lid + s] for s = wg/2, wg/4, ..., 1 (FISTA.cl:133-208). */
+static float xo_l2_wg_(const float *img, int nx, int ny, int wg)
+{
+    float *loc = (float *)malloc(sizeof(float) * (size_t)wg);
+    float *rows = (float *)malloc(sizeof(float) * (size_t)ny);
+    if (!loc || !rows) {
+        free(loc);
+        free(rows);
+        return NAN;
+    }
+    for (int Y = 0; Y < ny; ++Y) {
+        for (int l = 0; l < wg; ++l) {
+            loc[l] = 0.0f;
+            for (int i = 0; i < nx / wg; ++i) {
+                const float v = img[(size_t)Y * nx + l + i * wg];
+                loc[l] += v * v;
+            }
+        }
+        for (int s = wg / 2; s > 0; s >>= 1)
+            for (int l = 0; l < s; ++l) loc[l] += loc[l + s];
+        rows[Y] = loc[0];
+    }
+    for (int l = 0; l < wg; ++l) {
+        loc[l] = 0.0f;
+        for (int i = 0; i < ny / wg; ++i) loc[l] += rows[l + i * wg];
+    }
+    for (int s = wg / 2; s > 0; s >>= 1)
+        for (int l = 0; l < s; ++l) loc[l] += loc[l + s];
+    const float r = loc[0];
+    free(loc);
+    free(rows);
+    return r;
+}
+
+/* layer_mode: powerIter1 declares its sampling coordinate without setting the layer
+ * (FISTA.cl:60, `float4 xyz;` and xyz.z never written), so which layer it projects is
+ * undefined; 0 reads layer 0 for every subset (a zero-initialised coordinate, as the OpenCL-C
+ * shim and a cleared register give), 1 reads the subset's own layer (the evident intent). */
+void xo_power_iteration_f32(const float *cs, const xo_geom *g, int trials, int work_group, int layer_mode, float *L)
+{
+    const int nx = g->nx, ny = g->ny, px = g->px, pa = g->pa, ss = g->ss, D = g->depth;
+    const int wg = work_group < nx ? work_group : nx; /* min(CL_DEVICE_MAX_WORK_GROUP_SIZE, g_ox) */
+    const int rows = pa / ss;
+    const size_t nimg = (size_t)nx * ny;
+    float *img = (float *)malloc(sizeof(float) * nimg * ss);
+    float *cnd = (float *)malloc(sizeof(float) * nimg * ss);
+    float *prj = (float *)malloc(sizeof(float) * (size_t)px * (rows > 0 ? rows : 1) * ss);
+    float *l2 = (float *)calloc((size_t)ss, sizeof(float));
+    if (!img || !cnd || !prj || !l2) goto done;
+    for (size_t i = 0; i < nimg * ss; ++i) img[i] = 1.0f; /* the fill of GPU.cpp:2122 */
+    {
+        const float scale = ((float)ss / (float)pa) / (float)D;
+        for (int trial = 0; trial < trials; ++trial) {
+            /* powerIter1 over (px, pa/ss, ss): ray sums of subset z's rows of the read layer,
+             * integer half sizes, no +0.5 */
+#pragma omp parallel for collapse(3) schedule(static)
+            for (int z = 0; z < ss; ++z)
+                for (int k = 0; k < rows; ++k)
+                    for (int X = 0; X < px; ++X) {
+                        const int th = z + k * ss;
+                        const float c = cs[2 * th], s = cs[2 * th + 1];
+                        const float *im = img + (layer_mode ? (size_t)z * nimg : 0);
+                        float acc = 0.0f;
+                        for (int Y = 0; Y < D; ++Y) {
+                            const float u = ((float)(X - px / 2) * c + (float)(Y - D / 2) * s) + (float)(nx / 2);
+                            const float v = ((float)(-(X - px / 2)) * s + (float)(Y - D / 2) * c) + (float)(ny / 2);
+                            acc += xo_linear_(im, nx, ny, u, v);
+                        }
+                        prj[((size_t)z * rows + k) * px + X] = acc;
+                    }
+            /* powerIter2 over (nx, ny, ss): nearest-bin backprojection, floor rule, * ss/pa/D */
+#pragma omp parallel for collapse(2) schedule(static)
+            for (int z = 0; z < ss; ++z)
+                for (int Y = 0; Y < ny; ++Y)
+                    for (int X = 0; X < nx; ++X) {
+                        float b = 0.0f;
+                        for (int k = 0; k < rows; ++k) {
+                            const int th = z + k * ss;
+                            const float c = cs[2 * th], s = cs[2 * th + 1];
+                            const float t = ((float)(X - nx / 2) * c - (float)(Y - ny / 2) * s) + (float)(px / 2);
+                            const int bin = (int)floorf(t);
+                            b += (bin >= 0 && bin < px) ? prj[((size_t)z * rows + k) * px + bin] : 0.0f;
+                        }
+                        cnd[(size_t)z * nimg + (size_t)Y * nx + X] = b * scale;
+                    }
+            for (int z = 0; z < ss; ++z) l2[z] = xo_l2_wg_(cnd + (size_t)z * nimg, nx, ny, wg);
+            /* powerIter3: normalise (the candidate read at integer coordinates, linear sampler) */
+#pragma omp parallel for collapse(2) schedule(static)
+            for (int z = 0; z < ss; ++z)
+                for (int Y = 0; Y < ny; ++Y)
+                    for (int X = 0; X < nx; ++X)
+                        img[(size_t)z * nimg + (size_t)Y * nx + X] =
+                            xo_int_linear_(cnd + (size_t)z * nimg, nx, ny, X, Y, g->fetch_mode) / sqrtf(l2[z]);
+        }
+        for (int z = 0; z < ss; ++z) L[z] = l2[z];
+    }
+done:
+    free(img);
+    free(cnd);
+    free(prj);
+    free(l2);
+}
+
+/* FISTA_execution for dN slices: imgs [dN][ny][nx] (out), meas [dN][pa][px] the sinograms the
+ * kernels read (already corrected when correctionMode > 0), res0 [dN][pa][px] the initial
+ * content of the residual image (the uncorrected sinograms with a correction -- GPU.cpp:1812
+ * copies them there -- else zeros: rows AART1 never writes keep it), L [ss] from the power
+ * iteration, lambda_d the -D LAMBDA_FISTA value.  flags bit 1: store each FISTA3D x_{t+1} as
+ * the next image (the reference binds that output to the beta image, GPU.cpp:1867-1868, so
+ * its image is the first cycle's ISTA3D result). */
+void xo_fista_run_f32(float *imgs, const float *meas, const float *res0, const float *cs, const xo_geom *g, int dN,
+                      const int *sub, int it, float alpha, const float *L, double lambda_d, int flags)
+{
+    const int nx = g->nx, ny = g->ny, px = g->px, pa = g->pa, ss = g->ss;
+    const size_t nimg = (size_t)nx * ny, nprj = (size_t)px * pa, all = nimg * dN;
+    float *x = imgs;
+    float *dest = (float *)malloc(sizeof(float) * all), *v = (float *)malloc(sizeof(float) * all);
+    float *w = (float *)malloc(sizeof(float) * all), *beta = (float *)calloc(all, sizeof(float));
+    float *tw = (float *)malloc(sizeof(float) * all), *tx = (float *)malloc(sizeof(float) * all);
+    float *tb = (float *)malloc(sizeof(float) * all), *res = (float *)malloc(sizeof(float) * nprj * dN);
+    if (!dest || !v || !w || !beta || !tw || !tx || !tb || !res) goto done;
+    memcpy(res, res0, sizeof(float) * nprj * dN);
+    for (int z = 0; z < dN; ++z) xo_backprojection_f32(meas + z * nprj, cs, g, sub[0], dest + z * nimg);
+    memcpy(x, dest, sizeof(float) * all);
+    memcpy(w, x, sizeof(float) * all);
+    {
+        const float *X = x;
+        int first = 1;
+        for (int i = 0; i < it; ++i)
+            for (int k = 0; k < ss; ++k) {
+                const int s = sub[k];
+                for (int z = 0; z < dN; ++z) {
+                    xo_aart1_f32(X + z * nimg, meas + z * nprj, cs, g, s, pa / ss, res + z * nprj);
+                    xo_fista_bp_f32(X + z * nimg, v + z * nimg, res + z * nprj, cs, g, s, alpha, L[s]);
+                }
+                const float lam = (float)(lambda_d / (double)L[s] * 0.5);
+                if (first) {
+                    xo_ista3d_f32(v, nx, ny, dN, lam, dest);
+                    X = w;
+                    first = 0;
+                } else {
+                    xo_fista3d_f32(x, v, beta, nx, ny, dN, lam, tw, tx, tb);
+                    memcpy(w, tw, sizeof(float) * all);
+                    memcpy(beta, tb, sizeof(float) * all);
+                    if (flags & 1) memcpy(dest, tx, sizeof(float) * all);
+                }
+                memcpy(x, dest, sizeof(float) * all);
+            }
+    }
+done:
+    free(dest);
+    free(v);
+    free(w);
+    free(beta);
+    free(tw);
+    free(tx);
+    free(tb);
+    free(res);
+}

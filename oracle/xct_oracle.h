@@ -67,6 +67,15 @@ void xo_ista3d_f32(const float *v, int nx, int ny, int dN, float lambda, float *
 void xo_fista3d_f32(const float *x_in, const float *v, const float *beta, int nx, int ny, int dN, float lambda,
                     float *w_new, float *x_new, float *beta_new);
 
+/* FISTA with compressed sensing (FISTA_ocl): the power iteration's Lipschitz estimates L [ss]
+ * (work_group: the reference's min(CL_DEVICE_MAX_WORK_GROUP_SIZE, ox) reduction width;
+ * layer_mode: which layer powerIter1 reads, see xct_oracle.c) and FISTA_execution on dN slices
+ * (see xct_oracle.c for the arguments). */
+void xo_power_iteration_f32(const float *cs, const xo_geom *g, int trials, int work_group, int layer_mode,
+                            float *L);
+void xo_fista_run_f32(float *imgs, const float *meas, const float *res0, const float *cs, const xo_geom *g, int dN,
+                      const int *sub, int it, float alpha, const float *L, double lambda_d, int flags);
+
 #define XO_DECL(T, S)                                                                                   \
     void xo_projection##S(const T *img, const T *cs, const xo_geom *g, int sub, int ss, int nrows, T *prj); \
     void xo_osem1##S(const T *img, const T *meas, const T *cs, const xo_geom *g, int sub, int nrows,      \

@@ -32,6 +32,11 @@ Fixtures (np.savez_compressed):
   cs_64.npz      compressed-sensing OS-EM (FISTA_OSEM_execution with ISTA3D/FISTA3D) of a
                  batch of 3 slices of a 64x64x3 ellipsoid phantom (seed 4), 90 angles, 64 bins,
                  I0 = 1e4 (seeds 0..2), 10 subsets x 2 iterations, CSlambda 1e-4, from 1.0.
+  fista_64.npz   FISTA with compressed sensing (powerIteration, 30 trials; FISTA_execution
+                 with AART1, FISTAbackProjection, ISTA3D/FISTA3D) of 3 slices of a 64x64x3
+                 ellipsoid phantom (seed 6), 90 angles, 64 bins, I0 = 1e4, 10 subsets x 2
+                 iterations, CSlambda 1e-4, AART factor 1.0; also the run that stores
+                 FISTA3D's x_{t+1}.
 """
 import os
 import sys
@@ -190,6 +195,29 @@ def cs_case(name, n, px, pa, ss, it, dN, lam, seed, i0):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
 
 
+def fista_case(name, n, px, pa, ss, it, dN, lam, alpha, trials, seed, i0):
+    ang = P.uniform_angles(pa)
+    prm = P.ellipsoid_params(n, dN, count=6, seed=seed)
+    meas = np.stack([P.noisy_log_sinogram(O.projection(P.ellipsoid_slice(prm, z, n, n), ang, px, order=LIT), i0, z)
+                     for z in range(dN)])
+    sub = O.subset_order(ss)
+    L = O.power_iteration(ang, n, n, px, ss, trials=trials)
+    out = O.fista_run(np.zeros((dN, n, n)), meas, ang, ss, it, L, alpha, lam, sub_order=sub)
+    upd = O.fista_run(np.zeros((dN, n, n)), meas, ang, ss, it, L, alpha, lam, sub_order=sub, flags=1)
+    arrays = dict(angles=ang, meas=meas, sub=sub, L=L, fista=out, fista_update_x=upd,
+                  shape=np.array([n, n, px, pa, ss, it, trials], np.int32), cs_lambda=np.array([lam], np.float32),
+                  alpha=np.array([alpha], np.float32))
+    if O.ref_available():
+        ref = O.RefKernels(n, n, px, pa, ss, cs_lambda="%g" % np.float32(lam))
+        assert np.array_equal(ref.power_iteration(ang, trials=trials), L), name + ": power iteration differs"
+        assert np.array_equal(ref.fista_execution(meas, ang, sub, it, L, alpha), out), name + ": FISTA differs"
+        arrays["pinned_by_reference_kernels"] = np.array([1], np.int32)
+        print(name, "pinned: bit-identical to the reference kernels")
+    else:
+        arrays["pinned_by_reference_kernels"] = np.array([0], np.int32)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+
+
 if __name__ == "__main__":
     O.build()
     case("small_64", 64, 64, 64, 90, 10, 2, 10, 1, 1e5, 11)
@@ -200,3 +228,4 @@ if __name__ == "__main__":
     rcs_case("rcs_64", 64, 64, 90, 10, 9, -2.0, 0.5, 1.0, 5, 1e5, 15, 64)
     reslice_case("reslice_small", 16, 12, 24, 16, 0.125, 0.3)
     cs_case("cs_64", 64, 64, 90, 10, 2, 3, 1.0e-4, 4, 1e4)
+    fista_case("fista_64", 64, 64, 90, 10, 2, 3, 1.0e-4, 1.0, 30, 6, 1e4)
