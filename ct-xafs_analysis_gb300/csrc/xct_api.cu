@@ -151,6 +151,9 @@ static void plan_free(xct_plan *p)
     cudaFree(p->d_rc_prm);
     cudaFree(p->d_fi);
     cudaFree(p->d_cs);
+    cudaFree(p->d_fista);
+    cudaFree(p->d_pi);
+    cudaFree(p->d_pi_l2);
     cudaFree(p->d_sino2);
     cudaFree(p->d_img2);
     if (p->s_h2d) cudaStreamDestroy(p->s_h2d);
@@ -1101,7 +1104,7 @@ static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const
                 // join couples neighbouring slices
                 rc = dN >= 2 ? subset_step_split(p, dN, meas, d_img, s, st)
                              : subset_step(p, dN, meas, d_img, p->d_ratio, p->d_acc, s, st);
-                if (!rc) rc = launch_fista3d(w, d_img, beta, xn, g.nx, g.ny, dN, lambda, p->ctx->sm_count, st);
+                if (!rc) rc = launch_fista3d(w, w, d_img, beta, xn, g.nx, g.ny, dN, lambda, p->ctx->sm_count, st);
             }
             if (rc) return rc;
             XCT_CUDA_TRY(cudaMemcpyAsync(d_img, xn, bytes, cudaMemcpyDeviceToDevice, st));
@@ -1230,6 +1233,223 @@ int xct_rot_center_search(xct_plan *p, int n, float shift_start, float shift_ste
         }
     *best = b;
     return XCT_OK;
+}
+
+// ------------------------------------------------- FISTA with compressed sensing (FISTA_ocl)
+// powerIteration (GPU.cpp:2079-2188): per subset z, the estimate image (all 1 at first) is
+// forward-projected on z's rows (powerIter1: the tiled projector with the half-texel shift of
+// its coordinates), backprojected (powerIter2), its squared norm taken over the columns and
+// rows the reference's work-groups visit (imageL2AbsX/Y) and the image normalised
+// (powerIter3); L[z] is the last norm.  powerIter1 never sets the layer of its sampling
+// coordinate (FISTA.cl:60), so by default every subset projects layer 0's estimate -- then
+// only layer 0's iterate matters, and the other subsets are evaluated on its final state
+// alone (the same values, ss times less work); XCT_PI_OWN_LAYER projects each subset's own.
+int xct_fista_power_iteration(xct_plan *p, int trials, int work_group, int flags, float *L_out, void *stream)
+{
+    XCT_RANGE("xct_fista_power_iteration");
+    if (!p) return xct_fail(XCT_E_INVALID, "xct_fista_power_iteration: plan is null");
+    if (trials < 1 || trials > 100000) return xct_fail(XCT_E_INVALID, "xct_fista_power_iteration: trials must be >= 1");
+    if (work_group < 1) return xct_fail(XCT_E_INVALID, "xct_fista_power_iteration: work_group must be >= 1");
+    if (flags & ~XCT_PI_OWN_LAYER) return xct_fail(XCT_E_INVALID, "xct_fista_power_iteration: unknown flags");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const KGeom &g = p->kg;
+    const int ss = g.ss, rows = g.pa / g.ss;
+    const bool own = (flags & XCT_PI_OWN_LAYER) != 0;
+    const int layers = own ? ss : 1;
+    const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa;
+    if (p->pi_layers < layers) {
+        cudaFree(p->d_pi);
+        p->d_pi = nullptr;
+        p->pi_layers = 0;
+        cudaError_t e = cudaMalloc(&p->d_pi, sizeof(float) * ((size_t)(layers + 1) * nimg + nprj));
+        if (e != cudaSuccess) {
+            p->d_pi = nullptr;
+            return xct_cuda_fail(e, "cudaMalloc power-iteration buffers");
+        }
+        p->pi_layers = layers;
+    }
+    if (!p->d_pi_l2) {
+        cudaError_t e = cudaMalloc(&p->d_pi_l2, sizeof(double) * (size_t)std::max(ss, 1));
+        if (e != cudaSuccess) {
+            p->d_pi_l2 = nullptr;
+            return xct_cuda_fail(e, "cudaMalloc power-iteration norms");
+        }
+    }
+    float *img = p->d_pi, *cnd = p->d_pi + (size_t)p->pi_layers * nimg, *prj = cnd + nimg;
+    int rc = launch_fill(img, (long long)layers * (long long)nimg, 1.0f, p->ctx->sm_count, st);  // GPU.cpp:2122
+    if (rc) return rc;
+    // powerIter1's coordinates: (X - px/2) c + (Y - D/2) s + nx/2 in integer halves, read by the
+    // linear sampler at that minus 0.5 (no +0.5 as in OSEM1)
+    KGeom gs = g;
+    gs.hx = (float)(g.nx / 2) - 0.5f;
+    gs.hy = (float)(g.ny / 2) - 0.5f;
+    gs.cx = (float)(g.px / 2);
+    gs.hd = (float)(g.depth / 2);
+    gs.ms_chunk = 0;
+    const int wg = std::min(work_group, g.nx);  // min(CL_DEVICE_MAX_WORK_GROUP_SIZE, g_ox)
+    const int nxe = (g.nx / wg) * wg, nye = (g.ny / wg) * wg;
+    const float scale = ((float)ss / (float)g.pa) / (float)g.depth;
+    for (int t = 0; t < trials; ++t) {
+        const bool last = t == trials - 1;
+        for (int z = 0; z < ss; ++z) {
+            if (!own && !last && z > 0) continue;  // only layer 0's iterate is ever projected
+            float *im = img + (own ? (size_t)z * nimg : 0);
+            if (p->g.kernels == XCT_KERNELS_TILED)
+                rc = launch_fwd_tiled(gs, p->d_trig, im, nullptr, prj, p->d_acc, 1, z, ss, rows, st);
+            else rc = launch_fwd_plain(gs, p->d_trig, im, nullptr, prj, 1, z, ss, rows, st);
+            if (!rc) rc = launch_pi_bp(g, p->d_trig, prj, cnd, z, ss, rows, scale, st);
+            if (!rc) rc = launch_pi_l2(cnd, g.nx, nxe, nye, p->d_pi_l2 + z, p->ctx->sm_count, st);
+            // on the last trial every subset reads the same state; no further normalisation
+            if (!rc && !last) rc = launch_pi_norm(cnd, im, g.nx, g.ny, p->d_pi_l2 + z, g.fetch, st);
+            if (rc) return rc;
+        }
+    }
+    std::vector<double> l2(ss);
+    XCT_CUDA_TRY(cudaMemcpyAsync(l2.data(), p->d_pi_l2, sizeof(double) * ss, cudaMemcpyDeviceToHost, st));
+    XCT_CUDA_TRY(cudaStreamSynchronize(st));
+    p->lip.assign(ss, 0.0f);
+    for (int z = 0; z < ss; ++z) p->lip[z] = (float)l2[z];
+    if (L_out)
+        for (int z = 0; z < ss; ++z) L_out[z] = p->lip[z];
+    return XCT_OK;
+}
+
+int xct_fista_set_lipschitz(xct_plan *p, const float *L)
+{
+    if (!p || !L) return xct_fail(XCT_E_INVALID, "xct_fista_set_lipschitz: null argument");
+    for (int z = 0; z < p->g.ss; ++z)
+        if (!(L[z] > 0.0f && L[z] < 3.0e38f))
+            return xct_fail(XCT_E_INVALID, "xct_fista_set_lipschitz: every L must be finite and > 0");
+    p->lip.assign(L, L + p->g.ss);
+    return XCT_OK;
+}
+
+// FISTA_execution (GPU.cpp:1755-1924) on dN slices on the device, with the reference's kernel
+// argument bindings: the sinogram correction if the plan has one (the uncorrected sinogram
+// stays in the residual image, :1812-1816); x = the plain backprojection of subset sub[0]
+// (:1853-1858), w = x, beta = 0; per subset AART1 (the residual of x in the first cycle, of w
+// after), the gradient step v (FISTAbackProjection, or with XCT_FISTA_ADJOINT the exact
+// adjoint), then ISTA3D(v) into dest in the first cycle and FISTA3D(x, v, beta) after --
+// whose x_{t+1} the reference writes into the beta image, where beta_{t+1} overwrites it
+// (:1867-1868), so dest keeps the first cycle's result; XCT_FISTA_UPDATE_X stores x_{t+1} in
+// dest instead -- and x = dest.  The residual image is the plan's ratio buffer.
+static int fista_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, float alpha,
+                      double lambda_d, int flags, cudaStream_t st)
+{
+    const KGeom &g = p->kg;
+    const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.px * g.pa, nb = (size_t)p->g.max_batch;
+    if (!p->d_fista) {
+        cudaError_t e = cudaMalloc(&p->d_fista, sizeof(float) * 4 * nb * nimg);
+        if (e != cudaSuccess) {
+            p->d_fista = nullptr;
+            return xct_cuda_fail(e, "cudaMalloc FISTA buffers");
+        }
+    }
+    float *v = p->d_fista, *w = v + nb * nimg, *beta = w + nb * nimg, *dest = beta + nb * nimg;
+    float *res = p->d_ratio;
+    const size_t ibytes = sizeof(float) * dN * nimg, pbytes = sizeof(float) * dN * nprj;
+    const float *meas = d_sino;
+    int rc;
+    if (p->g.correction_mode > 0) {
+        rc = launch_sino_correction(g, d_sino, p->d_corr, p->d_corr_ang, p->d_corr_bin, p->g.correction_mode, dN, st);
+        if (rc) return rc;
+        meas = p->d_corr;
+        XCT_CUDA_TRY(cudaMemcpyAsync(res, d_sino, pbytes, cudaMemcpyDeviceToDevice, st));
+    } else {
+        XCT_CUDA_TRY(cudaMemsetAsync(res, 0, pbytes, st));
+    }
+    rc = launch_bp_ref_plain(g, p->d_trig, meas, dest, dN, sub[0], g.ss, st);
+    if (rc) return rc;
+    XCT_CUDA_TRY(cudaMemcpyAsync(d_img, dest, ibytes, cudaMemcpyDeviceToDevice, st));
+    XCT_CUDA_TRY(cudaMemcpyAsync(w, d_img, ibytes, cudaMemcpyDeviceToDevice, st));
+    XCT_CUDA_TRY(cudaMemsetAsync(beta, 0, ibytes, st));
+    const float *X = d_img;
+    bool first = true;
+    for (int i = 0; i < it; ++i)
+        for (int k = 0; k < g.ss; ++k) {
+            const int s = sub[k];
+            const int rows = subset_rows(p, s);
+            const float L = p->lip[s];
+            // AART1: the forward projection into the subset's residual rows, then y - A x there
+            if (p->g.kernels == XCT_KERNELS_TILED)
+                rc = launch_fwd_tiled(g, p->d_trig, X, nullptr, res, p->d_acc, dN, s, g.ss, rows, st);
+            else rc = launch_fwd_plain(g, p->d_trig, X, nullptr, res, dN, s, g.ss, rows, st);
+            if (!rc) rc = launch_residual(g, meas, res, dN, s, g.ss, rows, st);
+            if (rc) return rc;
+            if (flags & XCT_FISTA_ADJOINT) {
+                const float coef = ((((alpha * (float)g.ss) / (float)g.pa) / (float)g.depth) / L) * 0.5f;
+                rc = launch_adj_subset(g, p->d_trig, res, v, dN, s, g.ss, (g.pa - s + g.ss - 1) / g.ss, X, coef, st);
+            } else {
+                rc = launch_fista_bp(g, p->d_trig, X, v, res, dN, s, alpha, L, st);
+            }
+            if (rc) return rc;
+            const float lam = (float)(lambda_d / (double)L * 0.5);  // LAMBDA_FISTA/L[sub]*0.5f
+            if (first) {
+                rc = launch_ista3d(v, dest, g.nx, g.ny, dN, lam, p->ctx->sm_count, st);
+                X = w;
+                first = false;
+            } else {
+                rc = launch_fista3d(d_img, w, v, beta, (flags & XCT_FISTA_UPDATE_X) ? dest : nullptr, g.nx, g.ny, dN,
+                                    lam, p->ctx->sm_count, st);
+            }
+            if (rc) return rc;
+            XCT_CUDA_TRY(cudaMemcpyAsync(d_img, dest, ibytes, cudaMemcpyDeviceToDevice, st));
+        }
+    return XCT_OK;
+}
+
+static int check_fista(xct_plan *p, float alpha, float cs_lambda, int flags, cudaStream_t st)
+{
+    if (!(alpha > -1.0e30f && alpha < 1.0e30f)) return xct_fail(XCT_E_INVALID, "FISTA: alpha must be finite");
+    if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
+        return xct_fail(XCT_E_INVALID, "FISTA: cs_lambda must be finite and >= 0");
+    if (flags & ~(XCT_FISTA_UPDATE_X | XCT_FISTA_ADJOINT)) return xct_fail(XCT_E_INVALID, "FISTA: unknown flags");
+    // FISTA_ocl estimates the Lipschitz constants before reconstructing (GPU.cpp:2250-2256)
+    if ((int)p->lip.size() != p->g.ss) return xct_fista_power_iteration(p, 30, 1024, 0, nullptr, st);
+    return XCT_OK;
+}
+
+// -D LAMBDA_FISTA: the float CSlambda streamed with six significant digits (FISTA_programBuild,
+// GPU.cpp:2044), compiled as a double literal.
+static double fista_lambda_literal(float cs_lambda)
+{
+    char b[64];
+    snprintf(b, sizeof b, "%g", (double)cs_lambda);
+    return strtod(b, nullptr);
+}
+
+int xct_fista_run_device(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, float alpha,
+                         float cs_lambda, int flags, void *stream)
+{
+    XCT_RANGE("xct_fista_run_device");
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    if (!d_sino || !d_img) return xct_fail(XCT_E_INVALID, "xct_fista_run_device: null device pointer");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = check_fista(p, alpha, cs_lambda, flags, st);
+    if (rc) return rc;
+    return fista_loop(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, alpha,
+                      fista_lambda_literal(cs_lambda), flags, st);
+}
+
+int xct_fista_run(xct_plan *p, int dN, const float *const *sino_host, float *const *img_host, const int *sub, int it,
+                  float alpha, float cs_lambda, int flags)
+{
+    XCT_RANGE("xct_fista_run");
+    if (p && it < 0) it = p->g.it;
+    int rc = check_run(p, dN, sub, it);
+    if (rc) return rc;
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    rc = check_fista(p, alpha, cs_lambda, flags, p->stream);
+    if (rc) return rc;
+    const double lam = fista_lambda_literal(cs_lambda);
+    // the images' initial contents are not read: the backprojection of subset sub[0] replaces them
+    return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
+        return fista_loop(p, dN, p->d_sino, p->d_img, sub ? sub : p->sub_default.data(), it, alpha, lam, flags, st);
+    });
 }
 
 int xct_plan_sync(xct_plan *p)

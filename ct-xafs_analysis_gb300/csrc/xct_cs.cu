@@ -76,8 +76,9 @@ __global__ void ista3d_kernel(const float *__restrict__ v, float *__restrict__ x
     }
 }
 
-// w and beta are read and written at the voxel's own index only (in place).
-__global__ void fista3d_kernel(float *__restrict__ w, const float *__restrict__ v, float *__restrict__ beta,
+// x_in (the image x_t), w and beta are read and written at the voxel's own index only, so
+// x_in may be w itself (FISTA_OSEM_execution passes w as x_t); x_new may be null (not stored).
+__global__ void fista3d_kernel(const float *x_in, float *w, const float *__restrict__ v, float *__restrict__ beta,
                                float *__restrict__ x_new, int nx, int ny, int dN, float lambda)
 {
     const long long total = (long long)nx * ny * dN;
@@ -86,9 +87,9 @@ __global__ void fista3d_kernel(float *__restrict__ w, const float *__restrict__ 
         const int X = (int)(i % nx);
         const long long r = i / nx;
         const int Y = (int)(r % ny), Z = (int)(r / ny);
-        const float xi = w[i], b = beta[i];
+        const float xi = x_in[i], b = beta[i];
         const float x = cs_select(v, nx, ny, dN, X, Y, Z, lambda);
-        x_new[i] = x;
+        if (x_new) x_new[i] = x;
         float bn = b * b * 4.0f + 1.0f;
         bn = (sqrtf(bn) + 1.0f) * 0.5f;
         const float g = __fdiv_rn(b - 1.0f, bn);
@@ -114,10 +115,10 @@ int launch_ista3d(const float *v, float *x_new, int nx, int ny, int dN, float la
     return XCT_OK;
 }
 
-int launch_fista3d(float *w, const float *v, float *beta, float *x_new, int nx, int ny, int dN, float lambda,
-                   int sm_count, cudaStream_t st)
+int launch_fista3d(const float *x_in, float *w, const float *v, float *beta, float *x_new, int nx, int ny, int dN,
+                   float lambda, int sm_count, cudaStream_t st)
 {
-    fista3d_kernel<<<cs_grid((long long)nx * ny * dN, sm_count), 256, 0, st>>>(w, v, beta, x_new, nx, ny, dN,
+    fista3d_kernel<<<cs_grid((long long)nx * ny * dN, sm_count), 256, 0, st>>>(x_in, w, v, beta, x_new, nx, ny, dN,
                                                                                 lambda);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return xct_cuda_fail(e, "fista3d_kernel launch");

@@ -65,6 +65,11 @@ struct xct_plan {
     float *d_fi = nullptr;       // [max_batch] focus indices
     float *d_cs = nullptr;       // compressed-sensing OS-EM: w, beta, x' [3][max_batch][ny][nx],
                                  // allocated by the first such run
+    float *d_fista = nullptr;    // FISTA: v, w, beta, dest [4][max_batch][ny][nx] (first FISTA run)
+    float *d_pi = nullptr;       // power iteration: layer images, candidate, projection (first use)
+    double *d_pi_l2 = nullptr;   // power iteration: squared norms of the candidates [ss]
+    int pi_layers = 0;           // layer images d_pi holds
+    std::vector<float> lip;      // Lipschitz estimates L[ss] of the subset operators (empty: none)
     float *d_sino2 = nullptr;    // volume streaming: the second staging set (first volume run)
     float *d_img2 = nullptr;
     cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
@@ -166,8 +171,25 @@ const char *xct_tune_env_path();
 void xct_plan_default_tuning(xct_plan *p);
 // Compressed-sensing proximal steps (xct_cs.cu): ISTA3D, FISTA3D over dN slices.
 int launch_ista3d(const float *v, float *x_new, int nx, int ny, int dN, float lambda, int sm_count, cudaStream_t st);
-int launch_fista3d(float *w, const float *v, float *beta, float *x_new, int nx, int ny, int dN, float lambda,
-                   int sm_count, cudaStream_t st);
+// FISTA3D with x_t read from x_in (may equal w) and x_{t+1} stored to x_new (may be null).
+int launch_fista3d(const float *x_in, float *w, const float *v, float *beta, float *x_new, int nx, int ny, int dN,
+                   float lambda, int sm_count, cudaStream_t st);
+// FISTA with compressed sensing (xct_fista.cu): the power iteration's backprojection (powerIter2,
+// rows th = sub + k*step, k < nrows, of prj [pa][px]) into cnd, the squared L2 norm of cnd over
+// columns [0, nxe) and rows [0, nye) into *out (double), the normalisation powerIter3; the AART1
+// residual in place on the subset rows of the forward projection `out`; FISTAbackProjection.
+int launch_pi_bp(const KGeom &g, const float2 *trig, const float *prj, float *cnd, int sub, int step, int nrows,
+                 float scale, cudaStream_t st);
+int launch_pi_l2(const float *cnd, int nx, int nxe, int nye, double *out, int sm_count, cudaStream_t st);
+int launch_pi_norm(const float *cnd, float *img, int nx, int ny, const double *l2, int fetch, cudaStream_t st);
+int launch_residual(const KGeom &g, const float *meas, float *out, int dN, int sub, int step, int nrows,
+                    cudaStream_t st);
+int launch_fista_bp(const KGeom &g, const float2 *trig, const float *x, float *v, const float *res, int dN, int sub,
+                    float alpha, float L, cudaStream_t st);
+// The exact adjoint over the angles th = sub + k*step, k < nang (all angles: 0, 1, pa); with
+// base non-null the result is base + scale * A^T sino.
+int launch_adj_subset(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, int sub, int step,
+                      int nang, const float *base, float scale, cudaStream_t st);
 // Rotation-centre search (xct_rcs.cu).
 void xct_mask_params(int W, int H, float shift, float ang_min, float ang_max, float *prm16);
 float xct_shift_value(float start, float step, int i);

@@ -619,10 +619,14 @@ constexpr int kAdjWarps = kThreads / 32;  // one angle per warp and window
 // rounds by at most 2^-16 of the ray's value, below the weight error of float32 sample
 // coordinates), smaller ones -- and every ray of a window with a non-finite value or one above
 // 1e30 -- scatter float atomics, which keep full relative precision.
+// The angles are th = sub + k*step for k < nang (all: 0, 1, pa); with base non-null the
+// output is base + scale * (A^T sino) (a gradient step).
 template <int T>
 __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__restrict__ sino,
                                                              float *__restrict__ img,
-                                                             const float2 *__restrict__ trig, KGeom g, int ntx)
+                                                             const float2 *__restrict__ trig, KGeom g, int ntx,
+                                                             int sub, int step, int nang,
+                                                             const float *__restrict__ base, float scale)
 {
     constexpr int kAdjT = T, kAdjP = T + 2;  // this launch's tile side and pitch
     __shared__ float accs[kAdjP * kAdjP];
@@ -642,9 +646,9 @@ __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__rest
     const float ylo = (float)(y0 - 1), yhi = (float)min(y0 + kAdjT, g.ny);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int D = g.depth;
-    for (int w0 = 0; w0 < g.pa; w0 += kAdjWarps) {
-        const int th = w0 + warp;
-        const bool active = th < g.pa;
+    for (int w0 = 0; w0 < nang; w0 += kAdjWarps) {
+        const bool active = w0 + warp < nang;
+        const int th = active ? sub + (w0 + warp) * step : 0;
         float c = 1.0f, s = 0.0f;
         int Xlo = 0, Xhi = -1;
         if (active) {
@@ -762,10 +766,15 @@ __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__rest
         __syncthreads();  // the integers are clear and wmax may be rewritten
     }
     float *im = img + (size_t)z * g.nx * g.ny;
+    const float *bz = base ? base + (size_t)z * g.nx * g.ny : nullptr;
     for (int i = threadIdx.x; i < kAdjT * kAdjT; i += kThreads) {
         const int r = i / kAdjT, cc = i - r * kAdjT;
         const int X = x0 + cc, Y = y0 + r;
-        if (X < g.nx && Y < g.ny) im[(size_t)Y * g.nx + X] = accs[(r + 1) * kAdjP + cc + 1];
+        if (X < g.nx && Y < g.ny) {
+            const float a = accs[(r + 1) * kAdjP + cc + 1];
+            const size_t o = (size_t)Y * g.nx + X;
+            im[o] = bz ? fmaf(scale, a, __ldg(bz + o)) : a;
+        }
     }
 }
 
@@ -1239,14 +1248,22 @@ int launch_fwd_tiled(const KGeom &g, const float2 *trig, const float *img, const
 
 int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, cudaStream_t st)
 {
+    return launch_adj_subset(g, trig, sino, img, dN, 0, 1, g.pa, nullptr, 0.0f, st);
+}
+
+int launch_adj_subset(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, int sub, int step,
+                      int nang, const float *base, float scale, cudaStream_t st)
+{
     if (dN <= 0) return XCT_OK;
     const long long big = (long long)((g.nx + kAdjT - 1) / kAdjT) * ((g.ny + kAdjT - 1) / kAdjT) * dN;
     if (big >= 3LL * device_sm_count()) {
         const int ntx = (g.nx + kAdjT - 1) / kAdjT, nty = (g.ny + kAdjT - 1) / kAdjT;
-        adj_tiled_kernel<kAdjT><<<dim3(ntx * nty, 1, dN), kThreads, 0, st>>>(sino, img, trig, g, ntx);
+        adj_tiled_kernel<kAdjT><<<dim3(ntx * nty, 1, dN), kThreads, 0, st>>>(sino, img, trig, g, ntx, sub, step, nang,
+                                                                            base, scale);
     } else {
         const int ntx = (g.nx + kAdjTSmall - 1) / kAdjTSmall, nty = (g.ny + kAdjTSmall - 1) / kAdjTSmall;
-        adj_tiled_kernel<kAdjTSmall><<<dim3(ntx * nty, 1, dN), kThreads, 0, st>>>(sino, img, trig, g, ntx);
+        adj_tiled_kernel<kAdjTSmall><<<dim3(ntx * nty, 1, dN), kThreads, 0, st>>>(sino, img, trig, g, ntx, sub, step,
+                                                                                  nang, base, scale);
     }
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);
     XCT_CUDA_TRY(cudaGetLastError());

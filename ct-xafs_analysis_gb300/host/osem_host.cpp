@@ -31,7 +31,7 @@ struct DeviceSlot {
     std::thread input_th, reconst_th, output_th;
 };
 
-enum Method { METHOD_OSEM, METHOD_FBP, METHOD_HYBRID };
+enum Method { METHOD_OSEM, METHOD_FBP, METHOD_HYBRID, METHOD_FISTA };
 Method g_method = METHOD_OSEM;
 std::vector<int> g_sub;           // subset order (GPU.cpp:564-582)
 std::atomic<int> g_status{0};     // first failure (the reference exits on the spot)
@@ -72,6 +72,8 @@ void osem_thread(DeviceSlot *d, std::vector<float *> imgs, std::vector<float *> 
     const int dN = endN - startN + 1;
     int rc;
     if (g_method == METHOD_FBP) rc = xct_fbp_run(d->plan, dN, g_zp, prjs.data(), imgs.data());
+    else if (g_method == METHOD_FISTA)  // FISTA_thread (GPU.cpp:1927-1979)
+        rc = xct_fista_run(d->plan, dN, prjs.data(), imgs.data(), g_sub.data(), g_it, (float)g_wt1, CSlambda, 0);
     else if (g_method == METHOD_HYBRID && CSitBool)  // hybrid_thread's FISTA branch (GPU.cpp:1569-1571)
         rc = xct_hybrid_cs_run(d->plan, dN, g_zp, baseupOrder, prjs.data(), imgs.data(), g_sub.data(), g_it, CSlambda);
     else if (g_method == METHOD_HYBRID)
@@ -103,7 +105,9 @@ void osem_input_thread(DeviceSlot *d, int startN, int endN)
         imgs.push_back(new float[(size_t)g_ox * g_oy]);
         ok = ok && read_data_input(g_d1, slice_name(g_f1, i), prjs.back(), (size_t)g_px * g_pa);
         // FBP and the hybrid overwrite every pixel: no initial image to read
-        if (g_method == METHOD_OSEM) ok = ok && first_image(g_f4, imgs.back(), (size_t)g_ox * g_oy);
+        // (FISTA_input_thread reads it too, though FISTA_execution then replaces it)
+        if (g_method == METHOD_OSEM || g_method == METHOD_FISTA)
+            ok = ok && first_image(g_f4, imgs.back(), (size_t)g_ox * g_oy);
     }
     join(d->reconst_th);
     if (!ok) {
@@ -163,6 +167,14 @@ int run_pipeline(const std::vector<int> &devices, const std::vector<float> &ang,
             xct_ctx_destroy(d->ctx);
             return XCT_E_INVALID;
         }
+        // FISTA_ocl estimates the subset operators' Lipschitz constants once per device before
+        // dispatching (powerIteration on the input-thread slot, GPU.cpp:2246-2257)
+        if (method == METHOD_FISTA && xct_fista_power_iteration(d->plan, 30, 1024, 0, nullptr, nullptr) != XCT_OK) {
+            std::cerr << "ERROR: " << xct_last_error() << std::endl;
+            xct_osem_plan_destroy(d->plan);
+            xct_ctx_destroy(d->ctx);
+            return XCT_E_CUDA;
+        }
         char name[256] = {0};
         xct_device_name(dev, name, sizeof name);
         std::cout << "Device No. " << dev + 1 << ": " << name << ", " << d->dN << " slices per call" << std::endl;
@@ -219,6 +231,20 @@ int GPU()
     const std::vector<int> devices = parse_device_list(g_devList, ndev);
     time(&g_t0);
     switch (g_mode) {
+    case 1:
+    case 3:
+        // AART (1) and ASIRT (3): only their compressed-sensing form, FISTA_ocl (GPU.cpp:37-41,
+        // 53-58), is built.  Mode 3 calls FISTA_ocl with one subset; the reference's kernels and
+        // loop still use g_ss there (reading past its one-entry subset order when g_ss > 1), so
+        // this build runs mode 3 with one subset throughout.
+        if (!CSitBool) {
+            std::cerr << "ERROR: reconstruction method " << g_mode
+                      << " without compressed sensing (AART/ASIRT) is not part of this build; set CSitBool" << std::endl;
+            return XCT_E_UNSUPPORTED;
+        }
+        std::cout << "Processing by " << (g_mode == 1 ? "AART" : "ASIRT") << " method with FISTA compressed sensing"
+                  << std::endl << std::endl;
+        return run_pipeline(devices, g_ang, g_mode == 1 ? g_ss : 1, METHOD_FISTA);
     case 2:
         std::cout << "Processing by MART method" << std::endl << std::endl;
         return OSEM_gpu(devices, g_ang, g_pa);  // OS-EM with ss = pa (GPU.cpp:51)
@@ -239,7 +265,8 @@ int GPU()
         return run_pipeline(devices, g_ang, g_ss, METHOD_HYBRID);
     default:
         std::cerr << "ERROR: reconstruction method " << g_mode
-                  << " is not part of this build (OS-EM family 2, 4, 5, 6; FBP 7; hybrid 8)" << std::endl;
+                  << " is not part of this build (FISTA 1, 3 with CSitBool; OS-EM family 2, 4, 5, 6; FBP 7; hybrid 8)"
+                  << std::endl;
         return XCT_E_UNSUPPORTED;
     }
 }

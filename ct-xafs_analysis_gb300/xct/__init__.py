@@ -38,6 +38,9 @@ SUBSETS_REF = 0
 SUBSETS_COVER = 1
 KERNELS_TILED = 0
 KERNELS_PLAIN = 1
+PI_OWN_LAYER = 1
+FISTA_UPDATE_X = 1
+FISTA_ADJOINT = 2
 
 # Every function include/xct.h declares (checked by the tests against the header).
 EXPORTS = (
@@ -53,6 +56,7 @@ EXPORTS = (
     "xct_denoise_sinogram",
     "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
     "xct_plan_multislice", "xct_plan_set_multislice",
+    "xct_fista_power_iteration", "xct_fista_set_lipschitz", "xct_fista_run_device", "xct_fista_run",
     "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume", "xct_hybrid_cs_run_device",
     "xct_hybrid_cs_run",
 )
@@ -138,6 +142,11 @@ def load():
     L.xct_reslice_plan_set_wait_limit.argtypes = [vp, ctypes.c_longlong]
     L.xct_denoise_sinogram.argtypes = [ip, ip, ip, c_f, vp, vp, vp]
     L.xct_cs_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
+    L.xct_fista_power_iteration.argtypes = [vp, ip, ip, ip, fp, vp]
+    L.xct_fista_set_lipschitz.argtypes = [vp, fp]
+    L.xct_fista_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, c_f, ip, vp]
+    L.xct_fista_run.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int), ip, c_f,
+                                c_f, ip]
     L.xct_cs_osem_run.argtypes = [vp, ip, ctypes.POINTER(fp), ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int), ip,
                                   c_f]
     L.xct_hybrid_cs_run_device.argtypes = [vp, ip, ip, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
@@ -352,6 +361,31 @@ class OSEMPlan:
         _check(self._lib.xct_cs_osem_run(self.handle, len(sinos), s_arr, i_arr, self._sub(sub), it, cs_lambda))
         return imgs
 
+    def power_iteration(self, trials=30, work_group=1024, own_layer=False, stream=None):
+        """The Lipschitz estimates L[ss] of the subset operators (powerIteration); kept in the
+        plan for the FISTA runs.  own_layer: each subset projects its own estimate (the
+        reference projects layer 0's for every subset)."""
+        out = np.zeros(self.ss, np.float32)
+        _check(self._lib.xct_fista_power_iteration(self.handle, trials, work_group,
+                                                   PI_OWN_LAYER if own_layer else 0,
+                                                   out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                   _stream(stream)))
+        return out
+
+    def set_lipschitz(self, L):
+        a = np.ascontiguousarray(L, dtype=np.float32)
+        if a.size != self.ss:
+            raise XCTError(XCT_E_INVALID, "L needs one value per subset")
+        _check(self._lib.xct_fista_set_lipschitz(self.handle, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def fista_run(self, sinos, imgs, alpha=1.0, cs_lambda=1.0e-4, sub=None, it=-1, flags=0):
+        """FISTA with compressed sensing (FISTA_thread / FISTA_execution) on host arrays;
+        reconstructions written into ``imgs`` (their contents are not read)."""
+        s_arr, i_arr = self._host_arrays(sinos, imgs)
+        _check(self._lib.xct_fista_run(self.handle, len(sinos), s_arr, i_arr, self._sub(sub), it, alpha, cs_lambda,
+                                       flags))
+        return imgs
+
     def fbp_run(self, sinos, imgs, zp=0):
         """FBP (FBP_thread) on host arrays; reconstructions written into ``imgs``."""
         s_arr, i_arr = self._host_arrays(sinos, imgs)
@@ -392,6 +426,16 @@ class OSEMPlan:
         _need(d_img, dN * self.ny * self.nx, "d_img")
         _check(self._lib.xct_cs_osem_run_device(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it,
                                                 cs_lambda, _stream(stream)))
+
+    def fista_run_device(self, d_sino, d_img, alpha=1.0, cs_lambda=1.0e-4, dN=None, sub=None, it=-1, flags=0,
+                         stream=None):
+        """FISTA with compressed sensing (FISTA_execution) on device tensors [dN][pa][px] ->
+        [dN][ny][nx] (out)."""
+        dN = d_img.shape[0] if dN is None else dN
+        _need(d_sino, dN * self.pa * self.px, "d_sino")
+        _need(d_img, dN * self.ny * self.nx, "d_img")
+        _check(self._lib.xct_fista_run_device(self.handle, dN, _ptr(d_sino), _ptr(d_img), self._sub(sub), it, alpha,
+                                              cs_lambda, flags, _stream(stream)))
 
     def osem1(self, sub, d_img, d_sino, d_ratio, dN=None, stream=None):
         """OSEM1 (OSEM.cl:38-68) alone: ratio rows of subset ``sub`` into d_ratio."""

@@ -179,6 +179,44 @@ int xct_cs_osem_run_device(xct_plan *plan, int dN, const float *d_sino, float *d
 int xct_cs_osem_run(xct_plan *plan, int dN, const float *const *sino_host, float *const *img_host, const int *sub,
                     int it, float cs_lambda);
 
+/* ---- FISTA with compressed sensing: replaces FISTA_ocl / FISTA_thread / FISTA_execution
+ * (GPU.cpp:1755-2299), the path of GPU() modes 1 (AART, ss subsets) and 3 (ASIRT, one subset)
+ * with CSitBool (GPU.cpp:37-41, 53-58) --------------------------------------------------
+ * xct_fista_power_iteration : powerIteration (GPU.cpp:2079-2188, FISTA.cl:50-208): the
+ *     Lipschitz estimate L[s] of every subset operator, from `trials` rounds (the reference
+ *     runs 30) of forward projection (powerIter1), floor-rule backprojection (powerIter2),
+ *     the squared L2 norm (imageL2AbsX/Y over the columns and rows that work-groups of
+ *     min(work_group, nx) items visit; the reference's work_group is the device's
+ *     CL_DEVICE_MAX_WORK_GROUP_SIZE, 1024 on NVIDIA GPUs) and normalisation (powerIter3).
+ *     powerIter1 never sets the layer of its sampling coordinate (FISTA.cl:60): by default
+ *     every subset projects layer 0's estimate, as a zero-initialised coordinate does;
+ *     XCT_PI_OWN_LAYER projects each subset's own.  Stores L in the plan (and L_out [ss] when
+ *     not NULL).  Synchronous on `stream`.
+ * xct_fista_set_lipschitz : sets L [ss] directly (finite, > 0).
+ * xct_fista_run_device : FISTA_execution on dN slices, d_sino [dN][pa][px] in, d_img
+ *     [dN][ny][nx] out (its initial contents are not read: the first image is the plain
+ *     backprojection of subset sub[0], GPU.cpp:1853-1858).  alpha is the AART factor g_wt1
+ *     (main.cpp:35, default 1), cs_lambda CSlambda (main.cpp:46, default 1e-4).  Per subset:
+ *     AART1's residual, FISTAbackProjection's gradient step, ISTA3D (first cycle) or FISTA3D.
+ *     The reference writes FISTA3D's x_{t+1} into the beta image, where beta_{t+1} overwrites
+ *     it (GPU.cpp:1867-1868), so its image stays the first cycle's ISTA3D result; that is kept
+ *     by default.  flags: XCT_FISTA_UPDATE_X stores x_{t+1} as the next image;
+ *     XCT_FISTA_ADJOINT replaces FISTAbackProjection's floor-rule backprojection by the exact
+ *     adjoint of the forward projector (xct_adj).  A plan without L runs the power iteration
+ *     (30 trials, work group 1024) first.  The slices of one call are the proximal step's
+ *     third axis, as in the compressed-sensing OS-EM.  Uses the plan's ratio buffer; the plan
+ *     allocates four image-sized buffers per slice on the first call.
+ * xct_fista_run : the same from host buffers (FISTA_thread, GPU.cpp:1927-1979), blocking. */
+#define XCT_PI_OWN_LAYER 1
+#define XCT_FISTA_UPDATE_X 1
+#define XCT_FISTA_ADJOINT 2
+int xct_fista_power_iteration(xct_plan *plan, int trials, int work_group, int flags, float *L_out, void *stream);
+int xct_fista_set_lipschitz(xct_plan *plan, const float *L);
+int xct_fista_run_device(xct_plan *plan, int dN, const float *d_sino, float *d_img, const int *sub, int it,
+                         float alpha, float cs_lambda, int flags, void *stream);
+int xct_fista_run(xct_plan *plan, int dN, const float *const *sino_host, float *const *img_host, const int *sub,
+                  int it, float alpha, float cs_lambda, int flags);
+
 /* ---- the two OS-EM kernels as separate steps (dN slices, device memory) -------------
  * xct_osem1 : OSEM1 (OSEM.cl:38-68) for subset `sub`: forward-projects d_img and writes
  *             the measured/estimated ratio rows of the subset into d_ratio [dN][pa][px]

@@ -196,6 +196,46 @@ def test_fbp_and_hybrid_methods_from_files(host_bin, oracle_lib, tmp_path, metho
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("method", [1, 3])
+def test_fista_batches_from_files(host_bin, oracle_lib, tmp_path, method):
+    """Methods 1 (AART) and 3 (ASIRT) with CSitBool: FISTA_ocl -- the power iteration once per
+    device, then FISTA_execution on overlapping batches of 4 slices (overlap 1), as the
+    compressed-sensing OS-EM dispatches them (GPU.cpp:2258-2276).  Method 3 uses one subset."""
+    from xct import phantom as P
+    O = oracle_lib
+    n, px, pa, ss, it = 48, 48, 40, 4, 2
+    ang = P.uniform_angles(pa)
+    d1, d2 = tmp_path / "in", tmp_path / "out"
+    d1.mkdir()
+    with open(tmp_path / "angles.log", "w") as f:
+        for a in ang:
+            f.write("%.9g\n" % a)
+    prm = P.ellipsoid_params(n, 6, count=5, seed=19)
+    meas = {}
+    for z in range(7, 13):
+        meas[z] = P.noisy_log_sinogram(O.projection(P.ellipsoid_slice(prm, z - 7, n, n), ang, px), 1e4, z)
+        meas[z].astype(np.float32).tofile(d1 / ("s%04d.raw" % z))
+    inp = tmp_path / "run.inp"
+    keys = [("#逐次圧縮センシング計算 (FBP適応外)", "1"), ("#逐次圧縮センシング計算加算ファクター", "0.0002"),
+            ("#逐次圧縮センシング計算重複レイヤー数", "1"), ("#AARTファクター", "0.8")]
+    write_inp(inp, extra=keys, d1=str(d1), d2=str(d2), f3=str(tmp_path / "angles.log"), px=px, pa=pa, n=n, it=it,
+              ss=ss, layers=6, par=4, method=method)
+    r = subprocess.run([host_bin, str(inp)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    s_used = ss if method == 1 else 1
+    L = O.power_iteration(ang, n, n, px, s_used, trials=30)
+
+    def batch(zs):
+        return O.fista_run(np.zeros((len(zs), n, n)), np.stack([meas[z] for z in zs]), ang, s_used, it, L, 0.8, 2e-4)
+    b1, b2, b3 = batch(range(7, 11)), batch(range(9, 13)), batch(range(11, 13))
+    want = {7: b1[0], 8: b1[1], 9: b1[2], 10: b2[1], 11: b2[2], 12: b3[1]}
+    for z, ref in want.items():
+        got = np.fromfile(d2 / ("rec_%04d.img" % z), np.float32).reshape(n, n)
+        rel = np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)
+        assert rel <= 1e-4, (z, rel)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("method", [6, 8])
 def test_compressed_sensing_batches_from_files(host_bin, oracle_lib, tmp_path, method):
     """CSitBool with 4 slices per call overlapping by 1 (GPU.cpp:636-647, 449-460; the hybrid's
