@@ -51,6 +51,27 @@ void xct_trig_table(const float *ang_deg, int pa, std::vector<float2> &cs)
     }
 }
 
+// sinogramCorrection factors (reconstShare.cl:44-64): angle_pr = angle/180*PI (float
+// division, then a double PI, stored to float); a = b = 0.5 (GPU.cpp:182-183); per angle
+// cos(angle_pr) and the sine factor a + b cos, per bin cos(asin(theta)).
+void xct_corr_tables(const float *ang_deg, int pa, int px, std::vector<float> &af, std::vector<float> &bf)
+{
+    af.assign(2 * (size_t)pa, 0.0f);
+    bf.assign((size_t)px, 0.0f);
+    for (int th = 0; th < pa; ++th) {
+        const float q = ang_deg[th] / 180.0f;
+        const float apr = (float)((double)q * 3.14159265358979323846);
+        const float ca = (float)cos((double)apr);
+        af[2 * th] = ca;
+        af[2 * th + 1] = 0.5f + 0.5f * ca;
+    }
+    for (int X = 0; X < px; ++X) {
+        const float theta = 2.0f * fabsf((float)X - (float)px / 2.0f) / (float)px;
+        const float as = (float)asin((double)theta);
+        bf[X] = (float)cos((double)as);
+    }
+}
+
 // Subset order of OSEM_ocl (GPU.cpp:564-582): a power-of-two ss gives the bit-reversal
 // permutation (0, ss/2, ss/4, 3ss/4, ...); any other ss the identity.  Entry k alone:
 int xct_subset_at(int ss, int k)
@@ -68,6 +89,17 @@ int xct_subset_at(int ss, int k)
 void xct_subset_order_host(int ss, int *sub)
 {
     for (int j = 0; j < ss; ++j) sub[j] = xct_subset_at(ss, j);
+}
+
+// The kernels' lambda: -D LAMBDA_FISTA is the float CSlambda written by an ostream (six
+// significant digits, GPU.cpp:549) and compiled as a double literal; lambda =
+// LAMBDA_FISTA/L[sub]*0.5f with L[sub] = 0.5 for every subset (GPU.cpp:343, FISTA.cl:426).
+float xct_cs_kernel_lambda(float cs_lambda)
+{
+    char b[64];
+    snprintf(b, sizeof b, "%g", (double)cs_lambda);
+    const double d = strtod(b, nullptr);
+    return (float)(d / (double)0.5f * 0.5);
 }
 
 extern "C" {
@@ -268,19 +300,8 @@ int xct_osem_plan_create(xct_ctx *ctx, const xct_geom *geom, xct_plan **out)
         // sinogramCorrection factors (reconstShare.cl:44-64): angle_pr = angle/180*PI
         // (float division, then a double PI, stored to float); a = b = 0.5
         // (GPU.cpp:182-183).
-        std::vector<float> af(2 * (size_t)geom->pa), bf(geom->px);
-        for (int th = 0; th < geom->pa; ++th) {
-            const float q = p->angles[th] / 180.0f;
-            const float apr = (float)((double)q * 3.14159265358979323846);
-            const float ca = (float)cos((double)apr);
-            af[2 * th] = ca;
-            af[2 * th + 1] = 0.5f + 0.5f * ca;
-        }
-        for (int X = 0; X < geom->px; ++X) {
-            const float theta = 2.0f * fabsf((float)X - (float)geom->px / 2.0f) / (float)geom->px;
-            const float as = (float)asin((double)theta);
-            bf[X] = (float)cos((double)as);
-        }
+        std::vector<float> af, bf;
+        xct_corr_tables(p->angles.data(), geom->pa, geom->px, af, bf);
         if ((e = cudaMalloc(&p->d_corr, sizeof(float) * nb * nprj)) != cudaSuccess) return fail(e, "cudaMalloc corr");
         if ((e = cudaMalloc(&p->d_corr_ang, sizeof(float) * af.size())) != cudaSuccess) return fail(e, "corr ang");
         if ((e = cudaMalloc(&p->d_corr_bin, sizeof(float) * bf.size())) != cudaSuccess) return fail(e, "corr bin");
@@ -806,7 +827,6 @@ int xct_fbp_run_device(xct_plan *p, int dN, int zp, const float *d_sino, float *
 
 static int cs_loop(xct_plan *p, int dN, const float *d_sino, float *d_img, const int *sub, int it, float lambda,
                    cudaStream_t st, bool correct = true);
-static float cs_kernel_lambda(float cs_lambda);
 
 // hybrid_thread (GPU.cpp:1458-1600): FBP_execution with the sinogram correction, the
 // base-up of FBPcorrection = 1 (slice minimum, then baseUp with baseupOrder), then
@@ -941,7 +961,7 @@ int xct_hybrid_cs_run_device(xct_plan *p, int dN, int zp, int baseup_order, cons
     if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
     return hybrid_device(p, dN, zp, baseup_order, d_sino, d_img, sub, it, (cudaStream_t)stream, true,
-                         cs_kernel_lambda(cs_lambda));
+                         xct_cs_kernel_lambda(cs_lambda));
 }
 
 int xct_hybrid_cs_run(xct_plan *p, int dN, int zp, int baseup_order, const float *const *sino_host,
@@ -955,7 +975,7 @@ int xct_hybrid_cs_run(xct_plan *p, int dN, int zp, int baseup_order, const float
     if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
         return xct_fail(XCT_E_INVALID, "xct_hybrid_cs_run: cs_lambda must be finite and >= 0");
     if ((rc = xct_fbp_check_zp(p->g.px, zp))) return rc;
-    const float lam = cs_kernel_lambda(cs_lambda);
+    const float lam = xct_cs_kernel_lambda(cs_lambda);
     return host_run(p, dN, sino_host, img_host, false, [&](cudaStream_t st) {
         return hybrid_device(p, dN, zp, baseup_order, p->d_sino, p->d_img, sub, it, st, true, lam);
     });
@@ -1051,17 +1071,6 @@ int xct_osem_run_volume(xct_plan *p, int n, const float *const *sino_host, float
 }
 
 // ------------------------------------------------------ compressed-sensing OS-EM (FISTA)
-// The kernels' lambda: -D LAMBDA_FISTA is the float CSlambda written by an ostream (six
-// significant digits, GPU.cpp:549) and compiled as a double literal; lambda =
-// LAMBDA_FISTA/L[sub]*0.5f with L[sub] = 0.5 for every subset (GPU.cpp:343, FISTA.cl:426).
-static float cs_kernel_lambda(float cs_lambda)
-{
-    char b[64];
-    snprintf(b, sizeof b, "%g", (double)cs_lambda);
-    const double d = strtod(b, nullptr);
-    return (float)(d / (double)0.5f * 0.5);
-}
-
 // FISTA_OSEM_execution (GPU.cpp:243-405) on dN slices on the device.  Per subset: OSEM1 and
 // OSEM2 (in place: the image becomes v, the OS-EM update), then FISTA3D(w, v, beta) writes x'
 // (then copied into the image), w' and beta' (in place).  The first cycle runs ISTA3D on the
@@ -1123,7 +1132,7 @@ int xct_cs_osem_run_device(xct_plan *p, int dN, const float *d_sino, float *d_im
     if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
         return xct_fail(XCT_E_INVALID, "xct_cs_osem_run_device: cs_lambda must be finite and >= 0");
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
-    return cs_loop(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, cs_kernel_lambda(cs_lambda),
+    return cs_loop(p, dN, d_sino, d_img, sub ? sub : p->sub_default.data(), it, xct_cs_kernel_lambda(cs_lambda),
                    (cudaStream_t)stream);
 }
 
@@ -1136,7 +1145,7 @@ int xct_cs_osem_run(xct_plan *p, int dN, const float *const *sino_host, float *c
     if (rc) return rc;
     if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
         return xct_fail(XCT_E_INVALID, "xct_cs_osem_run: cs_lambda must be finite and >= 0");
-    const float lam = cs_kernel_lambda(cs_lambda);
+    const float lam = xct_cs_kernel_lambda(cs_lambda);
     return host_run(p, dN, sino_host, img_host, true, [&](cudaStream_t st) {
         return cs_loop(p, dN, p->d_sino, p->d_img, sub ? sub : p->sub_default.data(), it, lam, st);
     });

@@ -39,6 +39,18 @@ struct xct_batch_plan {
     cudaStream_t cap = nullptr;       // capture stream
     cudaGraphExec_t exec = nullptr;
     size_t queue_bytes = 0;
+    // sinogram correction: corrected sinograms and factor tables of the items that have one
+    float *d_corr = nullptr;
+    float *d_corr_fac = nullptr;
+    int max_px = 0, max_pa = 0;
+    bool any_corr = false;
+    // compressed sensing over stacks of consecutive slices (empty: off)
+    std::vector<int> stack_first;     // first item of each stack
+    std::vector<XctStackDev> stacks;  // descriptors (images filled per run)
+    XctStackDev *d_stacks = nullptr;
+    float *d_cs = nullptr;            // w, beta, x' of every stack
+    long long max_vox = 0;
+    float cs_lambda = 0.0f;           // the kernels' lambda
 };
 
 static void batch_free(xct_batch_plan *p)
@@ -52,6 +64,10 @@ static void batch_free(xct_batch_plan *p)
     cudaFree(p->d_trig);
     cudaFree(p->d_ratio);
     cudaFree(p->d_acc);
+    cudaFree(p->d_corr);
+    cudaFree(p->d_corr_fac);
+    cudaFree(p->d_stacks);
+    cudaFree(p->d_cs);
     delete p;
 }
 
@@ -97,8 +113,6 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         if (rc) return rc;
         if (geoms[i].ss != ss)
             return xct_fail(XCT_E_INVALID, "xct_batch_plan_create: every slice of a batch needs the same subset count");
-        if (geoms[i].correction_mode != 0)
-            return xct_fail(XCT_E_UNSUPPORTED, "xct_batch_plan_create: sinogram correction is not available in batches");
     }
     XCT_CUDA_TRY(cudaSetDevice(ctx->device));
     xct_batch_plan *p = new (std::nothrow) xct_batch_plan();
@@ -115,7 +129,7 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         return r;
     };
     // sizes
-    size_t n_trig = 0, n_ratio = 0, n_acc = 0;
+    size_t n_trig = 0, n_ratio = 0, n_acc = 0, n_corr = 0, n_fac = 0;
     p->host.resize(n);
     for (int i = 0; i < n; ++i) {
         const xct_geom &g = geoms[i];
@@ -133,9 +147,17 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         k.cx = g.center_bin < 0.0f ? (float)g.px * 0.5f : g.center_bin;
         k.fetch = g.measured_fetch_mode;
         d.cover = g.subset_mode == XCT_SUBSETS_COVER;
+        d.corr_mode = g.correction_mode;
         n_trig += g.pa;
         n_ratio += (size_t)g.pa * g.px;
         n_acc += (size_t)((g.pa + g.ss - 1) / g.ss) * g.px;
+        p->max_px = std::max(p->max_px, g.px);
+        p->max_pa = std::max(p->max_pa, g.pa);
+        if (g.correction_mode > 0) {
+            p->any_corr = true;
+            n_corr += (size_t)g.pa * g.px;
+            n_fac += 2 * (size_t)g.pa + g.px;
+        }
     }
     cudaError_t e;
     if ((e = cudaMalloc(&p->d_items, sizeof(XctItemDev) * n)) != cudaSuccess) return fail(e, "cudaMalloc items");
@@ -151,8 +173,13 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
     // finalize kernel clears what it reads
     if ((e = cudaMemset(p->d_ratio, 0, sizeof(float) * n_ratio)) != cudaSuccess) return fail(e, "memset ratio");
     if ((e = cudaMemset(p->d_acc, 0, sizeof(double) * n_acc)) != cudaSuccess) return fail(e, "memset acc");
-    size_t ot = 0, orat = 0, oacc = 0;
+    if (p->any_corr) {
+        if ((e = cudaMalloc(&p->d_corr, sizeof(float) * n_corr)) != cudaSuccess) return fail(e, "cudaMalloc corr");
+        if ((e = cudaMalloc(&p->d_corr_fac, sizeof(float) * n_fac)) != cudaSuccess) return fail(e, "cudaMalloc fac");
+    }
+    size_t ot = 0, orat = 0, oacc = 0, ocorr = 0, ofac = 0;
     std::vector<float2> cs;
+    std::vector<float> af, bf;
     for (int i = 0; i < n; ++i) {
         const xct_geom &g = geoms[i];
         XctItemDev &d = p->host[i];
@@ -164,6 +191,23 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         d.acc = p->d_acc + oacc;
         d.sino = nullptr;
         d.img = nullptr;
+        d.sino_in = nullptr;
+        d.corr = nullptr;
+        d.corr_ang = nullptr;
+        d.corr_bin = nullptr;
+        if (g.correction_mode > 0) {
+            xct_corr_tables(g.angles_deg, g.pa, g.px, af, bf);
+            if ((e = cudaMemcpy(p->d_corr_fac + ofac, af.data(), sizeof(float) * af.size(), cudaMemcpyHostToDevice)) !=
+                    cudaSuccess ||
+                (e = cudaMemcpy(p->d_corr_fac + ofac + af.size(), bf.data(), sizeof(float) * bf.size(),
+                                cudaMemcpyHostToDevice)) != cudaSuccess)
+                return fail(e, "upload correction factors");
+            d.corr = p->d_corr + ocorr;
+            d.corr_ang = p->d_corr_fac + ofac;
+            d.corr_bin = p->d_corr_fac + ofac + af.size();
+            ocorr += (size_t)g.pa * g.px;
+            ofac += af.size() + bf.size();
+        }
         ot += g.pa;
         orat += (size_t)g.pa * g.px;
         oacc += (size_t)((g.pa + g.ss - 1) / g.ss) * g.px;
@@ -207,18 +251,36 @@ extern "C" int xct_batch_plan_destroy(xct_batch_plan *p)
     return XCT_OK;
 }
 
-// Capture the whole loop: clear the queue counters, then it x ss subset steps.
+// Capture the whole loop: clear the queue counters, the corrections (if any), then it x ss
+// subset steps -- with compressed sensing, w = x and beta = 0 first, the first subset step is
+// ISTA3D of the images before any OS-EM update (FISTA_OSEM_execution passes the image before
+// that subset's update to ISTA3D, GPU.cpp:335-336, so that OS-EM step is dead work and is
+// skipped, as in the single-shape plans), and every later one is the OS-EM step then FISTA3D,
+// each proximal result copied back into the images.
 static int capture(xct_batch_plan *p)
 {
     cudaGraph_t graph = nullptr;
     XCT_CUDA_TRY(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
     int rc = XCT_OK;
+    const int sm = p->ctx->sm_count, ns = (int)p->stacks.size();
+    const bool cs = ns > 0;
     cudaError_t e = cudaMemsetAsync(p->d_queues, 0, p->queue_bytes, p->cap);
     if (e != cudaSuccess) rc = xct_cuda_fail(e, "capture memset");
+    if (rc == XCT_OK && p->any_corr) rc = launch_sino_correction_batched(p->d_items, p->n, p->max_px, p->max_pa, p->cap);
+    if (rc == XCT_OK && cs) rc = launch_stack_copy(p->d_stacks, ns, p->max_vox, 1, sm, p->cap);
+    bool first = true;
     for (int i = 0; i < p->it && rc == XCT_OK; ++i)
-        for (int k = 0; k < p->ss && rc == XCT_OK; ++k)
-            rc = launch_osem_step_batched(p->d_items, p->d_bases, p->n, p->sub[k],
-                                          p->d_queues + 3 * (size_t)(i * p->ss + k), p->grids, p->fwd_T, p->cap);
+        for (int k = 0; k < p->ss && rc == XCT_OK; ++k) {
+            if (cs && first) {
+                rc = launch_ista3d_stacks(p->d_stacks, ns, p->max_vox, p->cs_lambda, sm, p->cap);
+                first = false;
+            } else {
+                rc = launch_osem_step_batched(p->d_items, p->d_bases, p->n, p->sub[k],
+                                              p->d_queues + 3 * (size_t)(i * p->ss + k), p->grids, p->fwd_T, p->cap);
+                if (rc == XCT_OK && cs) rc = launch_fista3d_stacks(p->d_stacks, ns, p->max_vox, p->cs_lambda, sm, p->cap);
+            }
+            if (rc == XCT_OK && cs) rc = launch_stack_copy(p->d_stacks, ns, p->max_vox, 0, sm, p->cap);
+        }
     e = cudaStreamEndCapture(p->cap, &graph);
     if (rc == XCT_OK && e != cudaSuccess) rc = xct_cuda_fail(e, "cudaStreamEndCapture");
     if (rc == XCT_OK) {
@@ -240,14 +302,91 @@ extern "C" int xct_batch_run(xct_batch_plan *p, const float *const *d_sino, floa
         int rc = capture(p);
         if (rc) return rc;
     }
+    // a stack's images must be one [dN][ny][nx] array
+    for (size_t s = 0; s < p->stacks.size(); ++s) {
+        const int f = p->stack_first[s];
+        const size_t m = (size_t)p->stacks[s].nx * p->stacks[s].ny;
+        for (int j = 1; j < p->stacks[s].dN; ++j)
+            if (d_img[f + j] != d_img[f] + j * m)
+                return xct_fail(XCT_E_INVALID,
+                                "xct_batch_run: with compressed sensing, the images of a stack must be consecutive in "
+                                "one array");
+        p->stacks[s].img = d_img[f];
+    }
     for (int i = 0; i < p->n; ++i) {
-        p->host[i].sino = d_sino[i];
+        p->host[i].sino_in = d_sino[i];
+        p->host[i].sino = p->host[i].corr_mode > 0 ? p->host[i].corr : d_sino[i];
         p->host[i].img = d_img[i];
     }
     cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
     XCT_CUDA_TRY(cudaMemcpyAsync(p->d_items, p->host.data(), sizeof(XctItemDev) * p->n, cudaMemcpyHostToDevice, st));
+    if (!p->stacks.empty())
+        XCT_CUDA_TRY(cudaMemcpyAsync(p->d_stacks, p->stacks.data(), sizeof(XctStackDev) * p->stacks.size(),
+                                     cudaMemcpyHostToDevice, st));
     XCT_CUDA_TRY(cudaGraphLaunch(p->exec, st));
-    g_xct_launches.fetch_add((long long)3 * p->it * p->ss, std::memory_order_relaxed);
+    // three per OS-EM step (the first step has none with compressed sensing), the
+    // correction, and with compressed sensing the setup copy plus two per step
+    const long long steps = (long long)p->it * p->ss, cs = p->stacks.empty() ? 0 : 1;
+    g_xct_launches.fetch_add(3 * (steps - cs) + (p->any_corr ? 1 : 0) + cs * (1 + 2 * steps),
+                             std::memory_order_relaxed);
+    return XCT_OK;
+}
+
+// Compressed sensing over stacks: stack_len[s] consecutive items of one shape form stack s
+// (the lengths add up to the batch's n); nstacks 0 turns it off.  The captured graph is
+// dropped (the next run captures again).
+extern "C" int xct_batch_plan_set_cs(xct_batch_plan *p, float cs_lambda, int nstacks, const int *stack_len)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "xct_batch_plan_set_cs: plan is null");
+    if (nstacks < 0 || (nstacks > 0 && !stack_len)) return xct_fail(XCT_E_INVALID, "xct_batch_plan_set_cs: bad stacks");
+    if (!(cs_lambda >= 0.0f && cs_lambda < 1.0e30f))
+        return xct_fail(XCT_E_INVALID, "xct_batch_plan_set_cs: cs_lambda must be finite and >= 0");
+    XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    std::vector<int> first;
+    std::vector<XctStackDev> st;
+    long long total = 0, max_vox = 0;
+    int at = 0;
+    for (int s = 0; s < nstacks; ++s) {
+        const int len = stack_len[s];
+        if (len <= 0 || at + len > p->n) return xct_fail(XCT_E_INVALID, "xct_batch_plan_set_cs: stack lengths exceed n");
+        const KGeom &g0 = p->host[at].g;
+        for (int j = 1; j < len; ++j)
+            if (p->host[at + j].g.nx != g0.nx || p->host[at + j].g.ny != g0.ny)
+                return xct_fail(XCT_E_INVALID, "xct_batch_plan_set_cs: the slices of a stack need one image size");
+        XctStackDev d = {nullptr, nullptr, nullptr, nullptr, g0.nx, g0.ny, len};
+        first.push_back(at);
+        st.push_back(d);
+        const long long v = (long long)g0.nx * g0.ny * len;
+        total += v;
+        max_vox = std::max(max_vox, v);
+        at += len;
+    }
+    if (nstacks > 0 && at != p->n) return xct_fail(XCT_E_INVALID, "xct_batch_plan_set_cs: stack lengths must add up to n");
+    cudaFree(p->d_cs);
+    cudaFree(p->d_stacks);
+    p->d_cs = nullptr;
+    p->d_stacks = nullptr;
+    p->stacks.clear();
+    p->stack_first.clear();
+    if (p->exec) {
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+    }
+    if (nstacks == 0) return XCT_OK;
+    XCT_CUDA_TRY(cudaMalloc(&p->d_cs, sizeof(float) * 3 * (size_t)total));
+    XCT_CUDA_TRY(cudaMalloc(&p->d_stacks, sizeof(XctStackDev) * nstacks));
+    long long o = 0;
+    for (auto &d : st) {
+        const long long v = (long long)d.nx * d.ny * d.dN;
+        d.w = p->d_cs + o;
+        d.beta = p->d_cs + total + o;
+        d.xn = p->d_cs + 2 * total + o;
+        o += v;
+    }
+    p->stacks = st;
+    p->stack_first = first;
+    p->max_vox = max_vox;
+    p->cs_lambda = xct_cs_kernel_lambda(cs_lambda);
     return XCT_OK;
 }
 

@@ -99,6 +99,61 @@ __global__ void fista3d_kernel(const float *x_in, float *w, const float *__restr
     }
 }
 
+// The same steps over the stacks of a batch plan (block row blockIdx.y = stack): ISTA3D of the
+// stack's images into xn, FISTA3D with x = w = the stack's w (FISTA_OSEM_execution's binding),
+// v = the images, and the copies around them.
+__global__ void ista3d_stacks_kernel(const XctStackDev *__restrict__ stacks, float lambda)
+{
+    const XctStackDev &S = stacks[blockIdx.y];
+    const long long total = (long long)S.nx * S.ny * S.dN;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int X = (int)(i % S.nx);
+        const long long r = i / S.nx;
+        const int Y = (int)(r % S.ny), Z = (int)(r / S.ny);
+        float x = cs_select(S.img, S.nx, S.ny, S.dN, X, Y, Z, lambda);
+        x = fmaxf(1.0e-6f, x);
+        S.xn[i] = (x != x) ? 1.0e-6f : x;
+    }
+}
+
+__global__ void fista3d_stacks_kernel(const XctStackDev *__restrict__ stacks, float lambda)
+{
+    const XctStackDev &S = stacks[blockIdx.y];
+    const long long total = (long long)S.nx * S.ny * S.dN;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int X = (int)(i % S.nx);
+        const long long r = i / S.nx;
+        const int Y = (int)(r % S.ny), Z = (int)(r / S.ny);
+        const float xi = S.w[i], b = S.beta[i];
+        const float x = cs_select(S.img, S.nx, S.ny, S.dN, X, Y, Z, lambda);
+        S.xn[i] = x;
+        float bn = b * b * 4.0f + 1.0f;
+        bn = (sqrtf(bn) + 1.0f) * 0.5f;
+        const float g = __fdiv_rn(b - 1.0f, bn);
+        S.beta[i] = bn;
+        const float wn = g * x + (1.0f - g) * xi;
+        S.w[i] = (wn != wn) ? 1.0e-6f : wn;
+    }
+}
+
+// what: 0 img <- xn; 1 w <- img and beta <- 0
+__global__ void stack_copy_kernel(const XctStackDev *__restrict__ stacks, int what)
+{
+    const XctStackDev &S = stacks[blockIdx.y];
+    const long long total = (long long)S.nx * S.ny * S.dN;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        if (what == 0) {
+            S.img[i] = S.xn[i];
+        } else {
+            S.w[i] = S.img[i];
+            S.beta[i] = 0.0f;
+        }
+    }
+}
+
 int cs_grid(long long n, int sm_count)
 {
     return (int)std::max(1LL, std::min((n + 255) / 256, (long long)sm_count * 16));
@@ -123,5 +178,51 @@ int launch_fista3d(const float *x_in, float *w, const float *v, float *beta, flo
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return xct_cuda_fail(e, "fista3d_kernel launch");
     g_xct_launches.fetch_add(1);
+    return XCT_OK;
+}
+
+// The stack launchers run only inside a batch plan's graph capture; xct_batch_run counts the
+// launches of each replay.
+static int stacks_grid(int nstacks, long long max_vox, int sm_count, dim3 &grid)
+{
+    if (nstacks <= 0 || nstacks > 65535) return xct_fail(XCT_E_INVALID, "stack count out of range");
+    const long long per = std::max(1LL, (long long)sm_count * 16 / nstacks);
+    grid = dim3((unsigned)std::max(1LL, std::min((max_vox + 255) / 256, per)), (unsigned)nstacks);
+    return XCT_OK;
+}
+
+int launch_ista3d_stacks(const XctStackDev *stacks, int nstacks, long long max_vox, float lambda, int sm_count,
+                         cudaStream_t st)
+{
+    dim3 grid;
+    int rc = stacks_grid(nstacks, max_vox, sm_count, grid);
+    if (rc) return rc;
+    ista3d_stacks_kernel<<<grid, 256, 0, st>>>(stacks, lambda);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return xct_cuda_fail(e, "ista3d_stacks_kernel launch");
+    return XCT_OK;
+}
+
+int launch_fista3d_stacks(const XctStackDev *stacks, int nstacks, long long max_vox, float lambda, int sm_count,
+                          cudaStream_t st)
+{
+    dim3 grid;
+    int rc = stacks_grid(nstacks, max_vox, sm_count, grid);
+    if (rc) return rc;
+    fista3d_stacks_kernel<<<grid, 256, 0, st>>>(stacks, lambda);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return xct_cuda_fail(e, "fista3d_stacks_kernel launch");
+    return XCT_OK;
+}
+
+int launch_stack_copy(const XctStackDev *stacks, int nstacks, long long max_vox, int what, int sm_count,
+                      cudaStream_t st)
+{
+    dim3 grid;
+    int rc = stacks_grid(nstacks, max_vox, sm_count, grid);
+    if (rc) return rc;
+    stack_copy_kernel<<<grid, 256, 0, st>>>(stacks, what);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return xct_cuda_fail(e, "stack_copy_kernel launch");
     return XCT_OK;
 }

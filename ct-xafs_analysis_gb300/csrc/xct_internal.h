@@ -29,13 +29,26 @@ struct KGeom {
 // One slice of a batched launch (device-side descriptor).
 struct XctItemDev {
     KGeom g;
-    const float *sino;   // measured sinogram [pa][px]
+    const float *sino;   // measured sinogram [pa][px] the OS-EM steps read (corrected if corr_mode)
     float *img;          // image [ny][nx], updated in place
     float *ratio;        // ratio image [pa][px] (rows never written stay 0)
     double *acc;         // ray-sum accumulator [ceil(pa/ss)][px] (kept zeroed between subsets)
     const float2 *trig;  // (cos, sin) [pa]
     int cover;           // XCT_SUBSETS_COVER
     int fwd_ntx, fwd_nty, bp_ntx;
+    int corr_mode;            // sinogramCorrection mode 1..4, 0 none
+    const float *sino_in;     // the caller's measured sinogram (the correction's input)
+    float *corr;              // corrected sinogram [pa][px] (corr_mode > 0; then sino == corr)
+    const float *corr_ang;    // [pa] x 2 per-angle correction factors
+    const float *corr_bin;    // [px] per-bin correction factors
+};
+
+// A stack of consecutive slices of one shape in a batch plan with compressed sensing: its
+// images form one [dN][ny][nx] array (the proximal step's third axis), with its own w, beta
+// and x' buffers of the same size.
+struct XctStackDev {
+    float *img, *w, *beta, *xn;
+    int nx, ny, dN;
 };
 
 struct xct_ctx {
@@ -199,6 +212,21 @@ int launch_fill(float *p, long long n, float v, int sm_count, cudaStream_t st);
 int launch_focus_index(const float *imgs, int nx, int ny, int n, const float *d_prm, double *red, float *findex,
                        cudaStream_t st);
 // sinogramCorrection (reconstShare.cl:35-70), modes 1..4, src -> dst.
+// The ISTA3D/FISTA3D kernels' lambda for CSlambda (L fixed at 0.5, the compressed-sensing OS-EM).
+float xct_cs_kernel_lambda(float cs_lambda);
+// sinogramCorrection factor tables of one geometry (angle factors [2*pa], bin factors [px]).
+void xct_corr_tables(const float *ang_deg, int pa, int px, std::vector<float> &af, std::vector<float> &bf);
+// sinogramCorrection of every item of a batch with corr_mode > 0 (sino_in -> corr); the grid
+// covers the largest (px, pa) of the batch.
+int launch_sino_correction_batched(const XctItemDev *items, int n, int max_px, int max_pa, cudaStream_t st);
+// Batched compressed-sensing steps over stacks (xct_cs.cu): ISTA3D (img -> xn), FISTA3D(x = img,
+// w, v = img, beta -> w, beta, xn), copies img <- xn and w <- img, beta <- 0.
+int launch_ista3d_stacks(const XctStackDev *stacks, int nstacks, long long max_vox, float lambda, int sm_count,
+                         cudaStream_t st);
+int launch_fista3d_stacks(const XctStackDev *stacks, int nstacks, long long max_vox, float lambda, int sm_count,
+                          cudaStream_t st);
+int launch_stack_copy(const XctStackDev *stacks, int nstacks, long long max_vox, int what, int sm_count,
+                      cudaStream_t st);
 int launch_sino_correction(const KGeom &g, const float *src, float *dst, const float *ang_fac, const float *bin_fac,
                            int mode, int dN, cudaStream_t st);
 

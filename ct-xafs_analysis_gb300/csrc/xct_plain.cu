@@ -98,6 +98,20 @@ __global__ void __launch_bounds__(256) bp_ref_plain_kernel(float *__restrict__ i
 // sinogramCorrection (reconstShare.cl:35-70), modes 1..4.  The transcendental factors
 // are tabulated on the host (ang_fac[2*th] = cos(angle_pr), ang_fac[2*th+1] = sinfactor,
 // bin_fac[X] = cos(asin(theta))), so the kernel is pure multiplies/compares.
+__device__ __forceinline__ float sino_corrected(float v, int X, int th, int px, const float *__restrict__ ang_fac,
+                                                const float *__restrict__ bin_fac, int mode)
+{
+    const float ca = ang_fac[2 * th], sf = ang_fac[2 * th + 1];
+    const float theta = 2.0f * fabsf((float)X - (float)px / 2.0f) / (float)px;
+    switch (mode) {
+    case 4: return (theta * theta < sf * sf) ? v : 0.0f;
+    case 3: return v * (bin_fac[X] * ca);
+    case 2: return v * ca;
+    case 1: return v * bin_fac[X];
+    default: return v;
+    }
+}
+
 __global__ void sino_correction_kernel(const float *__restrict__ src, float *__restrict__ dst,
                                        const float *__restrict__ ang_fac, const float *__restrict__ bin_fac, KGeom g,
                                        int mode)
@@ -107,17 +121,18 @@ __global__ void sino_correction_kernel(const float *__restrict__ src, float *__r
     const int z = blockIdx.z;
     if (X >= g.px) return;
     const size_t o = ((size_t)z * g.pa + th) * g.px + X;
-    float v = src[o];
-    const float ca = ang_fac[2 * th], sf = ang_fac[2 * th + 1];
-    const float theta = 2.0f * fabsf((float)X - (float)g.px / 2.0f) / (float)g.px;
-    switch (mode) {
-    case 4: v = (theta * theta < sf * sf) ? v : 0.0f; break;
-    case 3: v *= bin_fac[X] * ca; break;
-    case 2: v *= ca; break;
-    case 1: v *= bin_fac[X]; break;
-    default: break;
-    }
-    dst[o] = v;
+    dst[o] = sino_corrected(src[o], X, th, g.px, ang_fac, bin_fac, mode);
+}
+
+// The same for every item of a batch with a correction: block (x, th, item).
+__global__ void sino_correction_batched_kernel(const XctItemDev *__restrict__ items)
+{
+    const XctItemDev &it = items[blockIdx.z];
+    const int X = blockIdx.x * blockDim.x + threadIdx.x;
+    const int th = blockIdx.y;
+    if (it.corr_mode <= 0 || X >= it.g.px || th >= it.g.pa) return;
+    const size_t o = (size_t)th * it.g.px + X;
+    it.corr[o] = sino_corrected(it.sino_in[o], X, th, it.g.px, it.corr_ang, it.corr_bin, it.corr_mode);
 }
 
 }  // namespace
@@ -162,6 +177,15 @@ int launch_sino_correction(const KGeom &g, const float *src, float *dst, const f
     dim3 grid((g.px + 127) / 128, g.pa, dN);
     sino_correction_kernel<<<grid, 128, 0, st>>>(src, dst, ang_fac, bin_fac, g, mode);
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+    XCT_CUDA_TRY(cudaGetLastError());
+    return XCT_OK;
+}
+
+int launch_sino_correction_batched(const XctItemDev *items, int n, int max_px, int max_pa, cudaStream_t st)
+{
+    if (n <= 0) return XCT_OK;
+    dim3 grid((max_px + 127) / 128, max_pa, n);
+    sino_correction_batched_kernel<<<grid, 128, 0, st>>>(items);  // captured: counted per replay
     XCT_CUDA_TRY(cudaGetLastError());
     return XCT_OK;
 }

@@ -55,7 +55,7 @@ EXPORTS = (
     "xct_check_report", "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_reslice_plan_set_wait_limit",
     "xct_denoise_sinogram",
     "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
-    "xct_plan_multislice", "xct_plan_set_multislice",
+    "xct_plan_multislice", "xct_plan_set_multislice", "xct_batch_plan_set_cs",
     "xct_fista_power_iteration", "xct_fista_set_lipschitz", "xct_fista_run_device", "xct_fista_run",
     "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume", "xct_hybrid_cs_run_device",
     "xct_hybrid_cs_run",
@@ -142,6 +142,7 @@ def load():
     L.xct_reslice_plan_set_wait_limit.argtypes = [vp, ctypes.c_longlong]
     L.xct_denoise_sinogram.argtypes = [ip, ip, ip, c_f, vp, vp, vp]
     L.xct_cs_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
+    L.xct_batch_plan_set_cs.argtypes = [vp, c_f, ip, ctypes.POINTER(ctypes.c_int)]
     L.xct_fista_power_iteration.argtypes = [vp, ip, ip, ip, fp, vp]
     L.xct_fista_set_lipschitz.argtypes = [vp, fp]
     L.xct_fista_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, c_f, ip, vp]
@@ -632,6 +633,14 @@ class BatchPlan:
         s = (ctypes.c_void_p * n)(*[_ptr(t) for t in sinos])
         i = (ctypes.c_void_p * n)(*[_ptr(t) for t in imgs])
         _check(self._lib.xct_batch_run(self.handle, s, i, _stream(stream)))
+
+    def set_cs(self, stack_len, cs_lambda=1.0e-4):
+        """Compressed-sensing OS-EM over stacks of consecutive slices of one image size
+        (stack_len: the stacks' lengths in slice order; empty turns it off).  Each stack's
+        images must then be consecutive in one array when the plan runs."""
+        lens = [int(v) for v in stack_len]
+        arr = (ctypes.c_int * max(1, len(lens)))(*lens)
+        _check(self._lib.xct_batch_plan_set_cs(self.handle, float(cs_lambda), len(lens), arr))
 
     def close(self):
         if self.handle:

@@ -122,14 +122,22 @@ int xct_osem_run_volume(xct_plan *plan, int n, const float *const *sino_host, fl
  * captured on the first xct_batch_run and replayed after.  d_sino[i] / d_img[i] are slice
  * i's device sinogram [pa_i][px_i] and image [ny_i][nx_i] (initial in, result out); they may
  * change from run to run.  Runs of one plan must not overlap (they share its buffers).
- * Sinogram correction is not available in batches.  xct_osem_run_batched = create, run,
- * synchronise the stream, destroy. */
+ * A slice whose geometry has a correction_mode is corrected once per run into a buffer of
+ * the plan before the loop, as OSEM_execution does with prjCorrection set (GPU.cpp:175-186;
+ * the CT-XAFS stack flow always sets it, Reslice_CTreconst_ocl.cpp:104-117, GPU.cpp:447-451).
+ * xct_osem_run_batched = create, run, synchronise the stream, destroy.
+ * xct_batch_plan_set_cs : compressed-sensing OS-EM (FISTA_OSEM_execution, GPU.cpp:243-405)
+ *     over stacks: stack_len[s] consecutive slices of one image size form stack s (the lengths
+ *     add up to n; nstacks = 0 turns it off), the third axis of the proximal step; every run
+ *     then needs each stack's images consecutive in one [dN][ny][nx] array (d_img[i+1] =
+ *     d_img[i] + ny*nx within a stack).  Semantics as xct_cs_osem_run_device. */
 typedef struct xct_batch_plan xct_batch_plan;
 int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms, int it, xct_batch_plan **out);
 int xct_batch_run(xct_batch_plan *plan, const float *const *d_sino, float *const *d_img, void *stream);
 int xct_batch_plan_destroy(xct_batch_plan *plan);
 int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, const float *const *d_sino,
                          float *const *d_img, int it, void *stream);
+int xct_batch_plan_set_cs(xct_batch_plan *plan, float cs_lambda, int nstacks, const int *stack_len);
 
 /* ---- OS-EM without any allocation ----------------------------------------------------
  * No counterpart in the reference: the reference allocates its image objects on every call.

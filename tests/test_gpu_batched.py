@@ -102,3 +102,89 @@ def test_volume_stream_matches_batches(gpu_ctx, oracle_lib):
     for z in range(nz):
         assert np.linalg.norm(out[z] - hi[z].numpy()) / np.linalg.norm(hi[z].numpy()) <= 1e-6
     plan.close()
+
+
+def test_batched_sinogram_correction_modes(gpu_ctx, oracle_lib):
+    """Per-slice sinogram correction in a batch (modes 0-4 on slices of different shapes):
+    each slice is corrected once per run, as OSEM_execution does with prjCorrection set
+    (GPU.cpp:175-186), then reconstructed; against the oracle on the corrected sinogram and
+    against the single-plan path with the same mode."""
+    import xct
+    from xct import phantom as P
+    O = oracle_lib
+    ss, it = 5, 2
+    spec = [(64, 64, 90, 0), (72, 80, 60, 1), (48, 56, 45, 2), (80, 64, 70, 3), (56, 60, 50, 4)]
+    geoms, sinos, want, singles, host = [], [], [], [], []
+    for k, (n, px, pa, mode) in enumerate(spec):
+        ang = P.uniform_angles(pa)
+        img = P.rasterize_ellipses(P.ellipse_params(n, 5, 40 + k, axes=(2, n / 4)), n, n)
+        meas = P.noisy_log_sinogram(O.projection(img, ang, px), 1e5, k).astype(np.float32)
+        geoms.append(xct.make_geom(n, n, px, ang, ss, it, correction_mode=mode))
+        host.append(meas)
+        sinos.append(torch.from_numpy(meas).cuda().contiguous())
+        used = O.sino_correction(meas, ang, mode) if mode else meas
+        want.append(O.osem_run(np.ones((n, n), np.float32), used, ang, ss, it, order=O.ORDER_LITERAL))
+        plan = xct.OSEMPlan(gpu_ctx, n, n, px, ang, ss, it, correction_mode=mode)
+        x = torch.ones((1, n, n), device="cuda")
+        plan.run_device(sinos[-1].reshape(1, pa, px), x)
+        torch.cuda.synchronize()
+        singles.append(x[0].cpu().numpy().astype(np.float64))
+        plan.close()
+    bp = xct.BatchPlan(gpu_ctx, geoms, it)
+    for replay in range(2):
+        imgs = [torch.ones((n, n), device="cuda") for n, _, _, _ in spec]
+        bp.run(sinos, imgs)
+        torch.cuda.synchronize()
+        for k, (x, ref, single) in enumerate(zip(imgs, want, singles)):
+            got = x.cpu().numpy().astype(np.float64)
+            assert np.linalg.norm(got - single) / np.linalg.norm(single) <= 1e-6, (replay, k)
+            assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-4, (replay, k)
+            assert np.abs(got - ref).max() <= 1e-3 * np.abs(ref).max(), (replay, k)
+    # the caller's sinograms are not modified (the corrected copies live in the plan)
+    for k in range(len(spec)):
+        assert np.array_equal(sinos[k].cpu().numpy(), host[k])
+    bp.close()
+
+
+def test_batched_compressed_sensing_stacks(gpu_ctx, oracle_lib):
+    """Compressed-sensing OS-EM in a batch plan over three stacks of different image sizes
+    (3 x 64^2, 2 x 48^2, 1 x 40^2; each stack's images one array), against the oracle's
+    FISTA_OSEM_execution of each stack and against the single-plan call."""
+    import xct
+    from xct import phantom as P
+    O = oracle_lib
+    ss, it, lam = 5, 2, 1.0e-4
+    stacks = [(64, 64, 90, 3), (48, 50, 60, 2), (40, 40, 45, 1)]
+    geoms, sinos, want, singles, arrays = [], [], [], [], []
+    for s_i, (n, px, pa, dN) in enumerate(stacks):
+        ang = P.uniform_angles(pa)
+        prm = P.ellipsoid_params(n, dN, count=5, seed=50 + s_i)
+        meas = np.stack([P.noisy_log_sinogram(O.projection(P.ellipsoid_slice(prm, z, n, n), ang, px), 1e4, z)
+                         for z in range(dN)]).astype(np.float32)
+        for z in range(dN):
+            geoms.append(xct.make_geom(n, n, px, ang, ss, it))
+            sinos.append(torch.from_numpy(meas[z]).cuda().contiguous())
+        want.append(O.cs_osem_run(np.ones((dN, n, n), np.float32), meas, ang, ss, it, lam))
+        plan = xct.OSEMPlan(gpu_ctx, n, n, px, ang, ss, it, max_batch=dN)
+        x = torch.ones((dN, n, n), device="cuda")
+        plan.cs_run_device(torch.from_numpy(meas).cuda(), x, cs_lambda=lam)
+        torch.cuda.synchronize()
+        singles.append(x.cpu().numpy().astype(np.float64))
+        plan.close()
+    bp = xct.BatchPlan(gpu_ctx, geoms, it)
+    bp.set_cs([d for _, _, _, d in stacks], cs_lambda=lam)
+    for replay in range(2):
+        arrays = [torch.ones((dN, n, n), device="cuda") for n, _, _, dN in stacks]
+        imgs = [a[z] for a in arrays for z in range(a.shape[0])]
+        bp.run(sinos, imgs)
+        torch.cuda.synchronize()
+        for s_i, a in enumerate(arrays):
+            got = a.cpu().numpy().astype(np.float64)
+            assert np.linalg.norm(got - singles[s_i]) / np.linalg.norm(singles[s_i]) <= 1e-6, (replay, s_i)
+            ref = want[s_i]
+            assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-4, (replay, s_i)
+    # a stack whose images are not one array is refused
+    loose = [torch.ones((n, n), device="cuda") for n, _, _, dN in stacks for _ in range(dN)]
+    with pytest.raises(xct.XCTError):
+        bp.run(sinos, loose)
+    bp.close()
