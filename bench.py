@@ -20,8 +20,14 @@ Metric: slice-iterations per second (one slice through all 15 subsets once).
                     reconstruction), and beside it one blocking xct_osem_run per step;
   per_slice      -- the plain one-slice-per-call path (plain kernels, dN = 1) and the tiled
                     kernels at dN = 1, each on a bounded sample of slices;
-  ctxafs_batched -- the CT-XAFS stack sample (uneven slices) in one autotuned batched graph
-                    against one call per slice;
+  ctxafs_batched -- the CT-XAFS stack at scale: 64 energies x 8 slices = 512 uneven items
+                    (widths 512-2048, 360-1200 angles with drops) in one autotuned batch
+                    plan, against one call per item (plain and tiled kernels) on a sample
+                    scaled by work;
+  uniform_batch  -- 16 slices of the per-slice workload through one batch plan: its uniform
+                    route (single-shape plan) against its graph of persistent launches;
+  parity         -- slice 0 of the timed region against the oracle's full 15 x 4 OS-EM of
+                    the same sinogram (rel-L2 and max-abs of peak; the bar 1e-4 / 1e-3);
   small_256      -- the 256^2 workload (180 angles, 10 subsets x 5 it): the GPU at one and at
                     10 slices per call, beside the CPU oracle's full run of one slice;
   next_components-- throughput of FBP, the hybrid, the compressed-sensing OS-EM, reslice,
@@ -31,11 +37,12 @@ Metric: slice-iterations per second (one slice through all 15 subsets once).
                     it, rotation centre +3.5 bins, I0 = 2e4) streamed from page-locked host
                     memory by xct_osem_run_volume, against blocking per-batch calls and the
                     plain per-slice path;
-  roofline       -- the dominant kernel (tiled forward projector) timed live with CUDA
-                    events inside this run; its algorithmic FLOPs (12 per bilinear sample
-                    whose footprint meets the image) over its measured time, against the
-                    FP32 FMA peak measured by xct_fp32_peak in the same run;
-  cpu_baseline   -- the CPU oracle (OpenMP, all host cores) on a bounded sample.
+  roofline       -- the dominant kernel (the slice-interleaved forward projector, 8 slices
+                    per launch) timed live with CUDA events inside this run; its algorithmic
+                    FLOPs (12 per bilinear sample whose footprint meets the image) over its
+                    measured time, against the FP32 FMA peak measured by xct_fp32_peak in the
+                    same run;
+  cpu_baseline   -- the CPU oracle (OpenMP, all host cores) on one whole slice (15 x 4).
 
 --impl reference times the reference algorithm on the host cores (the CPU restatement of
 the reference's OpenCL kernels; the OpenCL runtime the reference needs is not available
@@ -243,25 +250,19 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_sample(nsub=3):
-    """Oracle (OpenMP, all cores) on `nsub` subsets of one slice; slice-iters/s."""
+def cpu_baseline_slice(meas, ang):
+    """The oracle (OpenMP, all host cores) on one whole unit of the workload: the full OS-EM
+    of one 2048^2 slice, 15 subsets x 4 iterations, in the reference's literal evaluation
+    order.  Returns the baseline figure (slice-iters/s) and the reconstructed slice."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
-    from xct import phantom
     oracle.build()
-    ang = phantom.uniform_angles(PA)
-    pars = phantom.ellipsoid_params(NX, NSLICES, 30, 2, mu=(0.005, 0.1))
-    img = phantom.ellipsoid_slice(pars, NSLICES // 2, NX, NY)
-    sub = oracle.subset_order(SS)
-    meas = oracle.projection(img, ang, PX, ss=SS, sub=int(sub[0]))
-    x = np.ones((NY, NX), np.float32)
     t0 = time.perf_counter()
-    for i in range(nsub):
-        r = oracle.osem1(x, meas, ang, SS, int(sub[i]), order=oracle.ORDER_LITERAL)
-        x = oracle.osem2(x, r, ang, SS, int(sub[i]), order=oracle.ORDER_LITERAL)
+    ref = oracle.osem_run(np.ones((NY, NX), np.float32), meas, ang, SS, IT, order=oracle.ORDER_LITERAL)
     dt = time.perf_counter() - t0
-    return {"value": nsub / SS / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d subsets (OSEM1+OSEM2) of one 2048^2 slice, 1500 angles, OpenMP" % nsub}
+    return ({"value": IT / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "s": dt,
+             "sample": "one 2048^2 slice of the timed volume, full OS-EM (15 subsets x 4 it, 1500 angles), OpenMP"},
+            np.asarray(ref, np.float64))
 
 
 def next_cpu_baselines():
@@ -348,35 +349,66 @@ def small_case_256(ctx, reps=5):
     return out
 
 
-def ctxafs_batched(ctx, n_items=32, ss=10, it=5):
-    """CT-XAFS stack sample: n_items slices of one energy point, shapes as the batched
-    workload (widths 512-2048 with matching bins, 360-1200 angles with 0-10 % dropped), each a
-    two-spectrum XANES mixture; 10 subsets x 5 iterations.  Slice-iters/s of one batched
-    graph (all slices at once) against one call per slice with the plain and the tiled
-    kernels.  Device-resident inputs, CUDA-event timing."""
+def ctxafs_stack_specs(n_energy, n_slices, seed=3, widths=(512, 1024, 1536, 2048), angles=(360, 720, 900, 1200),
+                       max_drop=0.10):
+    """Shapes of a CT-XAFS stack of n_energy x n_slices uneven items: slice s has width w_s
+    (bins = w_s; every width in `widths` equally often, seeded order), energy e has its own
+    projection count from `angles` over 180 deg with 0..max_drop of them dropped at random
+    (one angle list for all slices of that energy, as reslicing one projection set gives).
+    Returns the widths [n_slices] and the angle arrays [n_energy]."""
+    rng = np.random.default_rng(seed)
+    ws = np.resize(np.asarray(widths), n_slices)
+    rng.shuffle(ws)
+    angs = []
+    for _ in range(n_energy):
+        pa = int(rng.choice(angles))
+        drop = int(rng.integers(0, int(max_drop * pa) + 1))
+        keep = np.sort(rng.choice(pa, pa - drop, replace=False))
+        angs.append((keep * (180.0 / pa)).astype(np.float32))
+    return [int(w) for w in ws], angs
+
+
+def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
+    """The CT-XAFS stack at scale: n_energy x n_slices uneven items (widths 512-2048 with
+    matching bins, 360-1200 angles with 0-10 % dropped per energy), each slice a two-spectrum
+    XANES mixture at its energy, Poisson I0 = 1e5; 10 subsets x 5 iterations.  One autotuned
+    batch plan (graph of persistent launches over a device work queue) reconstructs all
+    items; the per-slice paths (one call per item, plain and tiled kernels) run on a seeded
+    sample of `sample` items and are scaled by the work they did (sum of rays x angles)
+    to the whole stack.  Device-resident inputs, CUDA-event timing."""
     import torch
     import xct
     from xct import phantom
-    spectra = phantom.xanes_mixture(64, seed=3)
-    specs = phantom.ctxafs_item_specs(n_items, seed=3)
-    sinos, geoms, shapes = [], [], []
+    widths, angs = ctxafs_stack_specs(n_energy, n_slices)
+    e_axis, s1, s2 = phantom.xanes_mixture(n_energy, seed=3)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(3)
-    for k, (w, ang) in enumerate(specs):
-        g = xct.make_geom(w, w, w, ang, ss, it)
-        p = xct.OSEMPlan(ctx, w, w, w, ang, ss, it)
-        img = phantom.xanes_slice(w, 40, 100 + k, spectra, torch_device="cuda").reshape(1, w, w).contiguous()
-        clean = torch.empty((1, len(ang), w), device="cuda")
-        p.fwd(img, clean)
-        sinos.append(phantom.noisy_log_sinogram_torch(clean[0], 1e5, generator=gen).contiguous())
-        p.close()
-        geoms.append(g)
-        shapes.append((w, len(ang)))
+    t_gen = time.perf_counter()
+    fields = []
+    for s_i, w in enumerate(widths):
+        sup, f = phantom.xanes_fields(w, 100 + s_i)
+        fields.append((torch.from_numpy(sup).cuda(), torch.from_numpy(f).cuda()))
+    sinos, geoms, shapes = [], [], []
+    for e in range(n_energy):
+        ang = angs[e]
+        for s_i, w in enumerate(widths):
+            sup, f = fields[s_i]
+            img = (sup * (f * float(s1[e]) + (1.0 - f) * float(s2[e])) * 0.02).float().reshape(1, w, w).contiguous()
+            p = xct.OSEMPlan(ctx, w, w, w, ang, ss, it)
+            clean = torch.empty((1, len(ang), w), device="cuda")
+            p.fwd(img, clean)
+            p.close()
+            sinos.append(phantom.noisy_log_sinogram_torch(clean[0], 1e5, generator=gen).contiguous())
+            geoms.append(xct.make_geom(w, w, w, ang, ss, it))
+            shapes.append((w, len(ang)))
     torch.cuda.synchronize()
+    n_items = len(sinos)
+    work = np.array([w * w * pa for w, pa in shapes], np.float64)  # taps ~ pixels x angles
     stream = torch.cuda.current_stream()
-    res = {"items": n_items, "subsets": ss, "iterations": it,
-           "widths": sorted(set(s[0] for s in shapes)), "angles_min": min(s[1] for s in shapes),
-           "angles_max": max(s[1] for s in shapes)}
+    res = {"items": n_items, "energies": n_energy, "slices": n_slices, "subsets": ss, "iterations": it,
+           "widths": sorted(set(widths)), "angles_min": min(s[1] for s in shapes),
+           "angles_max": max(s[1] for s in shapes), "generate_s": time.perf_counter() - t_gen,
+           "device_bytes": int(sum(w * w + w * pa for w, pa in shapes) * 4)}
 
     def timed(fn, reps=1):
         fn()  # warm (captures the graph / builds plans)
@@ -390,10 +422,13 @@ def ctxafs_batched(ctx, n_items=32, ss=10, it=5):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
+    t_plan = time.perf_counter()
     bp = xct.BatchPlan(ctx, geoms, it)
+    res["plan_s"] = time.perf_counter() - t_plan
     t_tune = time.perf_counter()
     res["tuning"] = dict(zip(("fwd_tile", "ang_chunk"), bp.autotune()))
     res["autotune_s"] = time.perf_counter() - t_tune
+    res["route"] = "uniform" if bp.uniform() else "graph"
     imgs = [torch.ones((w, w), device="cuda") for w, _ in shapes]
 
     def run_batched():
@@ -401,28 +436,82 @@ def ctxafs_batched(ctx, n_items=32, ss=10, it=5):
             x.fill_(1.0)
         bp.run(sinos, imgs, stream=stream)
 
-    ms = timed(run_batched, reps=3)
-    res["batched"] = {"value": n_items * it / (ms * 1e-3), "ms": ms}
+    l0 = xct.launch_count()
+    ms = timed(run_batched, reps=1)
+    res["batched"] = {"value": n_items * it / (ms * 1e-3), "items_per_s": n_items / (ms * 1e-3), "ms": ms,
+                      "launches_per_run": (xct.launch_count() - l0) // 2}
+    rng = np.random.default_rng(7)
+    samp = np.sort(rng.choice(n_items, min(sample, n_items), replace=False))
+    frac = work[samp].sum() / work.sum()
+    res["sample_items"] = int(len(samp))
+    res["sample_work_fraction"] = float(frac)
     for name, kern in (("per_slice_tiled", xct.KERNELS_TILED), ("per_slice_plain", xct.KERNELS_PLAIN)):
-        plans = [xct.OSEMPlan(ctx, w, w, w, g._angles, ss, it, kernels=kern) for (w, _), g in zip(shapes, geoms)]
+        plans = [xct.OSEMPlan(ctx, shapes[k][0], shapes[k][0], shapes[k][0], geoms[k]._angles, ss, it, kernels=kern)
+                 for k in samp]
         if kern == xct.KERNELS_TILED:
             for p in plans:
                 p.autotune(dN=1)
-        ximgs = [torch.ones((1, w, w), device="cuda") for w, _ in shapes]
+        ximgs = [torch.ones((1, shapes[k][0], shapes[k][0]), device="cuda") for k in samp]
 
         def run_single():
-            for p, s, x in zip(plans, sinos, ximgs):
+            for p, k, x in zip(plans, samp, ximgs):
                 x.fill_(1.0)
-                p.run_device(s.reshape(1, *s.shape), x, stream=stream)
+                p.run_device(sinos[k].reshape(1, *sinos[k].shape), x, stream=stream)
 
-        ms = timed(run_single)
-        res[name] = {"value": n_items * it / (ms * 1e-3), "ms": ms}
+        ms_s = timed(run_single)
+        ms_all = ms_s / frac  # the whole stack at the sample's rate per unit of work
+        res[name] = {"value": n_items * it / (ms_all * 1e-3), "items_per_s": n_items / (ms_all * 1e-3),
+                     "sample_ms": ms_s}
         for p in plans:
             p.close()
+        if name == "per_slice_tiled":
+            got = np.concatenate([imgs[k].cpu().numpy().ravel() for k in samp]).astype(np.float64)
+            ref = np.concatenate([x.cpu().numpy().ravel() for x in ximgs]).astype(np.float64)
+            res["rel_l2_batched_vs_per_slice"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
     bp.close()
     res["batched_over_plain"] = res["batched"]["value"] / res["per_slice_plain"]["value"]
     res["batched_over_tiled_per_slice"] = res["batched"]["value"] / res["per_slice_tiled"]["value"]
     return res
+
+
+def uniform_batch(ctx, sino, n=16, reps=2):
+    """A uniform batch (n slices of the per-slice workload's geometry, 2048^2, 1500 angles,
+    15 x 4) through one batch plan: with the sinograms and images each one array the plan
+    takes its uniform route (a single-shape plan, slice-interleaved forward projector); with
+    images in separate allocations the same plan replays its graph of persistent launches.
+    Slice-iters/s of both, CUDA-event timing, device-resident inputs."""
+    import torch
+    import xct
+    from xct import phantom
+    ang = phantom.uniform_angles(PA)
+    geoms = [xct.make_geom(NX, NY, PX, ang, SS, IT) for _ in range(n)]
+    bp = xct.BatchPlan(ctx, geoms, IT)
+    bp.autotune()
+    stream = torch.cuda.current_stream()
+    arr = torch.ones((n, NY, NX), device="cuda")
+    sep = [torch.ones((NY, NX), device="cuda") for _ in range(n)]
+    sl = [sino[z] for z in range(n)]
+    out = {"slices": n, "slices_per_call": bp.uniform()}
+    for name, imgs in (("uniform_route", [arr[z] for z in range(n)]), ("graph", sep)):
+        def run():
+            for x in imgs:
+                x.fill_(1.0)
+            bp.run(sl, imgs, stream=stream)
+        run()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            run()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out[name] = n * IT * reps / (a.elapsed_time(b) * 1e-3)
+    d = (arr - torch.stack(sep)).double()
+    out["rel_l2_route_vs_graph"] = float(d.norm() / torch.stack(sep).double().norm())
+    out["unit"] = UNIT
+    bp.close()
+    return out
 
 
 def volume_stream(ctx, nslices=40, dn=10):
@@ -756,7 +845,9 @@ def main():
     slice_iters = args.steps * DN * IT * world
     value = slice_iters / (ms * 1e-3)
 
-    # ---- parity spot check of the timed configuration (slice 0 vs a second run) ----
+    # slice 0 as the timed region left it (the first half of batch 0, on the caller's
+    # stream), checked against the oracle's full run of that slice below
+    timed_slice0 = imgs[0].cpu().numpy()
     finite = bool(torch.isfinite(imgs[:DN]).all())
 
     # ---- end to end through the C ABI with page-locked host buffers ----
@@ -817,6 +908,12 @@ def main():
     except Exception as e:  # reported, never fatal
         batched = {"error": str(e)[:300]}
 
+    # ---- a uniform batch through the batch plan: its uniform route against its graph ----
+    try:
+        uniform = uniform_batch(ctx, sino)
+    except Exception as e:  # reported, never fatal
+        uniform = {"error": str(e)[:300]}
+
     # ---- the 256^2 workload: GPU per call and batched, beside the CPU oracle ----
     try:
         small = small_case_256(ctx)
@@ -842,35 +939,39 @@ def main():
         nxt = {"error": str(e)[:300]}
 
     # ---- roofline of the dominant kernel (live CUDA events, same stream) ----
-    prof = plan.profile(sino[:DN], imgs[:DN].fill_(1.0), dN=DN, stream=stream)
+    # The timed batch of 10 runs as halves of 8 | 2 slices; the 8-slice half's forward
+    # projection is one launch of the slice-interleaved kernel per subset (fwd_ms_kernel),
+    # 82 % of the forward time of a step.  It is timed here on 8 slices: every launch of a
+    # 4 x 15 profile run bracketed by CUDA events on the launch stream.
+    G = xct.MULTISLICE_SLICES
+    prof = plan.profile(sino[:G], imgs[:G].fill_(1.0), dN=G, stream=stream)
     t_fwd, t_bp = algorithmic_counts(ang, NX, NY, PX)
-    fwd_flop_per_launch = 12.0 * t_fwd.sum() / SS * DN  # one subset's angles, dN slices
+    taps_per_launch = t_fwd.sum() / SS * G  # one subset's angles, G slices
+    fwd_flop_per_launch = 12.0 * taps_per_launch
     fwd_ms_avg = prof["fwd"]["ms"] / prof["fwd"]["launches"]
-    bp_flop_per_launch = 5.0 * t_bp.sum() / SS * DN + 4.0 * NX * NY * DN
+    bp_flop_per_launch = 5.0 * t_bp.sum() / SS * G + 4.0 * NX * NY * G
     bp_ms_avg = prof["bp"]["ms"] / prof["bp"]["launches"]
     fp32_peak = xct.fp32_peak_tflops(local)
     achieved = fwd_flop_per_launch / (fwd_ms_avg * 1e-3) / 1e12
     # HBM view of the same kernel: it reads each image once per subset and adds one double
     # per (ray, tile) -- compulsory bytes are tiny next to its arithmetic
-    fwd_bytes = DN * NX * NY * 4.0
-    # the kernel's own bound: the L1/shared-memory data path, 16 algorithmic bytes per bilinear
-    # tap (two 64-bit footprint loads) against 128 bytes per clock per SM
+    fwd_bytes = G * NX * NY * 4.0
+    # the kernel's own bound: the L1/shared-memory data path, one 16-byte record per tap and
+    # slice (the four bilinear coefficients of the footprint) against 128 B/clk/SM
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
     l1_peak = 128.0 * props.multi_processor_count * sm_mhz * 1e6
-    taps_per_launch = t_fwd.sum() / SS * DN
     roofline = {
-        "bound": "fp32", "kernel": "fwd_tiled_kernel (OSEM1 forward projection)",
+        "bound": "fp32", "kernel": "fwd_ms_kernel (OSEM1 forward projection, 8 slices per launch)",
         "l1_shared": {"achieved_tbs": taps_per_launch * 16.0 / (fwd_ms_avg * 1e-3) / 1e12,
                       "peak_tbs": l1_peak / 1e12,
                       "frac": taps_per_launch * 16.0 / (fwd_ms_avg * 1e-3) / l1_peak,
-                      "note": "16 B of footprint loads per tap over 128 B/clk/SM at the sampled SM clock; "
-                              "ncu: the shared-memory data wavefronts 88 % of active cycles "
-                              "(78.6 % elapsed) with 1.6x bank conflicts"},
+                      "note": "16 B (one float4 record) per tap and slice over 128 B/clk/SM at the sampled SM "
+                              "clock"},
         "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
         "peak_source": "measured live by xct_fp32_peak (FMA-chain kernel) in this run",
-        "flop_per_launch": fwd_flop_per_launch, "ms_per_launch": fwd_ms_avg,
-        "traffic": None,
+        "flop_per_launch": fwd_flop_per_launch, "taps_per_launch": taps_per_launch, "ms_per_launch": fwd_ms_avg,
+        "slices_per_launch": G, "traffic": None,
         "hbm": {"achieved_gbs": fwd_bytes / (fwd_ms_avg * 1e-3) / 1e9, "peak_gbs": None,
                 "note": "compulsory image bytes per launch over its time"},
         "bp": {"kernel": "bp_tiled_kernel (OSEM2 backprojection+update)", "ms_per_launch": bp_ms_avg,
@@ -882,22 +983,33 @@ def main():
             roofline["hbm"]["peak_gbs"] = json.load(f).get("hbm_gbs")
     except Exception:
         pass
-    # DRAM traffic of the forward kernel from the committed ncu capture of one slice, scaled
-    # to the DN slices of a bench launch (each slice's image is read once; 10 images exceed L2)
+    # DRAM traffic of the forward kernel per launch from the committed ncu capture of the same
+    # launch shape (8 slices of 2048^2, one subset of 100 angles)
+    prof_md = os.path.join(REPO, "profiles", "fwd_ms_kernel_2048x2048_1500ang_8slices.md")
     try:
-        with open(os.path.join(REPO, "profiles", "fwd_tiled_kernel_2048x2048_1500ang.md")) as f:
+        with open(prof_md) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_slice_launch:"):
-                    roofline["traffic"] = float(line.split(":")[1]) * DN
-                    roofline["traffic_source"] = ("ncu dram__bytes_read+write of one slice launch "
-                                                  "(profiles/fwd_tiled_kernel_2048x2048_1500ang.md) x %d slices" % DN)
+                if line.startswith("dram_bytes_per_launch:"):
+                    roofline["traffic"] = float(line.split(":")[1])
+                    roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                                                  "profiles/fwd_ms_kernel_2048x2048_1500ang_8slices.md")
     except Exception:
         pass
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu_baseline:
+        # the CPU baseline is the oracle's full OS-EM of slice 0 (15 subsets x 4 iterations, the
+        # reference's literal evaluation order); its result is the parity reference of the
+        # timed region's slice 0
         try:
-            cpu = cpu_baseline_sample()
+            cpu, ref0 = cpu_baseline_slice(sino[0].cpu().numpy(), ang)
+            d = timed_slice0.astype(np.float64) - ref0
+            parity = {"slice": 0, "rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref0)),
+                      "max_abs_of_peak": float(np.abs(d).max() / np.abs(ref0).max()),
+                      "bar": {"rel_l2": 1e-4, "max_abs_of_peak": 1e-3},
+                      "reference": "oracle OS-EM of the same sinogram, 15 x 4, reference order (OSEM.cl:38-105)"}
+            parity["pass"] = parity["rel_l2"] <= 1e-4 and parity["max_abs_of_peak"] <= 1e-3
         except Exception as e:  # reported, never fatal
             cpu = {"value": None, "error": str(e)[:200]}
         if isinstance(nxt, dict) and "error" not in nxt:
@@ -916,8 +1028,8 @@ def main():
                        "l2": "inputs larger than L2 (each step a new 290 MB batch)",
                        "parallelism": "dp%d over slices" % world},
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "per_slice": per_slice,
-            "ctxafs_batched": batched, "small_256": small, "volume_stream": volume, "next_components": nxt,
-            "roofline": roofline, "cpu_baseline": cpu, "finite": finite,
+            "ctxafs_batched": batched, "uniform_batch": uniform, "small_256": small, "volume_stream": volume, "next_components": nxt,
+            "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "finite": finite,
             "launches_per_step": launches / max(args.steps, 1),
             # library launches before the timed region: the skip count that makes an ncu launch
             # list (-s) start at the first timed step

@@ -51,6 +51,10 @@ struct xct_batch_plan {
     float *d_cs = nullptr;            // w, beta, x' of every stack
     long long max_vox = 0;
     float cs_lambda = 0.0f;           // the kernels' lambda
+    // uniform batches (every slice one geometry): a single-shape plan that runs them
+    // uni_batch at a time through the slice-interleaved forward projector
+    xct_plan *uni = nullptr;
+    int uni_batch = 0;
 };
 
 static void batch_free(xct_batch_plan *p)
@@ -68,6 +72,7 @@ static void batch_free(xct_batch_plan *p)
     cudaFree(p->d_corr_fac);
     cudaFree(p->d_stacks);
     cudaFree(p->d_cs);
+    if (p->uni) xct_osem_plan_destroy(p->uni);
     delete p;
 }
 
@@ -101,6 +106,21 @@ static int batch_layout(xct_batch_plan *p, int T, int chunk)
     }
     return XCT_OK;
 }
+
+// Two geometries describe the same reconstruction (sizes, centre, modes, angle list).
+static bool same_geom(const xct_geom &a, const xct_geom &b)
+{
+    const float ca = a.center_bin < 0.0f ? (float)a.px * 0.5f : a.center_bin;
+    const float cb = b.center_bin < 0.0f ? (float)b.px * 0.5f : b.center_bin;
+    return a.nx == b.nx && a.ny == b.ny && a.px == b.px && a.pa == b.pa && a.ss == b.ss && ca == cb &&
+           a.measured_fetch_mode == b.measured_fetch_mode && a.subset_mode == b.subset_mode &&
+           a.correction_mode == b.correction_mode &&
+           std::equal(a.angles_deg, a.angles_deg + a.pa, b.angles_deg);
+}
+
+// Slices per call of the uniform route: two halves of whole slice groups of the
+// slice-interleaved forward projector when the batch has them.
+static int uniform_batch(int n) { return std::min(n, 2 * fwd_ms_slices()); }
 
 extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms, int it, xct_batch_plan **out)
 {
@@ -240,6 +260,20 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         return rc;
     }
     if ((e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+    bool uniform = n >= 2;
+    for (int i = 1; i < n && uniform; ++i) uniform = same_geom(geoms[0], geoms[i]);
+    if (uniform) {
+        xct_geom g = geoms[0];
+        g.it = it;
+        g.max_batch = uniform_batch(n);
+        g.kernels = XCT_KERNELS_TILED;
+        rc = xct_osem_plan_create(ctx, &g, &p->uni);
+        if (rc) {
+            batch_free(p);
+            return rc;
+        }
+        p->uni_batch = g.max_batch;
+    }
     *out = p;
     return XCT_OK;
 }
@@ -298,6 +332,22 @@ extern "C" int xct_batch_run(xct_batch_plan *p, const float *const *d_sino, floa
     for (int i = 0; i < p->n; ++i)
         if (!d_sino[i] || !d_img[i]) return xct_fail(XCT_E_INVALID, "xct_batch_run: null slice pointer");
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
+    // uniform batch in one [n][pa][px] / [n][ny][nx] pair of arrays, no stacks: the
+    // single-shape plan, uni_batch slices per call
+    if (p->uni && p->stacks.empty()) {
+        const size_t nprj = (size_t)p->host[0].g.pa * p->host[0].g.px, nimg = (size_t)p->host[0].g.nx * p->host[0].g.ny;
+        bool contiguous = true;
+        for (int i = 1; i < p->n && contiguous; ++i)
+            contiguous = d_sino[i] == d_sino[0] + i * nprj && d_img[i] == d_img[0] + i * nimg;
+        if (contiguous) {
+            for (int off = 0; off < p->n; off += p->uni_batch) {
+                const int cnt = std::min(p->uni_batch, p->n - off);
+                int rc = xct_osem_run_device(p->uni, cnt, d_sino[off], d_img[off], nullptr, p->it, stream);
+                if (rc) return rc;
+            }
+            return XCT_OK;
+        }
+    }
     if (!p->exec) {
         int rc = capture(p);
         if (rc) return rc;
@@ -405,6 +455,15 @@ extern "C" int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, 
     return rc;
 }
 
+// Slices per call of the uniform route (0: the batch is not uniform; it always runs as the
+// graph of persistent launches).
+extern "C" int xct_batch_plan_uniform(xct_batch_plan *p, int *slices_per_call)
+{
+    if (!p || !slices_per_call) return xct_fail(XCT_E_INVALID, "xct_batch_plan_uniform: null argument");
+    *slices_per_call = p->uni ? p->uni_batch : 0;
+    return XCT_OK;
+}
+
 extern "C" int xct_batch_plan_tuning(xct_batch_plan *p, int *fwd_tile, int *ang_chunk)
 {
     if (!p || !fwd_tile || !ang_chunk) return xct_fail(XCT_E_INVALID, "xct_batch_plan_tuning: null argument");
@@ -421,6 +480,10 @@ extern "C" int xct_batch_plan_autotune(xct_batch_plan *p, const char *cache_path
     XCT_RANGE("xct_batch_plan_autotune");
     if (!p) return xct_fail(XCT_E_INVALID, "xct_batch_plan_autotune: plan is null");
     if (!cache_path) cache_path = xct_tune_env_path();
+    if (p->uni) {  // the uniform route's own tiles
+        int rc = xct_plan_autotune(p->uni, p->uni_batch, cache_path, flags, stream);
+        if (rc) return rc;
+    }
     TuneChoice best;
     if (!(flags & XCT_TUNE_FORCE) && xct_tune_lookup(p->key, cache_path, best))
         return batch_layout(p, best.T, best.chunk);

@@ -41,6 +41,7 @@ KERNELS_PLAIN = 1
 PI_OWN_LAYER = 1
 FISTA_UPDATE_X = 1
 FISTA_ADJOINT = 2
+MULTISLICE_SLICES = 8  # slices per group of the slice-interleaved forward projector
 
 # Every function include/xct.h declares (checked by the tests against the header).
 EXPORTS = (
@@ -55,7 +56,7 @@ EXPORTS = (
     "xct_check_report", "xct_reslice_plan_create", "xct_reslice", "xct_reslice_plan_destroy", "xct_reslice_plan_set_wait_limit",
     "xct_denoise_sinogram",
     "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
-    "xct_plan_multislice", "xct_plan_set_multislice", "xct_batch_plan_set_cs",
+    "xct_plan_multislice", "xct_plan_set_multislice", "xct_batch_plan_set_cs", "xct_batch_plan_uniform",
     "xct_fista_power_iteration", "xct_fista_set_lipschitz", "xct_fista_run_device", "xct_fista_run",
     "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume", "xct_hybrid_cs_run_device",
     "xct_hybrid_cs_run",
@@ -143,6 +144,7 @@ def load():
     L.xct_denoise_sinogram.argtypes = [ip, ip, ip, c_f, vp, vp, vp]
     L.xct_cs_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
     L.xct_batch_plan_set_cs.argtypes = [vp, c_f, ip, ctypes.POINTER(ctypes.c_int)]
+    L.xct_batch_plan_uniform.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.xct_fista_power_iteration.argtypes = [vp, ip, ip, ip, fp, vp]
     L.xct_fista_set_lipschitz.argtypes = [vp, fp]
     L.xct_fista_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, c_f, ip, vp]
@@ -622,6 +624,12 @@ class BatchPlan:
         t, c = ctypes.c_int(), ctypes.c_int()
         _check(self._lib.xct_batch_plan_tuning(self.handle, ctypes.byref(t), ctypes.byref(c)))
         return t.value, c.value
+
+    def uniform(self):
+        """Slices per call of the uniform route (0: the batch always runs as the graph)."""
+        v = ctypes.c_int()
+        _check(self._lib.xct_batch_plan_uniform(self.handle, ctypes.byref(v)))
+        return v.value
 
     def run(self, sinos, imgs, stream=None):
         n = len(self.geoms)

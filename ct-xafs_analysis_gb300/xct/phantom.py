@@ -140,15 +140,23 @@ def ctxafs_item_specs(n, seed=3, widths=(512, 1024, 1536, 2048), angles=(360, 72
     return out
 
 
-def xanes_slice(w, energy_index, seed, spectra, mu_scale=0.02, torch_device=None):
-    """One slice of a CT-XAFS volume at one energy: inside a few ellipses, each voxel is the
-    mixture f*S1(E) + (1-f)*S2(E) with a seeded per-voxel fraction f (smoothed noise), times
-    mu_scale per pixel."""
-    e, s1, s2 = spectra
+def xanes_fields(w, seed):
+    """The energy-independent fields of one CT-XAFS slice: the sample's support (a few
+    ellipses) and the seeded per-voxel fraction f of spectrum 1 (piecewise constant per
+    16x16 voxel block), both [w][w] float64."""
     rng = np.random.default_rng(seed)
     support = rasterize_ellipses(ellipse_params(w, 4, seed, axes=(0.1 * w, 0.35 * w), mu=(1.0, 1.0)), w, w) > 0
     f = rng.uniform(0.0, 1.0, (w // 16 + 1, w // 16 + 1))
-    f = np.kron(f, np.ones((16, 16)))[:w, :w]  # piecewise-constant per 16x16 voxel block
+    f = np.kron(f, np.ones((16, 16)))[:w, :w]
+    return support.astype(np.float64), f
+
+
+def xanes_slice(w, energy_index, seed, spectra, mu_scale=0.02, torch_device=None, fields=None):
+    """One slice of a CT-XAFS volume at one energy: inside a few ellipses, each voxel is the
+    mixture f*S1(E) + (1-f)*S2(E) with a seeded per-voxel fraction f (smoothed noise), times
+    mu_scale per pixel.  fields: xanes_fields(w, seed), computed once for many energies."""
+    e, s1, s2 = spectra
+    support, f = xanes_fields(w, seed) if fields is None else fields
     mu = support * (f * s1[energy_index] + (1.0 - f) * s2[energy_index]) * mu_scale
     mu = mu.astype(np.float32)
     if torch_device is not None:

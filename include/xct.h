@@ -130,7 +130,13 @@ int xct_osem_run_volume(xct_plan *plan, int n, const float *const *sino_host, fl
  *     over stacks: stack_len[s] consecutive slices of one image size form stack s (the lengths
  *     add up to n; nstacks = 0 turns it off), the third axis of the proximal step; every run
  *     then needs each stack's images consecutive in one [dN][ny][nx] array (d_img[i+1] =
- *     d_img[i] + ny*nx within a stack).  Semantics as xct_cs_osem_run_device. */
+ *     d_img[i] + ny*nx within a stack).  Semantics as xct_cs_osem_run_device.
+ * A uniform batch (n >= 2 slices of one geometry: sizes, centre, modes and angle list) whose
+ * sinograms and images are each one array ([n][pa][px], [n][ny][nx]) and that has no stacks
+ * runs through a single-shape plan of the same geometry instead, up to 16 slices per
+ * xct_osem_run_device call (the slice-interleaved forward projector serves such slices
+ * faster than the persistent launches); other runs of the plan use the graph.
+ * xct_batch_plan_uniform reports the slices per call of that route (0: not uniform). */
 typedef struct xct_batch_plan xct_batch_plan;
 int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms, int it, xct_batch_plan **out);
 int xct_batch_run(xct_batch_plan *plan, const float *const *d_sino, float *const *d_img, void *stream);
@@ -138,6 +144,7 @@ int xct_batch_plan_destroy(xct_batch_plan *plan);
 int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, const float *const *d_sino,
                          float *const *d_img, int it, void *stream);
 int xct_batch_plan_set_cs(xct_batch_plan *plan, float cs_lambda, int nstacks, const int *stack_len);
+int xct_batch_plan_uniform(xct_batch_plan *plan, int *slices_per_call);
 
 /* ---- OS-EM without any allocation ----------------------------------------------------
  * No counterpart in the reference: the reference allocates its image objects on every call.
@@ -398,15 +405,17 @@ int xct_batch_plan_tuning(xct_batch_plan *plan, int *fwd_tile, int *ang_chunk);
 /* ---- slice-interleaved forward projector -------------------------------------------------
  * No counterpart in the reference (its OSEM1 work-items each sum one ray of one slice).  The
  * slices of one OS-EM call share their geometry, so a plan can forward-project them in
- * groups of eight: a CTA stages one tile of eight slices, and the eight lanes of each
- * quarter-warp take the same sample of one ray in the eight slices (one shared-memory line,
- * no bank conflict; the ray's interval and coordinates are found once for all eight).  With
+ * groups of XCT_MULTISLICE_SLICES (eight): a CTA stages one tile of the eight slices (one
+ * 128-byte line of bilinear coefficients per texel), each quarter-warp walks two rays as one
+ * stream of samples, and each lane reads the eight slices of its sample in a rotated order
+ * (no shared-memory bank conflict; a sample's coordinates are found once for all eight).  With
  * it on, a call's slices go in groups of eight through it and the rest through the per-slice
  * tiled kernel, and a call that runs as two halves cuts them at a multiple of eight.  The
  * value is the number of subset angles one CTA serves (1..128); 0 turns it off.  Plans start
  * with the cached or autotuned choice, else on (128) when max_batch >= 8 and the tiles of one
  * group give at least two CTAs per SM.  Results agree with the per-slice kernel to float
  * rounding of the partial ray sums. */
+#define XCT_MULTISLICE_SLICES 8
 int xct_plan_multislice(xct_plan *plan, int *ang_chunk);
 int xct_plan_set_multislice(xct_plan *plan, int ang_chunk);
 

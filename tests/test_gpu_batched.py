@@ -188,3 +188,47 @@ def test_batched_compressed_sensing_stacks(gpu_ctx, oracle_lib):
     with pytest.raises(xct.XCTError):
         bp.run(sinos, loose)
     bp.close()
+
+
+def test_uniform_batch_route(gpu_ctx, oracle_lib):
+    """A batch of 16 slices of one geometry (512^2, 90 angles; the slice-interleaved forward
+    projector's shape) in one pair of arrays takes the uniform route -- a single-shape plan,
+    16 slices per call -- and gives the single-plan result; the same plan with the images in
+    separate allocations replays its graph of persistent launches; both against the oracle."""
+    import xct
+    from xct import phantom as P
+    O = oracle_lib
+    n, pa, ss, it, dn = 512, 90, 5, 2, 16
+    ang = P.uniform_angles(pa)
+    prm = P.ellipsoid_params(n, dn, count=8, seed=61)
+    meas = np.stack([P.noisy_log_sinogram(O.projection(P.ellipsoid_slice(prm, z, n, n), ang, n), 1e5, z)
+                     for z in range(dn)]).astype(np.float32)
+    d_s = torch.from_numpy(meas).cuda()
+    geoms = [xct.make_geom(n, n, n, ang, ss, it) for _ in range(dn)]
+    bp = xct.BatchPlan(gpu_ctx, geoms, it)
+    assert bp.uniform() == dn
+    plan = xct.OSEMPlan(gpu_ctx, n, n, n, ang, ss, it, max_batch=dn)
+    x1 = torch.ones((dn, n, n), device="cuda")
+    plan.run_device(d_s, x1)
+    arr = torch.ones((dn, n, n), device="cuda")
+    bp.run([d_s[z] for z in range(dn)], [arr[z] for z in range(dn)])
+    sep = [torch.ones((n, n), device="cuda") for _ in range(dn)]
+    bp.run([d_s[z] for z in range(dn)], sep)
+    torch.cuda.synchronize()
+    single = x1.cpu().numpy().astype(np.float64)
+    routed = arr.cpu().numpy().astype(np.float64)
+    graph = torch.stack(sep).cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(routed - single) / np.linalg.norm(single) <= 1e-6
+    assert np.linalg.norm(graph - single) / np.linalg.norm(single) <= 1e-6
+    for z in (0, dn - 1):
+        ref = O.osem_run(np.ones((n, n), np.float32), meas[z], ang, ss, it, order=O.ORDER_LITERAL)
+        for got in (routed[z], graph[z]):
+            assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-4, z
+            assert np.abs(got - ref).max() <= 1e-3 * np.abs(ref).max(), z
+    plan.close()
+    bp.close()
+    # different angle lists: not uniform
+    g2 = [xct.make_geom(64, 64, 64, ang, ss, it), xct.make_geom(64, 64, 64, ang + 0.5, ss, it)]
+    bp2 = xct.BatchPlan(gpu_ctx, g2, it)
+    assert bp2.uniform() == 0
+    bp2.close()
