@@ -295,21 +295,24 @@ __global__ void __launch_bounds__(kFwdThreads, FwdTile<T>::MinBlocks) fwd_tiled_
 // owns a T x T tile of base texels of eight slices; shared memory holds, per base texel, one
 // 16-byte element per slice -- (t00, t10 - t00, t01 - t00, (t11 - t01) - (t10 - t00)), the
 // whole 2x2 footprint -- and a texel's eight elements are one 128-byte record.  A warp takes
-// eight rays of one angle, a quarter-warp (eight lanes) per pair of consecutive rays A, B:
-// the pair's samples form one stream (A's interval in the tile, then B's), lane p taking
-// stream positions p, p + 8, ...  For each sample a lane finds the coordinates, floor and
-// record once and then reads the eight slices' elements starting at slot p and wrapping, so
-// at every load the quarter's eight lanes read eight different 16-byte bank groups: no load
-// has a bank conflict whatever the geometry, the coordinate work is spread over eight
-// slice-samples, a quarter whose stream is done costs no shared-memory wavefronts, and only
-// the stream's last pass leaves lanes idle (one pass per two rays).  Slot r of lane p
-// accumulates slice (r + p) mod 8, separately for A and B; eight shuffles give lane p the
-// quarter's totals for slice p, which it adds to the double accumulator with one atomic per
-// ray.  Work items (angle, eight rays) are taken from a shared counter, so warps finish
-// within one item of each other.
+// eight rays of one angle, a quarter-warp (eight lanes) per pair of consecutive rays: lanes
+// 0-3 of the quarter walk the first ray's samples in the tile, lanes 4-7 the second's, lane j
+// of a ray taking its samples j, j + 4, ...  For each sample a lane finds the coordinates,
+// floor and record once and then reads the eight slices' elements starting at slot p (its
+// lane in the quarter) and wrapping, so at every load the quarter's eight lanes read eight
+// different 16-byte bank groups: no load has a bank conflict whatever the geometry, the
+// coordinate work is spread over eight slice-samples, and a quarter whose rays are done
+// costs no shared-memory wavefronts.  The bilinear value of one slice,
+// t00 + fy dy + fx (dx + fy dxy), is two packed-pair FMAs: (t00, dx) + fy (dy, dxy), then
+// added into the slot's pair of partial sums with weights (1, fx).  Slot r of lane p
+// accumulates slice (r + p) mod 8; eight shuffles give lane p the quarter's totals for slice
+// p of both rays, which it adds to the double accumulator with one atomic per ray.  Work
+// items (angle, eight rays) are taken from a shared counter, so warps finish within one item
+// of each other.
 constexpr int kMsSlices = 8;
 constexpr int kMsThreads = 512;
 constexpr int kMsRays = 2 * 32 / kMsSlices;  // rays per warp (a pair per quarter-warp)
+constexpr int kMsLanesPerRay = kMsSlices / 2;
 constexpr int kMsTile = 42;              // base texels per tile side: 42^2 x 128 B = 221 KB
 constexpr int kMsStageRows = 6;          // element rows per staging strip
 
@@ -344,47 +347,24 @@ __device__ __forceinline__ double f32_to_f64(float v)
     return (double)v;
 }
 
-// Pass i of a quarter's ray-pair stream for lane ph: the sample (stream position 8i + ph,
-// of ray A below LA), its fractions and the byte address of its base texel's record.
-__device__ __forceinline__ unsigned ms_locate(int i, int ph, int LA, float ycA, float ycB, f2x sc, f2x axyA,
-                                              f2x axyB, f2x MM, unsigned base2, int T, float &fx, float &fy,
-                                              bool &onA)
+// One slice element (t00, dx | dy, dxy) of a record as two packed pairs.
+__device__ __forceinline__ void lds_2f2(unsigned addr, f2x &lo, f2x &hi)
 {
-    onA = kMsSlices * i + ph < LA;
-    const float yc = (onA ? ycA : ycB) + (float)(kMsSlices * i);
-    const f2x xy = f2_fma(f2_pack(yc, yc), sc, onA ? axyA : axyB);
-    const f2x tb = f2_add_rd(xy, MM);
-    const f2x fr = f2_sub(xy, f2_sub(tb, MM));
-    int ixb, iyb;
-    f2_unpack_bits(tb, ixb, iyb);
-    f2_unpack(fr, fx, fy);
-    return ((unsigned)iyb * (unsigned)T + (unsigned)ixb) * (unsigned)(kMsSlices * 16) + base2;
+    asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];" : "=l"(lo), "=l"(hi) : "r"(addr));
 }
 
-// The eight slices' elements of one record, slot r from byte offset off[r].
-__device__ __forceinline__ void ms_load(float4 (&e)[kMsSlices], unsigned rec, const unsigned (&off)[kMsSlices],
-                                        unsigned alo, unsigned ahi)
+// The eight slices' elements of the record at byte address rec, slot r from offset off[r],
+// added to the slots' partial sums: part[r] += (1, fx) * ((t00, dx) + fy * (dy, dxy)).
+__device__ __forceinline__ void ms_tap(unsigned rec, const unsigned (&off)[kMsSlices], unsigned alo, unsigned ahi,
+                                       float fx, float fy, f2x (&part)[kMsSlices])
 {
-    if (!XCT_IN(rec, alo, ahi, XCT_SITE_FWD_MS_TAP)) {
+    if (!XCT_IN(rec, alo, ahi, XCT_SITE_FWD_MS_TAP)) return;
+    f2x lo[kMsSlices], hi[kMsSlices];
 #pragma unroll
-        for (int r = 0; r < kMsSlices; ++r) e[r] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        return;
-    }
+    for (int r = 0; r < kMsSlices; ++r) lds_2f2(rec + off[r], lo[r], hi[r]);
+    const f2x fy2 = f2_pack(fy, fy), wx = f2_pack(1.0f, fx);
 #pragma unroll
-    for (int r = 0; r < kMsSlices; ++r) e[r] = lds_f4(rec + off[r]);
-}
-
-// The bilinear values of one record's eight slices, added to ray A's or B's slot sums
-// (predicated adds: a non-finite sample stays in its own ray).
-__device__ __forceinline__ void ms_accumulate(const float4 (&e)[kMsSlices], float fx, float fy, bool onA,
-                                              float (&sumA)[kMsSlices], float (&sumB)[kMsSlices])
-{
-#pragma unroll
-    for (int r = 0; r < kMsSlices; ++r) {
-        const float val = fmaf(fy, fmaf(fx, e[r].w, e[r].z), fmaf(fx, e[r].y, e[r].x));
-        if (onA) sumA[r] += val;
-        else sumB[r] += val;
-    }
+    for (int r = 0; r < kMsSlices; ++r) part[r] = f2_fma(wx, f2_fma(fy2, hi[r], lo[r]), part[r]);
 }
 
 // grid: (ntx*nty tiles, angle chunks, dN / 8 slice groups); acc [dN][nrows][px] doubles.
@@ -488,9 +468,11 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
 
     const int total = tail[0];
     const int lane = threadIdx.x & 31;
-    const int ph = lane & (kMsSlices - 1);    // stream phase; also this lane's first slot
+    const int ph = lane & (kMsSlices - 1);    // lane of the quarter; also this lane's first slot
     const int qb = lane & ~(kMsSlices - 1);   // first lane of the quarter
     const int pair = lane >> 3;               // ray pair of the warp's four
+    const int half = ph / kMsLanesPerRay;     // 0: the pair's first ray, 1: its second
+    const int jr = ph % kMsLanesPerRay;       // this lane's phase in its ray's samples
     const int D = g.depth;
     // byte address of the record of base texel (col, row) from the floor bits:
     // (iy_bits * T + ix_bits) * 128 + base2, the biases folded into base2 (mod 2^32)
@@ -504,11 +486,10 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
 #pragma unroll
     for (int r = 0; r < kMsSlices; ++r) off[r] = 16u * (unsigned)((r + ph) & (kMsSlices - 1));
     const f2x MM = f2_pack(kMagic, kMagic);
-    // lane ph of a quarter finds one interval limit of ray A (ph < 4) or B (ph >= 4): the
-    // lower (even) or upper (odd) Y limit from the x (ph & 3 < 2) or the y coordinate
-    const bool bound_x = (ph & 3) < 2;
-    const bool upper = (ph & 1) != 0;
-    const bool of_b = ph >= 4;
+    // the four lanes of a ray find its four interval limits: the lower (even jr) or upper
+    // (odd jr) Y limit from the x (jr < 2) or the y coordinate
+    const bool bound_x = jr < 2;
+    const bool upper = (jr & 1) != 0;
     int *counter = tail + 1;
     int k = 0;  // the warp's current angle: items only grow, so the search runs forward
 
@@ -519,15 +500,14 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
         if (item >= total) break;
         while (k + 1 < kn && gpre[k + 1] <= item) ++k;  // the last k with gpre[k] <= item
         const float c = scs[k].x, s = scs[k].y;
-        // the quarter's two consecutive rays A = XA and B = XA + 1
+        // the quarter's two consecutive rays XA and XA + 1; this lane's ray X
         const int XA = xlo_s[k] + (item - gpre[k]) * kMsRays + 2 * pair;
-        const int Xhi = xhi_s[k];
-        const int Xl = XA + (of_b ? 1 : 0);
-        const float Xc = (float)Xl - g.cx;
+        const int X = XA + half;
+        const float Xc = (float)X - g.cx;
         const float ax = fmaf(Xc, c, g.hx);
         const float ay = fmaf(Xc, -s, g.hy);
         int v = 0;
-        if (Xl <= Xhi) {
+        if (X <= xhi_s[k]) {
             const float a = bound_x ? ax : ay, sl = bound_x ? s : c;
             const float isl = bound_x ? inv_s[k].y : inv_s[k].x;
             const float lo_ = bound_x ? xlo : ylo, hi_ = bound_x ? xhi : yhi;
@@ -539,55 +519,52 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
                 v = upper ? ((a >= lo_ && a < hi_) ? D : 0) : 0;
             }
         }
-        // this lane's ray's limits: lower ones (even ph) max-combined, upper ones min-combined
-        // across the x and y limits (xor 2), then exchanged within the pair of lanes (xor 1)
-        // and with the other ray's lanes (xor 4)
+        // the ray's limits: lower ones (even jr) max-combined, upper ones min-combined across
+        // the x and y limits (xor 2), then exchanged within the pair of lanes (xor 1)
         const int w = __shfl_xor_sync(0xffffffffu, v, 2);
         const int m = upper ? min(v, w) : max(v, w);
         const int u = __shfl_xor_sync(0xffffffffu, m, 1);
-        const int ya_own = upper ? u : m, yb_own = upper ? m : u;
-        const int ya_oth = __shfl_xor_sync(0xffffffffu, ya_own, 4);
-        const int yb_oth = __shfl_xor_sync(0xffffffffu, yb_own, 4);
-        const int yaA = of_b ? ya_oth : ya_own, ybA = of_b ? yb_oth : yb_own;
-        const int yaB = of_b ? ya_own : ya_oth, ybB = of_b ? yb_own : yb_oth;
-        const int LA = max(ybA - yaA, 0), LB = max(ybB - yaB, 0);
-        // the ray parameters of A and B
-        const float XcA = (float)XA - g.cx, XcB = (float)(XA + 1) - g.cx;
-        const float axA = fmaf(XcA, c, g.hx), ayA = fmaf(XcA, -s, g.hy);
-        const float axB = fmaf(XcB, c, g.hx), ayB = fmaf(XcB, -s, g.hy);
-        // stream position t = 8i + ph: sample yaA + t of A for t < LA, else sample
-        // yaB + t - LA of B; Yc = Y - hd is tracked as a float (exact small integers)
-        const int n = (LA + LB > ph) ? (LA + LB - ph + kMsSlices - 1) / kMsSlices : 0;
-        const float ycA = (float)(yaA + ph) - g.hd, ycB = (float)(yaB - LA + ph) - g.hd;
+        const int ya = upper ? u : m, yb = upper ? m : u;
+        const int L = max(yb - ya, 0);
+        const int Lo = __shfl_xor_sync(0xffffffffu, L, kMsLanesPerRay);  // the other ray's
+        // samples ya + jr, ya + jr + 4, ... of this lane's ray; Yc = Y - hd is tracked as a
+        // float (exact small integers)
+        const int n = L > jr ? (L - jr + kMsLanesPerRay - 1) / kMsLanesPerRay : 0;
+        float yc = (float)(ya + jr) - g.hd;
         const f2x sc = f2_pack(s, c);
-        const f2x axyA = f2_pack(axA, ayA), axyB = f2_pack(axB, ayB);
-        float sumA[kMsSlices], sumB[kMsSlices];
+        const f2x axy = f2_pack(ax, ay);
+        f2x part[kMsSlices];
 #pragma unroll
-        for (int r = 0; r < kMsSlices; ++r) {
-            sumA[r] = 0.0f;
-            sumB[r] = 0.0f;
-        }
-        for (int i = 0; i < n; ++i) {
+        for (int r = 0; r < kMsSlices; ++r) part[r] = 0ull;
+        for (int i = 0; i < n; ++i, yc += (float)kMsLanesPerRay) {
+            const f2x xy = f2_fma(f2_pack(yc, yc), sc, axy);
+            const f2x tb = f2_add_rd(xy, MM);
+            const f2x fr = f2_sub(xy, f2_sub(tb, MM));
+            int ixb, iyb;
             float fx, fy;
-            bool onA;
-            float4 e[kMsSlices];
-            ms_load(e, ms_locate(i, ph, LA, ycA, ycB, sc, axyA, axyB, MM, base2, T, fx, fy, onA), off, alo, ahi);
-            ms_accumulate(e, fx, fy, onA, sumA, sumB);
+            f2_unpack_bits(tb, ixb, iyb);
+            f2_unpack(fr, fx, fy);
+            ms_tap(((unsigned)iyb * (unsigned)T + (unsigned)ixb) * (unsigned)(kMsSlices * 16) + base2, off, alo, ahi,
+                   fx, fy, part);
         }
-        // lane p's slot d holds slice (d + p) mod 8: lane p gathers slice p's partial sums from
-        // lanes (p - d) mod 8 of its quarter, slot d -- for A and for B
-        float totA = 0.0f, totB = 0.0f;
+        // lane p gathers slice p's partial sums from lanes (p - d) mod 8 of its quarter, slot
+        // d: lanes 0-3 hold the first ray's, lanes 4-7 the second's
+        float tot0 = 0.0f, tot1 = 0.0f;
 #pragma unroll
         for (int d = 0; d < kMsSlices; ++d) {
-            const int src = qb + ((ph - d) & (kMsSlices - 1));
-            totA += __shfl_sync(0xffffffffu, sumA[d], src);
-            totB += __shfl_sync(0xffffffffu, sumB[d], src);
+            const int sp = (ph - d) & (kMsSlices - 1);
+            float plo, phi;
+            f2_unpack(part[d], plo, phi);
+            const float pv = __shfl_sync(0xffffffffu, plo + phi, qb + sp);
+            if (sp < kMsLanesPerRay) tot0 += pv;
+            else tot1 += pv;
         }
+        const int L0 = half ? Lo : L, L1 = half ? L : Lo;
         double *accz = acc + ((size_t)(z0 + ph) * nrows + k0 + k) * g.px;
-        if (LA > 0 && XCT_IN((long long)k * g.px + XA, 0, (long long)(nrows - k0) * g.px - 1, XCT_SITE_FWD_ACC))
-            atomicAdd(accz + XA, f32_to_f64(totA));
-        if (LB > 0 && XCT_IN((long long)k * g.px + XA + 1, 0, (long long)(nrows - k0) * g.px - 1, XCT_SITE_FWD_ACC))
-            atomicAdd(accz + XA + 1, f32_to_f64(totB));
+        if (L0 > 0 && XCT_IN((long long)k * g.px + XA, 0, (long long)(nrows - k0) * g.px - 1, XCT_SITE_FWD_ACC))
+            atomicAdd(accz + XA, f32_to_f64(tot0));
+        if (L1 > 0 && XCT_IN((long long)k * g.px + XA + 1, 0, (long long)(nrows - k0) * g.px - 1, XCT_SITE_FWD_ACC))
+            atomicAdd(accz + XA + 1, f32_to_f64(tot1));
     }
 }
 
