@@ -974,8 +974,10 @@ def main():
         "slices_per_launch": G, "traffic": None,
         "hbm": {"achieved_gbs": fwd_bytes / (fwd_ms_avg * 1e-3) / 1e9, "peak_gbs": None,
                 "note": "compulsory image bytes per launch over its time"},
-        "bp": {"kernel": "bp_tiled_kernel (OSEM2 backprojection+update)", "ms_per_launch": bp_ms_avg,
-               "achieved_tflops": bp_flop_per_launch / (bp_ms_avg * 1e-3) / 1e12},
+        "bp": {"kernel": "bp_ms_kernel (OSEM2 backprojection+update, 8 slices per launch)", "ms_per_launch": bp_ms_avg,
+               "achieved_tflops": bp_flop_per_launch / (bp_ms_avg * 1e-3) / 1e12,
+               "frac": bp_flop_per_launch / (bp_ms_avg * 1e-3) / 1e12 / fp32_peak,
+               "gathers_per_launch": t_bp.sum() / SS * G},
         "share": {k: prof[k]["ms"] / prof["total"]["ms"] for k in ("fwd", "finalize", "bp")},
     }
     try:

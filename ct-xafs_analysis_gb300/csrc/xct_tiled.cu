@@ -938,6 +938,184 @@ __global__ void __launch_bounds__(BpCfg<R>::Threads) bp_tiled_kernel(float *__re
             (int)blockIdx.x % ntx, (int)blockIdx.x / ntx, ssf, paf, sh);
 }
 
+// --------------------------------------------- backprojector, eight slices per tile
+// For the slices of one OS-EM call (one geometry) a (pixel, angle) pair reads the same bin in
+// all eight slices of a group, so the bin expression is evaluated once for eight gathers.  A
+// CTA of 256 threads owns a 32 x 32 pixel tile of eight slices and stages, per angle and
+// slice, the window of the tile's bins (< 48, bounded exactly by the tile corners as in
+// bp_tiled_kernel, its start rounded down to a multiple of 4) with asynchronous 16-byte copies
+// (zero-filled off the detector), 24 angles at a time.  A thread takes 4 pixels of one row (8
+// apart), a warp 8 adjacent pixels in each of 4 rows: the bins one load instruction touches
+// span fewer than 32 consecutive words, so no load has a bank conflict.  Per pixel and angle:
+// the literal bin expression of bp_tiled_kernel, one address, eight 4-byte loads at constant
+// offsets (one per slice), four packed adds -- in angle order, so each slice's sum is
+// bp_tiled_kernel's bit for bit -- and the update at the end.
+constexpr int kBpMsT = 32;
+constexpr int kBpMsThreads = 256;
+constexpr int kBpMsW = 52;      // staged bins per angle and slice (>= 31|c| + 31|s| + 3 + 3 = 49.9)
+constexpr int kBpMsChunk = 24;  // angles per staging pass
+constexpr int kBpMsPix = 4;     // pixels per thread, 8 apart
+constexpr unsigned kBpMsSliceBytes = (unsigned)(kBpMsChunk * kBpMsW * 4);  // one slice's windows
+
+struct BpMsShared {
+    float win[kMsSlices * kBpMsChunk * kBpMsW];  // [slice][angle][bin]
+    float2 scs[kBpMsChunk];                      // (c, s)
+    int slo[kBpMsChunk];                         // first staged bin (a multiple of 4)
+    unsigned soff[kBpMsChunk];                   // byte address of slice 0's entry (bits - BIAS - lo)
+};
+
+__device__ __forceinline__ void cp_async16(unsigned dst, const void *src, unsigned src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async4(unsigned dst, const void *src, unsigned src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int kOff>
+__device__ __forceinline__ float lds_f1_at(unsigned addr)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1+%2];" : "=f"(v) : "r"(addr), "n"(kOff));
+    return v;
+}
+
+// grid: (ntx*nty tiles of 32 x 32, 1, dN / 8 slice groups).  vec: 16-byte staging copies
+// (px a multiple of 4 and a 16-byte aligned ratio array).
+__global__ void __launch_bounds__(kBpMsThreads) bp_ms_kernel(float *__restrict__ img, const float *__restrict__ ratio,
+                                                             const float2 *__restrict__ trig, KGeom g, int sub,
+                                                             int nang, int ntx, float ssf, float paf, int vec)
+{
+    __shared__ __align__(16) BpMsShared sh;
+    const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
+    const int z0 = (int)blockIdx.z * kMsSlices;
+    const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.pa * g.px;
+    const float *rz = ratio + (size_t)z0 * nprj;
+    const int X0 = bx * kBpMsT, Y0 = by * kBpMsT;
+    const int X1 = min(X0 + kBpMsT, g.nx) - 1, Y1 = min(Y0 + kBpMsT, g.ny) - 1;
+    const int t = threadIdx.x;
+    const int tx = t & 7, ty = t >> 3;
+    // pixel i of this thread: (X0 + tx + 8i, Y0 + ty); threads past the image edge of a partial
+    // tile gather for the edge pixel (inside the staged window) and write nothing
+    const float Yc = (float)min(Y0 + ty, Y1) - g.hy;
+    float xc[kBpMsPix];
+#pragma unroll
+    for (int i = 0; i < kBpMsPix; ++i) xc[i] = (float)min(X0 + tx + 8 * i, X1) - g.hx;
+    f2x acc[kBpMsPix][kMsSlices / 2];  // slice pairs of each pixel
+#pragma unroll
+    for (int i = 0; i < kBpMsPix; ++i)
+#pragma unroll
+        for (int h = 0; h < kMsSlices / 2; ++h) acc[i][h] = 0ull;
+    const f2x cxp = f2_pack(g.cx, g.cx);
+    const f2x hp = f2_pack(0.5f, 0.5f);
+    const f2x MM = f2_pack(kMagic, kMagic);
+    const unsigned wbase = (unsigned)__cvta_generic_to_shared(sh.win);
+
+    for (int k0 = 0; k0 < nang; k0 += kBpMsChunk) {
+        const int kn = min(kBpMsChunk, nang - k0);
+        __syncthreads();  // the previous chunk's gathers are done with the shared arrays
+        for (int k = t; k < kn; k += kBpMsThreads) {
+            const float2 cs = trig[sub + (k0 + k) * g.ss];
+            sh.scs[k] = cs;
+            // the bin coordinate is monotone in X and in Y: the corners bound the window
+            const float xa = (float)X0 - g.hx, xb = (float)X1 - g.hx;
+            const float yA = (float)Y0 - g.hy, yB = (float)Y1 - g.hy;
+            const float qa = yA * cs.y, qb = yB * cs.y;
+            int lo = xct_floor_bits(xct_bin_coord(xa, cs.x, qa, g.cx));
+            lo = min(lo, xct_floor_bits(xct_bin_coord(xb, cs.x, qa, g.cx)));
+            lo = min(lo, xct_floor_bits(xct_bin_coord(xa, cs.x, qb, g.cx)));
+            lo = min(lo, xct_floor_bits(xct_bin_coord(xb, cs.x, qb, g.cx)));
+            lo &= ~3;  // the bias is a multiple of 4: this rounds the bin down to one
+            sh.slo[k] = lo - XCT_FLOOR_BIAS;
+            // slice 0's entry for floor bits fb: wbase + 4*(k*W + fb - lo)  (mod 2^32)
+            sh.soff[k] = wbase + 4u * (unsigned)(k * kBpMsW) - 4u * (unsigned)lo;
+        }
+        __syncthreads();
+        // window (z, k) = ratio[z0 + z][th_k][lo_k .. lo_k + W), 0 off the detector
+        if (vec) {
+            constexpr int kQ = kBpMsW / 4;
+            for (int i = t; i < kn * kMsSlices * kQ; i += kBpMsThreads) {
+                const int q = i % kQ, r = i / kQ;
+                const int z = r & (kMsSlices - 1), k = r >> 3;
+                const int bin = sh.slo[k] + 4 * q;
+                const int th = sub + (k0 + k) * g.ss;
+                const float *row = rz + (size_t)z * nprj + (size_t)th * g.px;
+                const int nb = bin < 0 ? 0 : min(4, g.px - bin);
+                const unsigned dst = wbase + (unsigned)z * kBpMsSliceBytes + 4u * (unsigned)(k * kBpMsW + 4 * q);
+                cp_async16(dst, nb > 0 ? (const void *)(row + bin) : (const void *)row, nb > 0 ? 4u * (unsigned)nb : 0u);
+            }
+        } else {
+            for (int i = t; i < kn * kMsSlices * kBpMsW; i += kBpMsThreads) {
+                const int j = i % kBpMsW, r = i / kBpMsW;
+                const int z = r & (kMsSlices - 1), k = r >> 3;
+                const int bin = sh.slo[k] + j;
+                const int th = sub + (k0 + k) * g.ss;
+                const float *row = rz + (size_t)z * nprj + (size_t)th * g.px;
+                const bool in = (unsigned)bin < (unsigned)g.px;
+                const unsigned dst = wbase + (unsigned)z * kBpMsSliceBytes + 4u * (unsigned)(k * kBpMsW + j);
+                cp_async4(dst, in ? (const void *)(row + bin) : (const void *)row, in ? 4u : 0u);
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        const unsigned wlo = wbase, whi = wbase + 4u * (unsigned)(kn * kBpMsW - 1);
+        (void)wlo;
+        (void)whi;
+        for (int k = 0; k < kn; ++k) {
+            const float c = sh.scs[k].x, s = sh.scs[k].y;
+            const unsigned off = sh.soff[k];
+            const float q = Yc * s;
+#pragma unroll
+            for (int j = 0; j < kBpMsPix / 2; ++j) {
+                // the literal bin expression of bp_tiled_kernel for pixels 2j and 2j+1
+                const float pa_ = xc[2 * j] * c, pb_ = xc[2 * j + 1] * c;
+                const f2x tt = f2_add_rd(f2_add(f2_add(f2_pack(pa_ - q, pb_ - q), cxp), hp), MM);
+                int b0, b1;
+                f2_unpack_bits(tt, b0, b1);
+                const unsigned ad[2] = {(unsigned)b0 * 4u + off, (unsigned)b1 * 4u + off};
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    float v[kMsSlices];
+                    if (XCT_IN(ad[u], wlo, whi, XCT_SITE_BP_WIN)) {
+                        v[0] = lds_f1_at<0 * kBpMsSliceBytes>(ad[u]);
+                        v[1] = lds_f1_at<1 * kBpMsSliceBytes>(ad[u]);
+                        v[2] = lds_f1_at<2 * kBpMsSliceBytes>(ad[u]);
+                        v[3] = lds_f1_at<3 * kBpMsSliceBytes>(ad[u]);
+                        v[4] = lds_f1_at<4 * kBpMsSliceBytes>(ad[u]);
+                        v[5] = lds_f1_at<5 * kBpMsSliceBytes>(ad[u]);
+                        v[6] = lds_f1_at<6 * kBpMsSliceBytes>(ad[u]);
+                        v[7] = lds_f1_at<7 * kBpMsSliceBytes>(ad[u]);
+                    } else {
+#pragma unroll
+                        for (int z = 0; z < kMsSlices; ++z) v[z] = 0.0f;
+                    }
+#pragma unroll
+                    for (int h = 0; h < kMsSlices / 2; ++h)
+                        acc[2 * j + u][h] = f2_add(acc[2 * j + u][h], f2_pack(v[2 * h], v[2 * h + 1]));
+                }
+            }
+        }
+    }
+    const int Y = Y0 + ty;
+    if (Y > Y1) return;
+#pragma unroll
+    for (int i = 0; i < kBpMsPix; ++i) {
+        const int X = X0 + tx + 8 * i;
+        if (X > X1) continue;
+#pragma unroll
+        for (int h = 0; h < kMsSlices / 2; ++h) {
+            float v0, v1;
+            f2_unpack(acc[i][h], v0, v1);
+            float *p0 = img + (size_t)(z0 + 2 * h) * nimg + (size_t)Y * g.nx + X;
+            *p0 = xct_update(*p0, v0, ssf, paf);
+            float *p1 = p0 + nimg;
+            *p1 = xct_update(*p1, v1, ssf, paf);
+        }
+    }
+}
+
 // ----------------------------------------------------------------- batched launches
 // One subset step of many slices of different shapes in one persistent launch per kernel:
 // CTAs take (slice, tile) work units from a device queue (an atomic counter) until the
@@ -1267,6 +1445,22 @@ int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const
 {
     if (dN <= 0) return XCT_OK;
     const int nang = (g.pa - sub + g.ss - 1) / g.ss;  // OSEM2's angle loop (OSEM.cl:93)
+    // with the slice-interleaved kernels on, whole groups of eight slices go through the
+    // eight-slice backprojector and the rest through the per-slice one
+    const int ms = g.ms_chunk > 0 ? (dN / kMsSlices) * kMsSlices : 0;
+    if (ms > 0) {
+        const int mtx = (g.nx + kBpMsT - 1) / kBpMsT, mty = (g.ny + kBpMsT - 1) / kBpMsT;
+        dim3 mgrid(mtx * mty, 1, ms / kMsSlices);
+        const int vec = g.px % 4 == 0 && ((uintptr_t)ratio & 15u) == 0;
+        bp_ms_kernel<<<mgrid, kBpMsThreads, 0, st>>>(img, ratio, trig, g, sub, nang, mtx, (float)g.ss, (float)g.pa,
+                                                     vec);
+        g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+        XCT_CUDA_TRY(cudaGetLastError());
+        if (ms == dN) return XCT_OK;
+        img += (size_t)ms * g.nx * g.ny;
+        ratio += (size_t)ms * g.pa * g.px;
+        dN -= ms;
+    }
     const int ntx = (g.nx + kBpTX - 1) / kBpTX, nty = (g.ny + kBpTY - 1) / kBpTY;
     dim3 grid(ntx * nty, 1, dN);
     // four rows per thread once the grid gives three waves of its resident CTAs (6 per SM)

@@ -1,5 +1,6 @@
-"""The slice-interleaved forward projector (groups of eight slices of one geometry, one
-128-byte shared-memory line per texel; xct_plan_set_multislice).
+"""The slice-interleaved kernels (groups of eight slices of one geometry;
+xct_plan_set_multislice): the forward projector (one 128-byte shared-memory line per texel)
+and the backprojector (one 32-byte window entry per bin holding the eight slices' ratios).
 
 It must compute what the per-slice tiled kernel computes -- the same samples and bilinear
 weights; only the order in which a ray's samples are added differs (one lane walks the
@@ -113,3 +114,33 @@ def test_multislice_default_and_switch(gpu_ctx):
     with pytest.raises(RuntimeError):
         plain.set_multislice(16)
     plain.close()
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_multislice_backprojector_bit_identical(gpu_ctx, oracle_lib, case):
+    """OSEM2 of dN slices with the eight-slice backprojector (groups of eight, the rest per
+    slice) gives every slice the per-slice kernel's image bit for bit, and the oracle's
+    (OSEM.cl:71-105 in the GPU order, which is the literal bin expression) bit for bit."""
+    import xct
+    O = oracle_lib
+    nx, ny, px, pa, ss, span, off, dN, chunk = CASES[case]
+    ang, imgs, cx = _case(CASES[case], 60 + case)
+    rng = np.random.default_rng(70 + case)
+    ratio = rng.uniform(0.5, 1.5, (dN, pa, px)).astype(np.float32)
+    plan = xct.OSEMPlan(gpu_ctx, nx, ny, px, ang, ss, 1, center_bin=cx, max_batch=dN)
+    d_r = torch.from_numpy(ratio).cuda()
+    for sub in (0, ss - 1):
+        plan.set_multislice(0)
+        ref = torch.from_numpy(imgs).cuda()
+        plan.osem2(sub, ref, d_r)
+        plan.set_multislice(chunk)
+        got = torch.from_numpy(imgs).cuda()
+        plan.osem2(sub, got, d_r)
+        torch.cuda.synchronize()
+        g = got.cpu().numpy()
+        r = ref.cpu().numpy()
+        assert np.array_equal(g, r), (sub, int(np.count_nonzero(g != r)))
+        for z in (0, dN - 1):
+            want = O.osem2(imgs[z], ratio[z], ang, ss, sub, cx=cx, order=O.ORDER_GPU)
+            assert np.array_equal(g[z], want), (sub, z, int(np.count_nonzero(g[z] != want)))
+    plan.close()
