@@ -755,6 +755,215 @@ __global__ void __launch_bounds__(kThreads) adj_tiled_kernel(const float *__rest
     }
 }
 
+// The exact adjoint over S slices of one geometry at once: adj_tiled_kernel's samples,
+// windows, fixed-point scales (one per slice and window) and epilogue, with each sample's
+// coordinates, weights and accumulator offset found once for the S slices.  Tile 32 texels;
+// the (T+2)^2 accumulators of a slice are kept at a pitch of 37 (a CPU model of the 32 lanes'
+// footprints over all angles gives 2.0 bank wavefronts per atomic instruction at this pitch,
+// 3.0 at pitch 34).  grid: (ntx*nty tiles, 1, dN / S slice groups); dynamic shared memory
+// AdjMs<S>::Smem.
+constexpr int kAdjMsT = 32, kAdjMsP = 37, kAdjMsR = kAdjMsT + 2;
+constexpr int kAdjMsSlices = 4;  // slices per adjoint group
+constexpr int kAdjMsN = kAdjMsR * kAdjMsP;  // accumulator entries per slice
+template <int S>
+struct AdjMs {
+    static constexpr size_t Smem = (size_t)S * kAdjMsN * (sizeof(float) + sizeof(int)) + kAdjWarps * S * sizeof(float);
+};
+
+template <int S>
+__global__ void __launch_bounds__(kThreads) adj_ms_kernel(const float *__restrict__ sino, float *__restrict__ img,
+                                                          const float2 *__restrict__ trig, KGeom g, int ntx, int sub,
+                                                          int step, int nang, const float *__restrict__ base,
+                                                          float scale_out)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *accs = reinterpret_cast<float *>(smem_raw);
+    int *acci = reinterpret_cast<int *>(accs + S * kAdjMsN);
+    float *wmax = reinterpret_cast<float *>(acci + S * kAdjMsN);
+    const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
+    const int z0 = (int)blockIdx.z * S;
+    const size_t nprj = (size_t)g.pa * g.px, nimg = (size_t)g.nx * g.ny;
+    const int x0 = bx * kAdjMsT, y0 = by * kAdjMsT;  // owned texels [x0, x0+T) x [y0, y0+T)
+    for (int i = threadIdx.x; i < S * kAdjMsN; i += kThreads) {
+        accs[i] = 0.0f;
+        acci[i] = 0;
+    }
+    __syncthreads();
+    const float *sn = sino + (size_t)z0 * nprj;
+    // base texels whose footprint touches the tile
+    const float xlo = (float)(x0 - 1), xhi = (float)min(x0 + kAdjMsT, g.nx);
+    const float ylo = (float)(y0 - 1), yhi = (float)min(y0 + kAdjMsT, g.ny);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int D = g.depth;
+    for (int w0 = 0; w0 < nang; w0 += kAdjWarps) {
+        const bool active = w0 + warp < nang;
+        const int th = active ? sub + (w0 + warp) * step : 0;
+        float c = 1.0f, s = 0.0f;
+        int Xlo = 0, Xhi = -1;
+        if (active) {
+            const float2 cs = trig[th];
+            c = cs.x;
+            s = cs.y;
+            float pmin = 3.0e38f, pmax = -3.0e38f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float px_ = (q & 1) ? xhi + 2.0f : xlo - 2.0f;
+                const float py_ = (q & 2) ? yhi + 2.0f : ylo - 2.0f;
+                const float p = (px_ - g.hx) * c - (py_ - g.hy) * s + g.cx;
+                pmin = fminf(pmin, p);
+                pmax = fmaxf(pmax, p);
+            }
+            Xlo = max(0, (int)floorf(pmin) - 1);
+            Xhi = min(g.px - 1, (int)ceilf(pmax) + 1);
+        }
+        const float *row = sn + (size_t)th * g.px;
+        // each slice's largest |ray value| over the window (NaN and inf make it non-finite)
+        float m[S];
+#pragma unroll
+        for (int z = 0; z < S; ++z) m[z] = 0.0f;
+        for (int X = Xlo + lane; X <= Xhi; X += 32) {
+#pragma unroll
+            for (int z = 0; z < S; ++z) {
+                const float v = fabsf(__ldg(row + (size_t)z * nprj + X));
+                m[z] = (v == v && m[z] == m[z]) ? fmaxf(m[z], v) : __int_as_float(0x7fc00000);
+            }
+        }
+#pragma unroll
+        for (int z = 0; z < S; ++z) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float t = __shfl_xor_sync(0xffffffffu, m[z], o);
+                m[z] = (t == t && m[z] == m[z]) ? fmaxf(m[z], t) : __int_as_float(0x7fc00000);
+            }
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int z = 0; z < S; ++z) wmax[warp * S + z] = m[z];
+        }
+        __syncthreads();
+        float vmax[S], sc[S], inv[S];
+        unsigned fixed = 0;  // bit z: slice z's window takes the fixed-point path
+#pragma unroll
+        for (int z = 0; z < S; ++z) {
+            float vm = 0.0f;
+#pragma unroll
+            for (int k = 0; k < kAdjWarps; ++k) {
+                const float t = wmax[k * S + z];
+                vm = (t == t && vm == vm) ? fmaxf(vm, t) : __int_as_float(0x7fc00000);
+            }
+            vmax[z] = vm;
+            sc[z] = 0.0f;
+            inv[z] = 0.0f;
+            // false for NaN and inf, and for finite windows above 1e30: those scatter float atomics
+            if (vm < 1.0e30f && vm > 0.0f) {
+                int e;
+                frexpf(vm, &e);  // vmax < 2^e
+                e = max(e, -78);  // keep the scale <= 2^100 (a finite float)
+                sc[z] = ldexpf(1.0f, 22 - e);
+                inv[z] = ldexpf(1.0f, e - 22);
+                fixed |= 1u << z;
+            }
+        }
+        if (active) {
+            // the forward projector's lane mapping: 8 consecutive rays, 4 lanes per ray
+            const float inv_s = 1.0f / s, inv_c = 1.0f / c;
+            const int ray = lane / kLanesPerRay, ph = lane % kLanesPerRay, grp = lane & ~(kLanesPerRay - 1);
+            const bool bound_x = ph < 2, upper = (ph & 1) != 0;
+            for (int b0 = Xlo; b0 <= Xhi; b0 += kRaysPerWarp) {
+                const int X = b0 + ray;
+                const bool live = X <= Xhi;
+                float v[S];
+                bool any = false;
+#pragma unroll
+                for (int z = 0; z < S; ++z) {
+                    v[z] = live ? __ldg(row + (size_t)z * nprj + X) : 0.0f;
+                    any |= v[z] != 0.0f;
+                }
+                const float Xc = (float)X - g.cx;
+                const float ax = fmaf(Xc, c, g.hx);
+                const float ay = fmaf(Xc, -s, g.hy);
+                int lim = 0;
+                if (live) {
+                    const float a = bound_x ? ax : ay, sl = bound_x ? s : c, isl = bound_x ? inv_s : inv_c;
+                    const float lo = bound_x ? xlo : ylo, hi = bound_x ? xhi : yhi;
+                    if (sl != 0.0f) {
+                        const float bnd = ((sl > 0.0f) != upper) ? lo : hi;
+                        lim = first_true(bnd, a, sl, isl, g.hd, D);
+                    } else {
+                        lim = upper ? ((a >= lo && a < hi) ? D : 0) : 0;
+                    }
+                }
+                const int l0 = __shfl_sync(0xffffffffu, lim, grp + 0), l1 = __shfl_sync(0xffffffffu, lim, grp + 1);
+                const int l2 = __shfl_sync(0xffffffffu, lim, grp + 2), l3 = __shfl_sync(0xffffffffu, lim, grp + 3);
+                const int ya = max(l0, l2);
+                const int yb = (live && any) ? min(l1, l3) : ya;  // a ray zero in every slice adds nothing
+                float vs[S];
+                unsigned as_int = 0;  // bit z: |v| >= vmax * 2^-6 in a fixed-point window
+#pragma unroll
+                for (int z = 0; z < S; ++z) {
+                    vs[z] = v[z] * sc[z];
+                    if (((fixed >> z) & 1u) && fabsf(v[z]) >= vmax[z] * 0.015625f) as_int |= 1u << z;
+                }
+                for (int Y = ya + ph; Y < yb; Y += kLanesPerRay) {
+                    const float Yc = (float)Y - g.hd;
+                    const float x = fmaf(Yc, s, ax), y = fmaf(Yc, c, ay);
+                    const float fi = floorf(x), fj = floorf(y);
+                    const float fx = x - fi, fy = y - fj;
+                    const int col = (int)fi - (x0 - 1), rr = (int)fj - (y0 - 1);
+                    const float gx = 1.0f - fx, gy = 1.0f - fy;
+                    if (!XCT_IN(rr * kAdjMsP + col, 0, (kAdjMsR - 2) * kAdjMsP + kAdjMsR - 2, XCT_SITE_ADJ)) continue;
+                    const int o = rr * kAdjMsP + col;
+#pragma unroll
+                    for (int z = 0; z < S; ++z) {
+                        int *ai = acci + z * kAdjMsN + o;
+                        float *af = accs + z * kAdjMsN + o;
+                        if ((as_int >> z) & 1u) {
+                            // round(x) for |x| < 2^22: the low bits of x + 1.5*2^23
+                            const float p0 = vs[z] * gy, p1 = vs[z] * fy;
+                            atomicAdd(ai, __float_as_int(gx * p0 + kMagic) - 0x4B400000);
+                            atomicAdd(ai + 1, __float_as_int(fx * p0 + kMagic) - 0x4B400000);
+                            atomicAdd(ai + kAdjMsP, __float_as_int(gx * p1 + kMagic) - 0x4B400000);
+                            atomicAdd(ai + kAdjMsP + 1, __float_as_int(fx * p1 + kMagic) - 0x4B400000);
+                        } else if (v[z] != 0.0f) {
+                            atomicAdd(af, gx * gy * v[z]);
+                            atomicAdd(af + 1, fx * gy * v[z]);
+                            atomicAdd(af + kAdjMsP, gx * fy * v[z]);
+                            atomicAdd(af + kAdjMsP + 1, fx * fy * v[z]);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int z = 0; z < S; ++z) {
+            if ((fixed >> z) & 1u) {
+                for (int i = threadIdx.x; i < kAdjMsN; i += kThreads) {
+                    const int q = acci[z * kAdjMsN + i];
+                    if (q != 0) {
+                        accs[z * kAdjMsN + i] += (float)q * inv[z];
+                        acci[z * kAdjMsN + i] = 0;
+                    }
+                }
+            }
+        }
+        __syncthreads();  // the integers are clear and wmax may be rewritten
+    }
+    for (int z = 0; z < S; ++z) {
+        float *im = img + (size_t)(z0 + z) * nimg;
+        const float *bz = base ? base + (size_t)(z0 + z) * nimg : nullptr;
+        for (int i = threadIdx.x; i < kAdjMsT * kAdjMsT; i += kThreads) {
+            const int r = i / kAdjMsT, cc = i - r * kAdjMsT;
+            const int X = x0 + cc, Y = y0 + r;
+            if (X < g.nx && Y < g.ny) {
+                const float a = accs[z * kAdjMsN + (r + 1) * kAdjMsP + cc + 1];
+                const size_t o = (size_t)Y * g.nx + X;
+                im[o] = bz ? fmaf(scale_out, a, __ldg(bz + o)) : a;
+            }
+        }
+    }
+}
+
 // acc -> OSEM1 ratio (meas != nullptr) or raw projection, rows th = sub + k*step; clears acc.
 __global__ void fwd_finalize_kernel(double *__restrict__ acc, const float *__restrict__ meas,
                                     float *__restrict__ out, KGeom g, int sub, int step, int nrows)
@@ -1406,10 +1615,43 @@ int launch_adj_tiled(const KGeom &g, const float2 *trig, const float *sino, floa
     return launch_adj_subset(g, trig, sino, img, dN, 0, 1, g.pa, nullptr, 0.0f, st);
 }
 
+// Launch of adj_ms_kernel<S> over groups of S slices (its shared memory opted in once per
+// device).
+template <int S>
+static int launch_adj_ms(const KGeom &g, const float2 *trig, const float *sino, float *img, int groups, int sub,
+                         int step, int nang, const float *base, float scale, cudaStream_t st)
+{
+    static std::atomic<bool> done[64];
+    int dev = 0;
+    XCT_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return xct_fail(XCT_E_INVALID, "device index out of range");
+    if (!done[dev].load(std::memory_order_acquire)) {
+        XCT_CUDA_TRY(cudaFuncSetAttribute((const void *)adj_ms_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)AdjMs<S>::Smem));
+        done[dev].store(true, std::memory_order_release);
+    }
+    const int ntx = (g.nx + kAdjMsT - 1) / kAdjMsT, nty = (g.ny + kAdjMsT - 1) / kAdjMsT;
+    adj_ms_kernel<S><<<dim3(ntx * nty, 1, groups), kThreads, AdjMs<S>::Smem, st>>>(sino, img, trig, g, ntx, sub, step,
+                                                                                  nang, base, scale);
+    g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+    XCT_CUDA_TRY(cudaGetLastError());
+    return XCT_OK;
+}
+
 int launch_adj_subset(const KGeom &g, const float2 *trig, const float *sino, float *img, int dN, int sub, int step,
                       int nang, const float *base, float scale, cudaStream_t st)
 {
     if (dN <= 0) return XCT_OK;
+    // with the slice-interleaved kernels on, groups of slices share each sample's work
+    if (g.ms_chunk > 0 && dN >= kAdjMsSlices) {
+        const int groups = dN / kAdjMsSlices, ms = groups * kAdjMsSlices;
+        const int rc = launch_adj_ms<kAdjMsSlices>(g, trig, sino, img, groups, sub, step, nang, base, scale, st);
+        if (rc || ms == dN) return rc;
+        sino += (size_t)ms * g.pa * g.px;
+        img += (size_t)ms * g.nx * g.ny;
+        if (base) base += (size_t)ms * g.nx * g.ny;
+        dN -= ms;
+    }
     const long long big = (long long)((g.nx + kAdjT - 1) / kAdjT) * ((g.ny + kAdjT - 1) / kAdjT) * dN;
     if (big >= 3LL * device_sm_count()) {
         const int ntx = (g.nx + kAdjT - 1) / kAdjT, nty = (g.ny + kAdjT - 1) / kAdjT;

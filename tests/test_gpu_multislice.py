@@ -144,3 +144,52 @@ def test_multislice_backprojector_bit_identical(gpu_ctx, oracle_lib, case):
             want = O.osem2(imgs[z], ratio[z], ang, ss, sub, cx=cx, order=O.ORDER_GPU)
             assert np.array_equal(g[z], want), (sub, z, int(np.count_nonzero(g[z] != want)))
     plan.close()
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_multislice_adjoint_matches_per_slice_kernel(gpu_ctx, case):
+    """The exact adjoint over groups of slices (each sample's coordinates and weights shared
+    by the group) against the per-slice adjoint kernel: with every ray of a window within 2^6
+    of its largest the sums are fixed-point integers, so the two agree bit for bit."""
+    import xct
+    nx, ny, px, pa, ss, span, off, dN, chunk = CASES[case]
+    ang, _, cx = _case(CASES[case], 80 + case)
+    rng = np.random.default_rng(90 + case)
+    sino = torch.from_numpy(rng.uniform(0.5, 1.5, (dN, pa, px)).astype(np.float32)).cuda()
+    plan = xct.OSEMPlan(gpu_ctx, nx, ny, px, ang, ss, 1, center_bin=cx, max_batch=dN)
+    plan.set_multislice(0)
+    ref = torch.empty((dN, ny, nx), device="cuda")
+    plan.adj(sino, ref)
+    plan.set_multislice(chunk)
+    got = torch.empty((dN, ny, nx), device="cuda")
+    plan.adj(sino, got)
+    torch.cuda.synchronize()
+    g, r = got.cpu().numpy(), ref.cpu().numpy()
+    assert np.array_equal(g, r), int(np.count_nonzero(g != r))
+    plan.close()
+
+
+def test_multislice_adjoint_gradient_step(gpu_ctx):
+    """XCT_FISTA_ADJOINT (x + coef * A^T r in the adjoint's epilogue) on five slices: groups
+    of four through the multi-slice adjoint and one through the per-slice kernel give the
+    per-slice result (residuals mix magnitudes, so float-atomic rays allow rounding order)."""
+    import xct
+    from xct import phantom as P
+    n, px, pa, ss, it, dN = 96, 96, 60, 6, 2, 5
+    ang = P.uniform_angles(pa)
+    prm = P.ellipsoid_params(n, dN, count=6, seed=97)
+    imgs = np.stack([P.ellipsoid_slice(prm, z, n, n) for z in range(dN)]).astype(np.float32)
+    plan = xct.OSEMPlan(gpu_ctx, n, n, px, ang, ss, it, max_batch=dN)
+    plan.set_lipschitz(plan.power_iteration(trials=10))
+    meas = torch.empty((dN, pa, px), device="cuda")
+    plan.fwd(torch.from_numpy(imgs).cuda(), meas)
+    out = {}
+    for ms in (0, 128):
+        plan.set_multislice(ms)
+        x = torch.zeros((dN, n, n), device="cuda")
+        plan.fista_run_device(meas, x, flags=xct.FISTA_ADJOINT | xct.FISTA_UPDATE_X)
+        torch.cuda.synchronize()
+        out[ms] = x.cpu().numpy().astype(np.float64)
+    assert np.all(np.isfinite(out[128]))
+    assert _rel(out[128], out[0]) <= 1e-6
+    plan.close()
