@@ -181,10 +181,11 @@ void xct_plan_default_tuning(xct_plan *p)
 {
     TuneChoice c;
     const std::string key = xct_tune_key(p->ctx->name, p->g.nx, p->g.ny, p->g.px, p->g.pa, p->g.ss, p->g.max_batch);
-    if (!xct_tune_lookup(key, xct_tune_env_path(), c)) {
+    if (!xct_tune_lookup(key, xct_tune_env_path(), c))
         c = xct_tune_default(p->ctx->sm_count, [&](int T, int ch) { return plan_ctas(p, p->g.max_batch, T, ch); });
-        c.ms_chunk = plan_default_ms_chunk(p);
-    }
+    // the cache holds the per-slice kernel's tiles; the slice-interleaved kernels' switch
+    // follows the plan's shape
+    c.ms_chunk = plan_default_ms_chunk(p);
     p->kg.fwd_T = c.T;
     p->kg.fwd_chunk = c.chunk;
     p->kg.ms_chunk = c.ms_chunk;

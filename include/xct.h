@@ -402,19 +402,26 @@ int xct_plan_set_tuning(xct_plan *plan, int fwd_tile, int ang_chunk);
 int xct_batch_plan_autotune(xct_batch_plan *plan, const char *cache_path, int flags, void *stream);
 int xct_batch_plan_tuning(xct_batch_plan *plan, int *fwd_tile, int *ang_chunk);
 
-/* ---- slice-interleaved forward projector -------------------------------------------------
- * No counterpart in the reference (its OSEM1 work-items each sum one ray of one slice).  The
- * slices of one OS-EM call share their geometry, so a plan can forward-project them in
- * groups of XCT_MULTISLICE_SLICES (eight): a CTA stages one tile of the eight slices (one
- * 128-byte line of bilinear coefficients per texel), each quarter-warp walks two rays as one
- * stream of samples, and each lane reads the eight slices of its sample in a rotated order
- * (no shared-memory bank conflict; a sample's coordinates are found once for all eight).  With
- * it on, a call's slices go in groups of eight through it and the rest through the per-slice
- * tiled kernel, and a call that runs as two halves cuts them at a multiple of eight.  The
- * value is the number of subset angles one CTA serves (1..128); 0 turns it off.  Plans start
- * with the cached or autotuned choice, else on (128) when max_batch >= 8 and the tiles of one
- * group give at least two CTAs per SM.  Results agree with the per-slice kernel to float
- * rounding of the partial ray sums. */
+/* ---- slice-interleaved kernels ---------------------------------------------------------
+ * No counterpart in the reference (its OSEM1/OSEM2 work-items each serve one slice).  The
+ * slices of one call share their geometry, so a plan can serve them in groups:
+ *  - forward projection (OSEM1, xct_fwd) in groups of XCT_MULTISLICE_SLICES (eight): a CTA
+ *    stages one tile of the eight slices (one 128-byte line of bilinear coefficients per
+ *    texel), a quarter-warp walks two rays, and each lane reads the eight slices of its sample
+ *    in a rotated order (no shared-memory bank conflict; a sample's coordinates are found once
+ *    for all eight).  Results agree with the per-slice kernel to float rounding of the partial
+ *    ray sums;
+ *  - backprojection + update (OSEM2) in groups of eight: one bin expression per eight gathers;
+ *    bit-identical to the per-slice kernel;
+ *  - the exact adjoint (xct_adj and the FISTA adjoint step) in groups of four: each sample's
+ *    coordinates and weights serve the four slices; identical to the per-slice kernel where
+ *    its fixed-point path applies, else to float rounding.
+ * With it on, a call's slices go in groups through these kernels and the rest through the
+ * per-slice ones, and a call that runs as two halves cuts them at a multiple of eight.  The
+ * value is the number of subset angles one forward CTA serves (1..128); 0 turns all three
+ * off.  Plans start on (128) when max_batch >= 8 and the forward tiles of one group give at
+ * least two CTAs per SM, else off (the tile cache and the autotuner leave this switch
+ * alone). */
 #define XCT_MULTISLICE_SLICES 8
 int xct_plan_multislice(xct_plan *plan, int *ang_chunk);
 int xct_plan_set_multislice(xct_plan *plan, int ang_chunk);
