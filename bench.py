@@ -740,6 +740,27 @@ def profile_case():
     print(json.dumps({"profile_case": "ok", "mean": float(x.mean())}))
 
 
+def profile_case_operators(n=8):
+    """Small case for profilers, the operator pair: the forward projection and the exact
+    adjoint of n slices of the workload over all 1500 angles, each once (the slice-interleaved
+    forward projector and the gather adjoint for n = 8).  ~0.3 GB on the device."""
+    import torch
+    import xct
+    from xct import phantom
+    ang = phantom.uniform_angles(PA)
+    ctx = xct.Context(0)
+    plan = xct.OSEMPlan(ctx, NX, NY, PX, ang, SS, 1, max_batch=n)
+    pars = phantom.ellipsoid_params(NX, NSLICES, 30, 2, mu=(0.005, 0.1))
+    img = torch.stack([phantom.ellipsoid_slice(pars, z, NX, NY, torch_device="cuda") for z in range(n)]).contiguous()
+    sino = torch.empty((n, PA, PX), device="cuda")
+    plan.fwd(img, sino)
+    back = torch.empty_like(img)
+    plan.adj(sino, back)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "operators", "n": n, "multislice": plan.multislice(),
+                      "mean": float(back.mean())}))
+
+
 def profile_case_slices(n=8):
     """Small case for profilers, the slice-interleaved forward projector: n slices of the
     workload (sinograms made with the per-slice forward projector, one launch per 128 angles),
@@ -770,10 +791,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", nargs="?", const="osem", choices=["osem", "slices", "next"],
+    ap.add_argument("--profile-case", nargs="?", const="osem", choices=["osem", "slices", "next", "operators"],
                     help="run a small profiling case and exit: osem (one slice, one OS-EM iteration), slices "
-                         "(eight slices, one OS-EM iteration, slice-interleaved forward projector) or next "
-                         "(the components either side of the path, each once)")
+                         "(eight slices, one OS-EM iteration, slice-interleaved kernels), next (the components "
+                         "either side of the path, each once) or operators (forward projection and exact adjoint "
+                         "of eight slices)")
     args = ap.parse_args()
     if args.profile_case == "osem":
         profile_case()
@@ -783,6 +805,9 @@ def main():
         return
     if args.profile_case == "next":
         profile_case_next()
+        return
+    if args.profile_case == "operators":
+        profile_case_operators()
         return
 
     rank = _env_int("RANK", 0)

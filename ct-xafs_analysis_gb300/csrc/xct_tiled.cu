@@ -118,6 +118,25 @@ __device__ __forceinline__ int first_true(float b, float a, float sl, float inv_
     return first_true_search(b, a, sl, hd, D);
 }
 
+// Asynchronous global -> shared copies (zero-filled past src_bytes) and their wait.
+__device__ __forceinline__ void cp_async16(unsigned dst, const void *src, unsigned src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async4(unsigned dst, const void *src, unsigned src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int kOff>
+__device__ __forceinline__ float lds_f1_at(unsigned addr)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1+%2];" : "=f"(v) : "r"(addr), "n"(kOff));
+    return v;
+}
+
 __device__ __forceinline__ void lds_f2(unsigned addr, float &a, float &b)
 {
     asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(a), "=f"(b) : "r"(addr));
@@ -964,6 +983,212 @@ __global__ void __launch_bounds__(kThreads) adj_ms_kernel(const float *__restric
     }
 }
 
+// The exact adjoint over eight slices as a gather, without atomics.  Every sample (ray X,
+// index Y) of the forward projector has one base texel (floor of its coordinates); its value
+// v goes to that base texel's four footprint texels with the weights gx gy, fx gy, gx fy,
+// fx fy.  A thread owns one base texel (i, j) and keeps four accumulators per slice -- the
+// parts its samples give to (i, j), (i+1, j), (i, j+1), (i+1, j+1) -- so each sample is
+// handled by exactly one thread.  Per angle the thread finds its samples: a half-open unit
+// square holds at most two points of the rotated unit sample lattice, which lie on the at
+// most two rays whose lattice coordinate is within 0.717 of the square's centre, each at
+// most two sample indices within 0.717 of the centre's projection on the ray; each of those
+// four candidates is evaluated with the forward projector's own arithmetic (fma
+// coordinates, round-down floor) and kept when its base texel is (i, j), the ray is on the
+// detector and the index within [0, D).  A CTA of 512 threads owns 32 x 16 base texels and
+// writes the 31 x 15 texels whose four base texels it holds, texel (i, j) = A00(i, j) +
+// A10(i-1, j) + A01(i, j-1) + A11(i-1, j-1), after staging the four parts in shared memory.
+// The rays' values of 16 angles at a time are staged per slice by asynchronous copies.
+// Float sums in angle order: deterministic, and no fixed-point rounding.
+constexpr int kAdjGBX = 32, kAdjGBY = 16;            // base texels per CTA
+constexpr int kAdjGThreads = kAdjGBX * kAdjGBY;      // one per base texel
+constexpr int kAdjGW = 44;                           // staged rays per angle
+constexpr int kAdjGChunk = 16;                       // angles per staging pass
+template <int S>
+struct AdjG {
+    // window: [slice pair][angle][ray] of float2; parts: [corner][slice][thread]
+    static constexpr unsigned PairBytes = (unsigned)(kAdjGChunk * kAdjGW * 8);
+    static constexpr size_t WinBytes = (size_t)(S / 2) * PairBytes;
+    static constexpr size_t CombBytes = (size_t)4 * S * kAdjGThreads * 4;
+    static constexpr size_t Smem = (WinBytes > CombBytes ? WinBytes : CombBytes) + kAdjGChunk * 16;
+};
+
+__device__ __forceinline__ f2x lds_f2x(unsigned addr)
+{
+    f2x v;
+    asm volatile("ld.shared.b64 %0, [%1];" : "=l"(v) : "r"(addr));
+    return v;
+}
+
+// S (even) slices per CTA; the library launches S = 8.
+template <int S>
+__global__ void __launch_bounds__(kAdjGThreads, 2) adj_gather_kernel(const float *__restrict__ sino,
+                                                                     float *__restrict__ img,
+                                                                     const float2 *__restrict__ trig, KGeom g,
+                                                                     int ntx, int sub, int step, int nang,
+                                                                     const float *__restrict__ base, float scale_out)
+{
+    constexpr int P = S / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *part = reinterpret_cast<float *>(smem_raw);  // the window, later the parts
+    float2 *scs = reinterpret_cast<float2 *>(smem_raw + AdjG<S>::Smem - kAdjGChunk * 16);
+    int *sxw = reinterpret_cast<int *>(scs + kAdjGChunk);
+    const int tx = threadIdx.x % kAdjGBX, ty = threadIdx.x / kAdjGBX;
+    const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
+    const int z0 = (int)blockIdx.z * S;
+    const size_t nprj = (size_t)g.pa * g.px, nimg = (size_t)g.nx * g.ny;
+    const float *sz = sino + (size_t)z0 * nprj;
+    // base texels [bi0, bi0 + 32) x [bj0, bj0 + 16); output texels from bi0 + 1, bj0 + 1
+    const int bi0 = bx * (kAdjGBX - 1) - 1, bj0 = by * (kAdjGBY - 1) - 1;
+    const int i = bi0 + tx, j = bj0 + ty;
+    const int ibits = i + XCT_FLOOR_BIAS, jbits = j + XCT_FLOOR_BIAS;
+    const float ci = (float)i + 0.5f, cj = (float)j + 0.5f;  // the square's centre
+    const float di = ci - g.hx, dj = cj - g.hy;
+    const int D = g.depth;
+    const unsigned wbase = (unsigned)__cvta_generic_to_shared(part);
+    const f2x MM = f2_pack(kMagic, kMagic), one2 = f2_pack(1.0f, 1.0f);
+    const f2x hxy = f2_pack(g.hx, g.hy), cij = f2_pack(ci, cj);
+    f2x acc[4][P];  // [corner 00, 10, 01, 11][slice pair]
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int h = 0; h < P; ++h) acc[q][h] = 0ull;
+
+    for (int k0 = 0; k0 < nang; k0 += kAdjGChunk) {
+        const int kn = min(kAdjGChunk, nang - k0);
+        __syncthreads();  // the previous chunk's reads are done
+        for (int k = threadIdx.x; k < kn; k += kAdjGThreads) {
+            const float2 cs = trig[sub + (k0 + k) * step];
+            scs[k] = cs;
+            // rays whose lattice coordinate meets the block's base squares
+            float umin = 3.0e38f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float px_ = (float)(bi0 + ((q & 1) ? kAdjGBX : 0)) - g.hx;
+                const float py_ = (float)(bj0 + ((q & 2) ? kAdjGBY : 0)) - g.hy;
+                umin = fminf(umin, px_ * cs.x - py_ * cs.y + g.cx);
+            }
+            sxw[k] = (int)floorf(umin) - 2;
+        }
+        __syncthreads();
+        // window (pair p, angle k, ray sxw[k] + r) = (slice 2p, slice 2p + 1), 0 off the detector
+        for (int e = threadIdx.x; e < kn * S * kAdjGW; e += kAdjGThreads) {
+            const int r = e % kAdjGW, t2 = e / kAdjGW;
+            const int z = t2 % S, k = t2 / S;
+            const int X = sxw[k] + r;
+            const float *row = sz + (size_t)z * nprj + (size_t)(sub + (k0 + k) * step) * g.px;
+            const bool in = (unsigned)X < (unsigned)g.px;
+            const unsigned dst = wbase + (unsigned)(z >> 1) * AdjG<S>::PairBytes + 8u * (unsigned)(k * kAdjGW + r) +
+                                 4u * (unsigned)(z & 1);
+            cp_async4(dst, in ? (const void *)(row + X) : (const void *)row, in ? 4u : 0u);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        for (int k = 0; k < kn; ++k) {
+            const float c = scs[k].x, s = scs[k].y;
+            const f2x cs2 = f2_pack(c, -s), sc2 = f2_pack(s, c);
+            const unsigned wk = wbase + 8u * (unsigned)(k * kAdjGW - sxw[k]);
+            // the candidates: rays Xa, Xa + 1; on each, indices Ya, Ya + 1
+            const float u0 = fmaf(di, c, fmaf(-dj, s, g.cx));
+            const int Xa = (xct_floor_bits(u0 - 0.717f) - XCT_FLOOR_BIAS) + 1;
+            f2x cxy[4];
+            int cX[4];
+            unsigned valid = 0;
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                const int X = Xa + a;
+                const float Xc = (float)X - g.cx;
+                const f2x axy = f2_fma(f2_pack(Xc, Xc), cs2, hxy);  // (ax, ay) as the forward
+                float dx_, dy_;
+                f2_unpack(f2_sub(cij, axy), dx_, dy_);
+                const float yc0 = fmaf(dx_, s, dy_ * c);
+                const int Ya = (xct_floor_bits(yc0 + g.hd - 0.717f) - XCT_FLOOR_BIAS) + 1;
+                const bool xin = (unsigned)X < (unsigned)g.px;
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    const int Y = Ya + b;
+                    const float Yc = (float)Y - g.hd;
+                    const f2x xy = f2_fma(f2_pack(Yc, Yc), sc2, axy);  // (x, y) as the forward
+                    int xb, yb;
+                    f2_unpack_bits(f2_add_rd(xy, MM), xb, yb);
+                    const int q = 2 * a + b;
+                    cxy[q] = xy;
+                    cX[q] = X;
+                    if (xb == ibits && yb == jbits && xin && (unsigned)Y < (unsigned)D) valid |= 1u << q;
+                }
+            }
+            while (valid) {
+                const int q = __ffs(valid) - 1;
+                valid &= valid - 1;
+                const f2x xy = q == 0 ? cxy[0] : q == 1 ? cxy[1] : q == 2 ? cxy[2] : cxy[3];
+                const int X = q == 0 ? cX[0] : q == 1 ? cX[1] : q == 2 ? cX[2] : cX[3];
+                // fractions and the four bilinear weights (gx gy, fx gy, gx fy, fx fy)
+                const f2x fr = f2_sub(xy, f2_pack(__int_as_float(ibits) - kMagic, __int_as_float(jbits) - kMagic));
+                const f2x gr = f2_sub(one2, fr);
+                float fx, fy, gx, gy;
+                f2_unpack(fr, fx, fy);
+                f2_unpack(gr, gx, gy);
+                const float w[4] = {gx * gy, fx * gy, gx * fy, fx * fy};
+                const unsigned ad = wk + 8u * (unsigned)X;
+                if (!XCT_IN(ad, wbase, wbase + AdjG<S>::WinBytes - 8, XCT_SITE_ADJ)) continue;
+                f2x v[P];
+#pragma unroll
+                for (int h = 0; h < P; ++h) v[h] = lds_f2x(ad + (unsigned)h * AdjG<S>::PairBytes);
+#pragma unroll
+                for (int cq = 0; cq < 4; ++cq) {
+                    const f2x ww = f2_pack(w[cq], w[cq]);
+#pragma unroll
+                    for (int h = 0; h < P; ++h) acc[cq][h] = f2_fma(ww, v[h], acc[cq][h]);
+                }
+            }
+        }
+    }
+    // the parts: part[corner][slice][thread]
+    __syncthreads();
+#pragma unroll
+    for (int cq = 0; cq < 4; ++cq)
+#pragma unroll
+        for (int h = 0; h < P; ++h) {
+            float a0, a1;
+            f2_unpack(acc[cq][h], a0, a1);
+            part[(cq * S + 2 * h) * kAdjGThreads + threadIdx.x] = a0;
+            part[(cq * S + 2 * h + 1) * kAdjGThreads + threadIdx.x] = a1;
+        }
+    __syncthreads();
+    if (tx == 0 || ty == 0 || i >= g.nx || j >= g.ny) return;
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int z = 0; z < S; ++z) {
+        const float a = part[(0 * S + z) * kAdjGThreads + t] + part[(1 * S + z) * kAdjGThreads + t - 1] +
+                        part[(2 * S + z) * kAdjGThreads + t - kAdjGBX] +
+                        part[(3 * S + z) * kAdjGThreads + t - kAdjGBX - 1];
+        const size_t o = (size_t)(z0 + z) * nimg + (size_t)j * g.nx + i;
+        img[o] = base ? fmaf(scale_out, a, __ldg(base + o)) : a;
+    }
+}
+
+// Launch of adj_gather_kernel<S> over `groups` groups of S slices (its shared memory opted in
+// once per device).
+template <int S>
+static int launch_adj_gather(const KGeom &g, const float2 *trig, const float *sino, float *img, int groups, int sub,
+                             int step, int nang, const float *base, float scale, cudaStream_t st)
+{
+    static std::atomic<bool> done[64];
+    int dev = 0;
+    XCT_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return xct_fail(XCT_E_INVALID, "device index out of range");
+    if (!done[dev].load(std::memory_order_acquire)) {
+        XCT_CUDA_TRY(cudaFuncSetAttribute((const void *)adj_gather_kernel<S>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AdjG<S>::Smem));
+        done[dev].store(true, std::memory_order_release);
+    }
+    const int ntx = (g.nx + kAdjGBX - 2) / (kAdjGBX - 1), nty = (g.ny + kAdjGBY - 2) / (kAdjGBY - 1);
+    adj_gather_kernel<S><<<dim3(ntx * nty, 1, groups), kAdjGThreads, AdjG<S>::Smem, st>>>(sino, img, trig, g, ntx, sub,
+                                                                                         step, nang, base, scale);
+    g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+    XCT_CUDA_TRY(cudaGetLastError());
+    return XCT_OK;
+}
+
 // acc -> OSEM1 ratio (meas != nullptr) or raw projection, rows th = sub + k*step; clears acc.
 __global__ void fwd_finalize_kernel(double *__restrict__ acc, const float *__restrict__ meas,
                                     float *__restrict__ out, KGeom g, int sub, int step, int nrows)
@@ -1172,24 +1397,6 @@ struct BpMsShared {
     int slo[kBpMsChunk];                         // first staged bin (a multiple of 4)
     unsigned soff[kBpMsChunk];                   // byte address of slice 0's entry (bits - BIAS - lo)
 };
-
-__device__ __forceinline__ void cp_async16(unsigned dst, const void *src, unsigned src_bytes)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async4(unsigned dst, const void *src, unsigned src_bytes)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-template <int kOff>
-__device__ __forceinline__ float lds_f1_at(unsigned addr)
-{
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1+%2];" : "=f"(v) : "r"(addr), "n"(kOff));
-    return v;
-}
 
 // grid: (ntx*nty tiles of 32 x 32, 1, dN / 8 slice groups).  vec: 16-byte staging copies
 // (px a multiple of 4 and a 16-byte aligned ratio array).
@@ -1642,7 +1849,23 @@ int launch_adj_subset(const KGeom &g, const float2 *trig, const float *sino, flo
                       int nang, const float *base, float scale, cudaStream_t st)
 {
     if (dN <= 0) return XCT_OK;
-    // with the slice-interleaved kernels on, groups of slices share each sample's work
+    // with the slice-interleaved kernels on, groups of eight slices take the gather form
+    // (its candidate search is shared by the group; for fewer slices the scatter forms
+    // cost less), then groups of four the scatter form with shared sample work
+    if (g.ms_chunk > 0 && dN >= 8) {
+        const size_t np = (size_t)g.pa * g.px, ni = (size_t)g.nx * g.ny;
+        int rc = XCT_OK;
+        auto advance = [&](int n) {
+            sino += n * np;
+            img += n * ni;
+            if (base) base += n * ni;
+            dN -= n;
+        };
+        const int groups = dN / 8;
+        if ((rc = launch_adj_gather<8>(g, trig, sino, img, groups, sub, step, nang, base, scale, st))) return rc;
+        advance(groups * 8);
+        if (dN == 0) return XCT_OK;
+    }
     if (g.ms_chunk > 0 && dN >= kAdjMsSlices) {
         const int groups = dN / kAdjMsSlices, ms = groups * kAdjMsSlices;
         const int rc = launch_adj_ms<kAdjMsSlices>(g, trig, sino, img, groups, sub, step, nang, base, scale, st);
