@@ -1019,9 +1019,9 @@ __device__ __forceinline__ f2x lds_f2x(unsigned addr)
     return v;
 }
 
-// S (even) slices per CTA; the library launches S = 8.
+// S (even) slices per CTA; the library launches S = 8 and S = 10 (one CTA per SM).
 template <int S>
-__global__ void __launch_bounds__(kAdjGThreads, 2) adj_gather_kernel(const float *__restrict__ sino,
+__global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kernel(const float *__restrict__ sino,
                                                                      float *__restrict__ img,
                                                                      const float2 *__restrict__ trig, KGeom g,
                                                                      int ntx, int sub, int step, int nang,
@@ -1103,10 +1103,12 @@ __global__ void __launch_bounds__(kAdjGThreads, 2) adj_gather_kernel(const float
                 const float yc0 = fmaf(dx_, s, dy_ * c);
                 const int Ya = (xct_floor_bits(yc0 + g.hd - 0.717f) - XCT_FLOOR_BIAS) + 1;
                 const bool xin = (unsigned)X < (unsigned)g.px;
+                // Y - hd is exact (hd is a multiple of 0.5), so the second index is the first + 1
+                const float Yc0 = (float)Ya - g.hd;
 #pragma unroll
                 for (int b = 0; b < 2; ++b) {
                     const int Y = Ya + b;
-                    const float Yc = (float)Y - g.hd;
+                    const float Yc = Yc0 + (float)b;
                     const f2x xy = f2_fma(f2_pack(Yc, Yc), sc2, axy);  // (x, y) as the forward
                     int xb, yb;
                     f2_unpack_bits(f2_add_rd(xy, MM), xb, yb);
@@ -1849,9 +1851,10 @@ int launch_adj_subset(const KGeom &g, const float2 *trig, const float *sino, flo
                       int nang, const float *base, float scale, cudaStream_t st)
 {
     if (dN <= 0) return XCT_OK;
-    // with the slice-interleaved kernels on, groups of eight slices take the gather form
-    // (its candidate search is shared by the group; for fewer slices the scatter forms
-    // cost less), then groups of four the scatter form with shared sample work
+    // with the slice-interleaved kernels on, groups of eight or ten slices take the gather
+    // form (its candidate search is shared by the group; for fewer slices the scatter forms
+    // cost less) -- as many groups of ten as leave a multiple of eight, then groups of eight
+    // -- and groups of four the scatter form with shared sample work
     if (g.ms_chunk > 0 && dN >= 8) {
         const size_t np = (size_t)g.pa * g.px, ni = (size_t)g.nx * g.ny;
         int rc = XCT_OK;
@@ -1861,9 +1864,18 @@ int launch_adj_subset(const KGeom &g, const float2 *trig, const float *sino, flo
             if (base) base += n * ni;
             dN -= n;
         };
+        int tens = 0;
+        while (10 * tens <= dN && (dN - 10 * tens) % 8 != 0) ++tens;
+        if (10 * tens > dN) tens = 0;
+        if (tens > 0) {
+            if ((rc = launch_adj_gather<10>(g, trig, sino, img, tens, sub, step, nang, base, scale, st))) return rc;
+            advance(tens * 10);
+        }
         const int groups = dN / 8;
-        if ((rc = launch_adj_gather<8>(g, trig, sino, img, groups, sub, step, nang, base, scale, st))) return rc;
-        advance(groups * 8);
+        if (groups > 0) {
+            if ((rc = launch_adj_gather<8>(g, trig, sino, img, groups, sub, step, nang, base, scale, st))) return rc;
+            advance(groups * 8);
+        }
         if (dN == 0) return XCT_OK;
     }
     if (g.ms_chunk > 0 && dN >= kAdjMsSlices) {
