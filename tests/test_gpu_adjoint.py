@@ -202,3 +202,56 @@ def test_adjoint_is_deterministic(gpu_ctx):
     torch.cuda.synchronize()
     assert torch.equal(a, b)
     plan.close()
+
+
+def test_unrolled_reconstruction_at_operator_size(gpu_ctx, oracle_lib):
+    """The differentiable pair at the operator workload's size (1024^2, 720 angles, 1024
+    bins): a 50-step unrolled gradient reconstruction, checkpointed every iteration and not,
+    gives the same gradients (to the rounding of the adjoint's float-atomic rays) while the
+    checkpointed graph keeps less device memory; and the reference's own gradient step at that
+    size -- one FISTA_execution iteration of one subset (AART1 residual, FISTAbackProjection,
+    ISTA3D; GPU.cpp:1755-1924) -- matches the oracle's restatement of FISTA.cl/AART.cl."""
+    import xct
+    import xct.autograd as xa
+    from xct import phantom as P
+    O = oracle_lib
+    n, px, pa, iters = 1024, 1024, 720, 50
+    ang = P.uniform_angles(pa)
+    plan = xct.OSEMPlan(gpu_ctx, n, n, px, ang, 1, 1, max_batch=1)
+    truth_np = P.rasterize_ellipses(P.ellipse_params(n, 8, 11, axes=(20, 240), mu=(0.001, 0.01)), n, n)
+    truth = torch.from_numpy(truth_np).cuda().reshape(1, n, n)
+    y = torch.empty((1, pa, px), device="cuda")
+    plan.fwd(truth, y)
+    step = 1.0 / (pa * n * 1.5)
+    grads, peaks = [], []
+    for ckpt in (True, False):
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
+        base = torch.cuda.memory_allocated()
+        st = torch.tensor(step, device="cuda", requires_grad=True)
+        yy = y.clone().requires_grad_(True)
+        x = xa.unrolled_gradient_descent(torch.zeros((1, n, n), device="cuda"), yy, plan, st, iters,
+                                         checkpoint_each=ckpt)
+        loss = ((x - truth) ** 2).sum()
+        loss.backward()
+        torch.cuda.synchronize()
+        peaks.append(torch.cuda.max_memory_allocated() - base)
+        grads.append((float(st.grad), yy.grad.clone()))
+        del x, loss, yy, st
+    (g1, gy1), (g2, gy2) = grads
+    assert np.isfinite(g1) and abs(g1 - g2) <= 1e-3 * abs(g2)
+    assert float((gy1 - gy2).norm() / gy2.norm()) <= 1e-3
+    # checkpointed: one iterate per step (4 MB) instead of the iterate, its residual
+    # projection and the clamp's mask (measured 238 MB against 443 MB)
+    assert peaks[0] < 0.65 * peaks[1], peaks
+    # the reference gradient step (FISTAbackProjection, floor rule) against the oracle
+    L = plan.power_iteration(trials=10)
+    meas = y.cpu().numpy()
+    x = torch.zeros((1, n, n), device="cuda")
+    plan.fista_run_device(y, x, it=1)
+    torch.cuda.synchronize()
+    want = O.fista_run(np.zeros((1, n, n), np.float32), meas, ang, 1, 1, L)
+    got = x.cpu().numpy().astype(np.float64)
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel <= 1e-4, rel
+    plan.close()
