@@ -377,7 +377,7 @@ extern "C" int xct_batch_run(xct_batch_plan *p, const float *const *d_sino, floa
     // three per OS-EM step (the first step has none with compressed sensing), the
     // correction, and with compressed sensing the setup copy plus two per step
     const long long steps = (long long)p->it * p->ss, cs = p->stacks.empty() ? 0 : 1;
-    g_xct_launches.fetch_add(3 * (steps - cs) + (p->any_corr ? 1 : 0) + cs * (1 + 2 * steps),
+    g_xct_launches.fetch_add(3 * (steps - cs) + (p->any_corr ? (p->n + 65534) / 65535 : 0) + cs * (1 + 2 * steps),
                              std::memory_order_relaxed);
     return XCT_OK;
 }

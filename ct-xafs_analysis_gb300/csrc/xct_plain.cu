@@ -5,6 +5,8 @@
 // These are the "plain path" the tiled kernels are measured against, and the fallback
 // for shapes the tiled kernels do not take.  They read the image straight from global
 // memory through the read-only cache.
+#include <algorithm>
+
 #include "xct_device.cuh"
 
 namespace {
@@ -127,7 +129,7 @@ __global__ void sino_correction_kernel(const float *__restrict__ src, float *__r
 // The same for every item of a batch with a correction: block (x, th, item).
 __global__ void sino_correction_batched_kernel(const XctItemDev *__restrict__ items)
 {
-    const XctItemDev &it = items[blockIdx.z];
+    const XctItemDev &it = items[blockIdx.z];  // items: this launch's first item
     const int X = blockIdx.x * blockDim.x + threadIdx.x;
     const int th = blockIdx.y;
     if (it.corr_mode <= 0 || X >= it.g.px || th >= it.g.pa) return;
@@ -181,11 +183,14 @@ int launch_sino_correction(const KGeom &g, const float *src, float *dst, const f
     return XCT_OK;
 }
 
+// One launch per 65535 items (the grid's z limit); captured, so counted per replay.
 int launch_sino_correction_batched(const XctItemDev *items, int n, int max_px, int max_pa, cudaStream_t st)
 {
-    if (n <= 0) return XCT_OK;
-    dim3 grid((max_px + 127) / 128, max_pa, n);
-    sino_correction_batched_kernel<<<grid, 128, 0, st>>>(items);  // captured: counted per replay
-    XCT_CUDA_TRY(cudaGetLastError());
+    if (max_pa > 65535) return xct_fail(XCT_E_UNSUPPORTED, "sinogram correction in a batch: more than 65535 angles");
+    for (int first = 0; first < n; first += 65535) {
+        dim3 grid((max_px + 127) / 128, max_pa, std::min(65535, n - first));
+        sino_correction_batched_kernel<<<grid, 128, 0, st>>>(items + first);
+        XCT_CUDA_TRY(cudaGetLastError());
+    }
     return XCT_OK;
 }
