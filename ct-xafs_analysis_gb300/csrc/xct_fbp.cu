@@ -29,6 +29,7 @@
 
 #include <algorithm>
 
+#include "xct_async.cuh"
 #include "xct_check.cuh"
 #include "xct_device.cuh"
 #include "xct_f32x2.cuh"
@@ -359,6 +360,177 @@ __global__ void __launch_bounds__(512 / R, R == 4 ? 6 : 4) fbp_bp_kernel(const f
     }
 }
 
+// ---------------------------------------- FBP backprojection, eight slices per tile
+// For the slices of one call (one geometry) a (pixel, angle) pair reads the same two bins in
+// all eight slices of a group, so the bin coordinate, floor and fraction are found once for
+// eight lerps.  A CTA of 256 threads owns a 32 x 32 pixel tile of eight slices and stages,
+// per angle and pair of slices, the window of the tile's bins (< 49 with the lerp's second
+// bin, bounded exactly by the tile corners as in fbp_bp_kernel, its start rounded down to a
+// multiple of 4) as (t_z, t_z+1) pairs by asynchronous copies, 24 angles at a time.  A
+// thread takes 4 pixels of one row (8 apart); per pixel and angle: the literal expression of
+// fbp_bp_kernel for u, floor and fraction, two 8-byte loads per slice pair (bins i and
+// i + 1), the products in scalar and their sum and the accumulation packed over the slice
+// pair -- each slice's sum is fbp_bp_kernel's bit for bit.  The epilogue (field-of-view mask,
+// 1/(2 pa), the slice minimum for the base-up) is fbp_bp_kernel's.
+constexpr int kFbpMsT = 32, kFbpMsThreads = 256, kFbpMsW = 52, kFbpMsChunk = 24, kFbpMsPix = 4, kFbpMsSlices = 8;
+constexpr unsigned kFbpMsPairBytes = (unsigned)(kFbpMsChunk * kFbpMsW * 8);  // one slice pair's windows
+
+struct FbpMsShared {
+    float2 win[(kFbpMsSlices / 2) * kFbpMsChunk * kFbpMsW];  // [pair][angle][bin]: (t_z, t_z+1)
+    float2 scs[kFbpMsChunk];
+    int slo[kFbpMsChunk];
+    unsigned soff[kFbpMsChunk];  // shared address of angle k's entry for floor bits fb: soff[k] + 8*fb
+    float red[kFbpMsThreads / 32][kFbpMsSlices];
+};
+
+// grid: (ntx * nty tiles of 32 x 32, 1, dN / 8 slice groups).
+__global__ void __launch_bounds__(kFbpMsThreads) fbp_bp_ms_kernel(const float *__restrict__ fprj,
+                                                                  float *__restrict__ img,
+                                                                  const float2 *__restrict__ trig, KGeom g, int ntx,
+                                                                  int *__restrict__ min_keys)
+{
+    constexpr int P = kFbpMsSlices / 2;
+    __shared__ __align__(16) FbpMsShared sh;
+    const int z0 = (int)blockIdx.z * kFbpMsSlices;
+    const size_t nprj = (size_t)g.pa * g.px, nimg = (size_t)g.nx * g.ny;
+    const float *rz = fprj + (size_t)z0 * nprj;
+    const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
+    const int X0 = bx * kFbpMsT, Y0 = by * kFbpMsT;
+    const int X1 = min(X0 + kFbpMsT, g.nx) - 1, Y1 = min(Y0 + kFbpMsT, g.ny) - 1;
+    const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
+    const float Yc = (float)min(Y0 + ty, Y1) - g.hy;
+    float xc[kFbpMsPix];
+#pragma unroll
+    for (int i = 0; i < kFbpMsPix; ++i) xc[i] = (float)min(X0 + tx + 8 * i, X1) - g.hx;
+    f2x acc[kFbpMsPix][P];
+#pragma unroll
+    for (int i = 0; i < kFbpMsPix; ++i)
+#pragma unroll
+        for (int h = 0; h < P; ++h) acc[i][h] = 0ull;
+    const unsigned wbase = (unsigned)__cvta_generic_to_shared(sh.win);
+    const f2x cxp = f2_pack(g.cx, g.cx), hp = f2_pack(0.5f, 0.5f), MM = f2_pack(12582912.0f, 12582912.0f);
+    const f2x one2 = f2_pack(1.0f, 1.0f);
+    for (int k0 = 0; k0 < g.pa; k0 += kFbpMsChunk) {
+        const int kn = min(kFbpMsChunk, g.pa - k0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < kn; k += kFbpMsThreads) {
+            const float2 cs = trig[k0 + k];
+            sh.scs[k] = cs;
+            const float xa = (float)X0 - g.hx, xb = (float)X1 - g.hx;
+            const float qa = ((float)Y0 - g.hy) * cs.y, qb = ((float)Y1 - g.hy) * cs.y;
+            int lo = xct_floor_bits(xct_bin_coord(xa, cs.x, qa, g.cx) - 0.5f);
+            lo = min(lo, xct_floor_bits(xct_bin_coord(xb, cs.x, qa, g.cx) - 0.5f));
+            lo = min(lo, xct_floor_bits(xct_bin_coord(xa, cs.x, qb, g.cx) - 0.5f));
+            lo = min(lo, xct_floor_bits(xct_bin_coord(xb, cs.x, qb, g.cx) - 0.5f));
+            lo &= ~3;  // the bias is a multiple of 4: this rounds the bin down to one
+            sh.slo[k] = lo - XCT_FLOOR_BIAS;
+            sh.soff[k] = wbase + 8u * (unsigned)(k * kFbpMsW) - 8u * (unsigned)lo;
+        }
+        __syncthreads();
+        // window (pair p, angle k, bin lo_k + r) = (t_{2p}, t_{2p+1}), 0 off the detector
+        for (int e = threadIdx.x; e < kn * kFbpMsSlices * kFbpMsW; e += kFbpMsThreads) {
+            const int r = e % kFbpMsW, t2 = e / kFbpMsW;
+            const int z = t2 & (kFbpMsSlices - 1), k = t2 >> 3;
+            const int bin = sh.slo[k] + r;
+            const float *row = rz + (size_t)z * nprj + (size_t)(k0 + k) * g.px;
+            const bool in = (unsigned)bin < (unsigned)g.px;
+            const unsigned dst =
+                wbase + (unsigned)(z >> 1) * kFbpMsPairBytes + 8u * (unsigned)(k * kFbpMsW + r) + 4u * (unsigned)(z & 1);
+            cp_async4(dst, in ? (const void *)(row + bin) : (const void *)row, in ? 4u : 0u);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        // any entry whose next entry (the lerp's second bin) is staged
+        const unsigned wlo = wbase, whi = wbase + 8u * (unsigned)(kn * kFbpMsW - 2);
+        (void)wlo;
+        (void)whi;
+        for (int k = 0; k < kn; ++k) {
+            const float c = sh.scs[k].x, s = sh.scs[k].y;
+            const unsigned off = sh.soff[k];
+            const float q = Yc * s;
+#pragma unroll
+            for (int j = 0; j < kFbpMsPix / 2; ++j) {
+                // fbp_bp_kernel's expression for pixels 2j and 2j+1
+                const float p0 = xc[2 * j] * c, p1 = xc[2 * j + 1] * c;
+                const f2x d = f2_pack(p0 - q, p1 - q);
+                const f2x uu = f2_sub(f2_add(f2_add(d, cxp), hp), hp);
+                const f2x tb = f2_add_rd(uu, MM);
+                const f2x a2 = f2_sub(uu, f2_sub(tb, MM));
+                const f2x w2 = f2_sub(one2, a2);
+                int e0, e1;
+                f2_unpack_bits(tb, e0, e1);
+                float a[2], w[2];
+                f2_unpack(a2, a[0], a[1]);
+                f2_unpack(w2, w[0], w[1]);
+                const unsigned ad[2] = {(unsigned)e0 * 8u + off, (unsigned)e1 * 8u + off};
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    if (!XCT_IN(ad[u], wlo, whi, XCT_SITE_FBP_WIN)) continue;
+#pragma unroll
+                    for (int h = 0; h < P; ++h) {
+                        float t0a, t0b, t1a, t1b;  // (slice 2h, 2h+1) at bins i and i + 1
+                        if (h == 0) {
+                            lds_f2_at<0>(ad[u], t0a, t0b);
+                            lds_f2_at<8>(ad[u], t1a, t1b);
+                        } else if (h == 1) {
+                            lds_f2_at<1 * kFbpMsPairBytes>(ad[u], t0a, t0b);
+                            lds_f2_at<1 * kFbpMsPairBytes + 8>(ad[u], t1a, t1b);
+                        } else if (h == 2) {
+                            lds_f2_at<2 * kFbpMsPairBytes>(ad[u], t0a, t0b);
+                            lds_f2_at<2 * kFbpMsPairBytes + 8>(ad[u], t1a, t1b);
+                        } else {
+                            lds_f2_at<3 * kFbpMsPairBytes>(ad[u], t0a, t0b);
+                            lds_f2_at<3 * kFbpMsPairBytes + 8>(ad[u], t1a, t1b);
+                        }
+                        const float pa0 = w[u] * t0a, pb0 = w[u] * t0b, pa1 = a[u] * t1a, pb1 = a[u] * t1b;
+                        acc[2 * j + u][h] = f2_add(acc[2 * j + u][h], f2_add(f2_pack(pa0, pb0), f2_pack(pa1, pb1)));
+                    }
+                }
+            }
+        }
+    }
+    const float two_pa = (float)g.pa * 2.0f;
+    const int Y = Y0 + ty;
+    float vmin[kFbpMsSlices];
+#pragma unroll
+    for (int z = 0; z < kFbpMsSlices; ++z) vmin[z] = INFINITY;
+    if (Y <= Y1) {
+#pragma unroll
+        for (int i = 0; i < kFbpMsPix; ++i) {
+            const int X = X0 + tx + 8 * i;
+            if (X > X1) continue;
+            const float rr = sqrtf(xc[i] * xc[i] + Yc * Yc);
+#pragma unroll
+            for (int h = 0; h < P; ++h) {
+                float v2[2];
+                f2_unpack(acc[i][h], v2[0], v2[1]);
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int z = 2 * h + u;
+                    const float v = (rr < g.hx) ? __fdiv_rn(v2[u], two_pa) : 0.0f;
+                    img[(size_t)(z0 + z) * nimg + (size_t)Y * g.nx + X] = v;
+                    vmin[z] = fminf(vmin[z], v);
+                }
+            }
+        }
+    }
+    if (min_keys != nullptr) {
+#pragma unroll
+        for (int z = 0; z < kFbpMsSlices; ++z) {
+            float m = vmin[z];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if ((threadIdx.x & 31) == 0) sh.red[threadIdx.x >> 5][z] = m;
+        }
+        __syncthreads();
+        if (threadIdx.x < kFbpMsSlices) {
+            float m = sh.red[0][threadIdx.x];
+            for (int i = 1; i < kFbpMsThreads / 32; ++i) m = fminf(m, sh.red[i][threadIdx.x]);
+            atomicMin(min_keys + z0 + threadIdx.x, fkey(m));
+        }
+    }
+}
+
 // baseUp (reconstShare.cl:87-109) over dN slices of n pixels, in place, a = the slice
 // minimum: b1 = (v - a)/a (0 when a == 0); g = sum_{i<=order} (-1)^(i+1) b1^i / i in float;
 // v -= a * exp(g).
@@ -442,6 +614,22 @@ int launch_fbp_bp(const KGeom &g, const float2 *trig, const float *fprj, float *
     if (min_keys != nullptr) {
         cudaError_t e = cudaMemsetAsync(min_keys, 0x7F, sizeof(int) * dN, st);  // key of a huge float
         if (e != cudaSuccess) return xct_cuda_fail(e, "fbp min reset");
+    }
+    // with the slice-interleaved kernels on, groups of eight slices go through the
+    // eight-slice backprojector and the rest through the per-slice one
+    const int ms = g.ms_chunk > 0 ? (dN / kFbpMsSlices) * kFbpMsSlices : 0;
+    if (ms > 0) {
+        const int mtx = (g.nx + kFbpMsT - 1) / kFbpMsT, mty = (g.ny + kFbpMsT - 1) / kFbpMsT;
+        fbp_bp_ms_kernel<<<dim3(mtx * mty, 1, ms / kFbpMsSlices), kFbpMsThreads, 0, st>>>(fprj, img, trig, g, mtx,
+                                                                                          min_keys);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return xct_cuda_fail(e, "fbp_bp_ms_kernel launch");
+        g_xct_launches.fetch_add(1);
+        if (ms == dN) return XCT_OK;
+        fprj += (size_t)ms * g.pa * g.px;
+        img += (size_t)ms * g.nx * g.ny;
+        if (min_keys != nullptr) min_keys += ms;
+        dN -= ms;
     }
     dim3 grid(ntx * nty, 1, dN);
     // four rows per thread once the grid gives three waves of its resident CTAs (6 per SM)

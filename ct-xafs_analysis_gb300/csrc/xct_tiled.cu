@@ -32,6 +32,7 @@
 #include <atomic>
 #include <type_traits>
 
+#include "xct_async.cuh"
 #include "xct_check.cuh"
 #include "xct_device.cuh"
 #include "xct_f32x2.cuh"
@@ -116,25 +117,6 @@ __device__ __forceinline__ int first_true(float b, float a, float sl, float inv_
     const bool ph = (Y >= D) || (up ? (uh >= b) : (uh < b));
     if (!pl && ph) return Y;
     return first_true_search(b, a, sl, hd, D);
-}
-
-// Asynchronous global -> shared copies (zero-filled past src_bytes) and their wait.
-__device__ __forceinline__ void cp_async16(unsigned dst, const void *src, unsigned src_bytes)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async4(unsigned dst, const void *src, unsigned src_bytes)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-template <int kOff>
-__device__ __forceinline__ float lds_f1_at(unsigned addr)
-{
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1+%2];" : "=f"(v) : "r"(addr), "n"(kOff));
-    return v;
 }
 
 __device__ __forceinline__ void lds_f2(unsigned addr, float &a, float &b)

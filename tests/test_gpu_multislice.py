@@ -1,6 +1,6 @@
-"""The slice-interleaved kernels (groups of eight slices of one geometry;
-xct_plan_set_multislice): the forward projector (one 128-byte shared-memory line per texel)
-and the backprojector (one 32-byte window entry per bin holding the eight slices' ratios).
+"""The slice-interleaved kernels (groups of slices of one geometry; xct_plan_set_multislice):
+the forward projector (one 128-byte shared-memory line per texel), the OS-EM and FBP
+backprojectors (one bin expression per eight slices) and the exact adjoint (gather form).
 
 It must compute what the per-slice tiled kernel computes -- the same samples and bilinear
 weights; only the order in which a ray's samples are added differs (one lane walks the
@@ -224,4 +224,34 @@ def test_multislice_dot_product(gpu_ctx):
             lhs = float((ax[z].double() * y[z].double()).sum())
             rhs = float((x[z].double() * aty[z].double()).sum())
             assert abs(lhs - rhs) <= 1e-5 * abs(lhs), (z, lhs, rhs)
+    plan.close()
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_multislice_fbp_bit_identical(gpu_ctx, oracle_lib, case):
+    """The FBP backprojection of dN slices with the eight-slice kernel (groups of eight, the
+    rest per slice) gives every slice the per-slice kernel's image bit for bit, and the
+    hybrid's base-up (which uses the per-slice minimum the backprojector reduces) as well;
+    slice 0 is also bit-identical to the oracle's backProjectionFBP (FBP.cl:164-188)."""
+    import xct
+    O = oracle_lib
+    nx, ny, px, pa, ss, span, off, dN, chunk = CASES[case]
+    ang, _, cx = _case(CASES[case], 100 + case)
+    rng = np.random.default_rng(110 + case)
+    fp = rng.uniform(-0.5, 1.5, (dN, pa, px)).astype(np.float32)
+    plan = xct.OSEMPlan(gpu_ctx, nx, ny, px, ang, ss, 1, center_bin=cx, max_batch=dN)
+    d_fp = torch.from_numpy(fp).cuda()
+    out = {}
+    for ms in (0, chunk):
+        plan.set_multislice(ms)
+        x = torch.empty((dN, ny, nx), device="cuda")
+        plan.fbp_backproject(d_fp, x)
+        h = torch.empty((dN, ny, nx), device="cuda")
+        plan.hybrid(d_fp.abs().contiguous(), h, zp=0, it=0)
+        torch.cuda.synchronize()
+        out[ms] = (x.cpu().numpy(), h.cpu().numpy())
+    assert np.array_equal(out[chunk][0], out[0][0]), int(np.count_nonzero(out[chunk][0] != out[0][0]))
+    assert np.array_equal(out[chunk][1], out[0][1]), int(np.count_nonzero(out[chunk][1] != out[0][1]))
+    want = O.bp_fbp(fp[0], ang, nx, ny, cx=cx)
+    assert np.array_equal(out[chunk][0][0], want), int(np.count_nonzero(out[chunk][0][0] != want))
     plan.close()
