@@ -255,3 +255,29 @@ def test_multislice_fbp_bit_identical(gpu_ctx, oracle_lib, case):
     want = O.bp_fbp(fp[0], ang, nx, ny, cx=cx)
     assert np.array_equal(out[chunk][0][0], want), int(np.count_nonzero(out[chunk][0][0] != want))
     plan.close()
+
+
+def test_multislice_compressed_sensing(gpu_ctx, oracle_lib):
+    """Compressed-sensing OS-EM (FISTA_OSEM_execution, GPU.cpp:243-405) on a stack of nine
+    slices through the slice-interleaved kernels (eight) and the per-slice ones (one) against
+    the per-slice kernels alone and against the oracle."""
+    import xct
+    from xct import phantom as P
+    O = oracle_lib
+    n, pa, ss, it, dN, lam = 96, 72, 6, 2, 9, 1.0e-4
+    ang = P.uniform_angles(pa)
+    prm = P.ellipsoid_params(n, dN, count=6, seed=123)
+    meas = np.stack([P.noisy_log_sinogram(O.projection(P.ellipsoid_slice(prm, z, n, n), ang, n), 1e5, z)
+                     for z in range(dN)]).astype(np.float32)
+    plan = xct.OSEMPlan(gpu_ctx, n, n, n, ang, ss, it, max_batch=dN)
+    out = {}
+    for ms in (0, 128):
+        plan.set_multislice(ms)
+        x = torch.ones((dN, n, n), device="cuda")
+        plan.cs_run_device(torch.from_numpy(meas).cuda(), x, cs_lambda=lam)
+        torch.cuda.synchronize()
+        out[ms] = x.cpu().numpy().astype(np.float64)
+    assert _rel(out[128], out[0]) <= 1e-5
+    want = O.cs_osem_run(np.ones((dN, n, n), np.float32), meas, ang, ss, it, lam)
+    assert _rel(out[128], want) <= 1e-4
+    plan.close()
