@@ -741,9 +741,10 @@ def profile_case():
 
 
 def profile_case_operators(n=8):
-    """Small case for profilers, the operator pair: the forward projection and the exact
-    adjoint of n slices of the workload over all 1500 angles, each once (the slice-interleaved
-    forward projector and the gather adjoint for n = 8).  ~0.3 GB on the device."""
+    """Small case for profilers, the operator pair and FBP: the forward projection, the exact
+    adjoint and the FBP of n slices of the workload over all 1500 angles, each once (the
+    slice-interleaved forward projector, the gather adjoint and the eight-slice FBP
+    backprojector for n = 8).  ~0.5 GB on the device."""
     import torch
     import xct
     from xct import phantom
@@ -756,6 +757,8 @@ def profile_case_operators(n=8):
     plan.fwd(img, sino)
     back = torch.empty_like(img)
     plan.adj(sino, back)
+    rec = torch.empty_like(img)
+    plan.fbp(sino, rec, zp=4096)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": "operators", "n": n, "multislice": plan.multislice(),
                       "mean": float(back.mean())}))
