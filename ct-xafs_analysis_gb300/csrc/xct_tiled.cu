@@ -1375,22 +1375,24 @@ constexpr int kBpMsChunk = 24;  // angles per staging pass
 constexpr int kBpMsPix = 4;     // pixels per thread, 8 apart
 constexpr unsigned kBpMsSliceBytes = (unsigned)(kBpMsChunk * kBpMsW * 4);  // one slice's windows
 
+template <int S>
 struct BpMsShared {
-    float win[kMsSlices * kBpMsChunk * kBpMsW];  // [slice][angle][bin]
+    float win[S * kBpMsChunk * kBpMsW];          // [slice][angle][bin]
     float2 scs[kBpMsChunk];                      // (c, s)
     int slo[kBpMsChunk];                         // first staged bin (a multiple of 4)
     unsigned soff[kBpMsChunk];                   // byte address of slice 0's entry (bits - BIAS - lo)
 };
 
-// grid: (ntx*nty tiles of 32 x 32, 1, dN / 8 slice groups).  vec: 16-byte staging copies
-// (px a multiple of 4 and a 16-byte aligned ratio array).
+// grid: (ntx*nty tiles of 32 x 32, 1, dN / S slice groups), S = 8 or 2.  vec: 16-byte staging
+// copies (px a multiple of 4 and a 16-byte aligned ratio array).
+template <int S>
 __global__ void __launch_bounds__(kBpMsThreads) bp_ms_kernel(float *__restrict__ img, const float *__restrict__ ratio,
                                                              const float2 *__restrict__ trig, KGeom g, int sub,
                                                              int nang, int ntx, float ssf, float paf, int vec)
 {
-    __shared__ __align__(16) BpMsShared sh;
+    __shared__ __align__(16) BpMsShared<S> sh;
     const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
-    const int z0 = (int)blockIdx.z * kMsSlices;
+    const int z0 = (int)blockIdx.z * S;
     const size_t nimg = (size_t)g.nx * g.ny, nprj = (size_t)g.pa * g.px;
     const float *rz = ratio + (size_t)z0 * nprj;
     const int X0 = bx * kBpMsT, Y0 = by * kBpMsT;
@@ -1403,11 +1405,11 @@ __global__ void __launch_bounds__(kBpMsThreads) bp_ms_kernel(float *__restrict__
     float xc[kBpMsPix];
 #pragma unroll
     for (int i = 0; i < kBpMsPix; ++i) xc[i] = (float)min(X0 + tx + 8 * i, X1) - g.hx;
-    f2x acc[kBpMsPix][kMsSlices / 2];  // slice pairs of each pixel
+    f2x acc[kBpMsPix][S / 2];  // slice pairs of each pixel
 #pragma unroll
     for (int i = 0; i < kBpMsPix; ++i)
 #pragma unroll
-        for (int h = 0; h < kMsSlices / 2; ++h) acc[i][h] = 0ull;
+        for (int h = 0; h < S / 2; ++h) acc[i][h] = 0ull;
     const f2x cxp = f2_pack(g.cx, g.cx);
     const f2x hp = f2_pack(0.5f, 0.5f);
     const f2x MM = f2_pack(kMagic, kMagic);
@@ -1436,9 +1438,9 @@ __global__ void __launch_bounds__(kBpMsThreads) bp_ms_kernel(float *__restrict__
         // window (z, k) = ratio[z0 + z][th_k][lo_k .. lo_k + W), 0 off the detector
         if (vec) {
             constexpr int kQ = kBpMsW / 4;
-            for (int i = t; i < kn * kMsSlices * kQ; i += kBpMsThreads) {
+            for (int i = t; i < kn * S * kQ; i += kBpMsThreads) {
                 const int q = i % kQ, r = i / kQ;
-                const int z = r & (kMsSlices - 1), k = r >> 3;
+                const int z = r % S, k = r / S;
                 const int bin = sh.slo[k] + 4 * q;
                 const int th = sub + (k0 + k) * g.ss;
                 const float *row = rz + (size_t)z * nprj + (size_t)th * g.px;
@@ -1447,9 +1449,9 @@ __global__ void __launch_bounds__(kBpMsThreads) bp_ms_kernel(float *__restrict__
                 cp_async16(dst, nb > 0 ? (const void *)(row + bin) : (const void *)row, nb > 0 ? 4u * (unsigned)nb : 0u);
             }
         } else {
-            for (int i = t; i < kn * kMsSlices * kBpMsW; i += kBpMsThreads) {
+            for (int i = t; i < kn * S * kBpMsW; i += kBpMsThreads) {
                 const int j = i % kBpMsW, r = i / kBpMsW;
-                const int z = r & (kMsSlices - 1), k = r >> 3;
+                const int z = r % S, k = r / S;
                 const int bin = sh.slo[k] + j;
                 const int th = sub + (k0 + k) * g.ss;
                 const float *row = rz + (size_t)z * nprj + (size_t)th * g.px;
@@ -1477,22 +1479,24 @@ __global__ void __launch_bounds__(kBpMsThreads) bp_ms_kernel(float *__restrict__
                 const unsigned ad[2] = {(unsigned)b0 * 4u + off, (unsigned)b1 * 4u + off};
 #pragma unroll
                 for (int u = 0; u < 2; ++u) {
-                    float v[kMsSlices];
+                    float v[S];
                     if (XCT_IN(ad[u], wlo, whi, XCT_SITE_BP_WIN)) {
                         v[0] = lds_f1_at<0 * kBpMsSliceBytes>(ad[u]);
                         v[1] = lds_f1_at<1 * kBpMsSliceBytes>(ad[u]);
-                        v[2] = lds_f1_at<2 * kBpMsSliceBytes>(ad[u]);
-                        v[3] = lds_f1_at<3 * kBpMsSliceBytes>(ad[u]);
-                        v[4] = lds_f1_at<4 * kBpMsSliceBytes>(ad[u]);
-                        v[5] = lds_f1_at<5 * kBpMsSliceBytes>(ad[u]);
-                        v[6] = lds_f1_at<6 * kBpMsSliceBytes>(ad[u]);
-                        v[7] = lds_f1_at<7 * kBpMsSliceBytes>(ad[u]);
+                        if constexpr (S == 8) {
+                            v[2] = lds_f1_at<2 * kBpMsSliceBytes>(ad[u]);
+                            v[3] = lds_f1_at<3 * kBpMsSliceBytes>(ad[u]);
+                            v[4] = lds_f1_at<4 * kBpMsSliceBytes>(ad[u]);
+                            v[5] = lds_f1_at<5 * kBpMsSliceBytes>(ad[u]);
+                            v[6] = lds_f1_at<6 * kBpMsSliceBytes>(ad[u]);
+                            v[7] = lds_f1_at<7 * kBpMsSliceBytes>(ad[u]);
+                        }
                     } else {
 #pragma unroll
-                        for (int z = 0; z < kMsSlices; ++z) v[z] = 0.0f;
+                        for (int z = 0; z < S; ++z) v[z] = 0.0f;
                     }
 #pragma unroll
-                    for (int h = 0; h < kMsSlices / 2; ++h)
+                    for (int h = 0; h < S / 2; ++h)
                         acc[2 * j + u][h] = f2_add(acc[2 * j + u][h], f2_pack(v[2 * h], v[2 * h + 1]));
                 }
             }
@@ -1505,7 +1509,7 @@ __global__ void __launch_bounds__(kBpMsThreads) bp_ms_kernel(float *__restrict__
         const int X = X0 + tx + 8 * i;
         if (X > X1) continue;
 #pragma unroll
-        for (int h = 0; h < kMsSlices / 2; ++h) {
+        for (int h = 0; h < S / 2; ++h) {
             float v0, v1;
             f2_unpack(acc[i][h], v0, v1);
             float *p0 = img + (size_t)(z0 + 2 * h) * nimg + (size_t)Y * g.nx + X;
@@ -1905,20 +1909,31 @@ int launch_bp_update_tiled(const KGeom &g, const float2 *trig, float *img, const
     if (dN <= 0) return XCT_OK;
     const int nang = (g.pa - sub + g.ss - 1) / g.ss;  // OSEM2's angle loop (OSEM.cl:93)
     // with the slice-interleaved kernels on, whole groups of eight slices go through the
-    // eight-slice backprojector and the rest through the per-slice one
-    const int ms = g.ms_chunk > 0 ? (dN / kMsSlices) * kMsSlices : 0;
-    if (ms > 0) {
+    // eight-slice backprojector, pairs of the rest through its two-slice form, and a last
+    // single slice through the per-slice one
+    if (g.ms_chunk > 0 && dN >= 2) {
         const int mtx = (g.nx + kBpMsT - 1) / kBpMsT, mty = (g.ny + kBpMsT - 1) / kBpMsT;
-        dim3 mgrid(mtx * mty, 1, ms / kMsSlices);
         const int vec = g.px % 4 == 0 && ((uintptr_t)ratio & 15u) == 0;
-        bp_ms_kernel<<<mgrid, kBpMsThreads, 0, st>>>(img, ratio, trig, g, sub, nang, mtx, (float)g.ss, (float)g.pa,
-                                                     vec);
-        g_xct_launches.fetch_add(1, std::memory_order_relaxed);
-        XCT_CUDA_TRY(cudaGetLastError());
-        if (ms == dN) return XCT_OK;
-        img += (size_t)ms * g.nx * g.ny;
-        ratio += (size_t)ms * g.pa * g.px;
-        dN -= ms;
+        const int g8 = dN / kMsSlices, g2 = (dN - g8 * kMsSlices) / 2;
+        if (g8 > 0) {
+            bp_ms_kernel<kMsSlices><<<dim3(mtx * mty, 1, g8), kBpMsThreads, 0, st>>>(
+                img, ratio, trig, g, sub, nang, mtx, (float)g.ss, (float)g.pa, vec);
+            g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+            XCT_CUDA_TRY(cudaGetLastError());
+            img += (size_t)g8 * kMsSlices * g.nx * g.ny;
+            ratio += (size_t)g8 * kMsSlices * g.pa * g.px;
+            dN -= g8 * kMsSlices;
+        }
+        if (g2 > 0) {
+            bp_ms_kernel<2><<<dim3(mtx * mty, 1, g2), kBpMsThreads, 0, st>>>(img, ratio, trig, g, sub, nang, mtx,
+                                                                             (float)g.ss, (float)g.pa, vec);
+            g_xct_launches.fetch_add(1, std::memory_order_relaxed);
+            XCT_CUDA_TRY(cudaGetLastError());
+            img += (size_t)g2 * 2 * g.nx * g.ny;
+            ratio += (size_t)g2 * 2 * g.pa * g.px;
+            dN -= g2 * 2;
+        }
+        if (dN == 0) return XCT_OK;
     }
     const int ntx = (g.nx + kBpTX - 1) / kBpTX, nty = (g.ny + kBpTY - 1) / kBpTY;
     dim3 grid(ntx * nty, 1, dN);
