@@ -375,23 +375,25 @@ __global__ void __launch_bounds__(512 / R, R == 4 ? 6 : 4) fbp_bp_kernel(const f
 constexpr int kFbpMsT = 32, kFbpMsThreads = 256, kFbpMsW = 52, kFbpMsChunk = 24, kFbpMsPix = 4, kFbpMsSlices = 8;
 constexpr unsigned kFbpMsPairBytes = (unsigned)(kFbpMsChunk * kFbpMsW * 8);  // one slice pair's windows
 
+template <int S>
 struct FbpMsShared {
-    float2 win[(kFbpMsSlices / 2) * kFbpMsChunk * kFbpMsW];  // [pair][angle][bin]: (t_z, t_z+1)
+    float2 win[(S / 2) * kFbpMsChunk * kFbpMsW];  // [pair][angle][bin]: (t_z, t_z+1)
     float2 scs[kFbpMsChunk];
     int slo[kFbpMsChunk];
     unsigned soff[kFbpMsChunk];  // shared address of angle k's entry for floor bits fb: soff[k] + 8*fb
-    float red[kFbpMsThreads / 32][kFbpMsSlices];
+    float red[kFbpMsThreads / 32][S];
 };
 
-// grid: (ntx * nty tiles of 32 x 32, 1, dN / 8 slice groups).
+// grid: (ntx * nty tiles of 32 x 32, 1, dN / S slice groups), S = 8 or 2.
+template <int S>
 __global__ void __launch_bounds__(kFbpMsThreads) fbp_bp_ms_kernel(const float *__restrict__ fprj,
                                                                   float *__restrict__ img,
                                                                   const float2 *__restrict__ trig, KGeom g, int ntx,
                                                                   int *__restrict__ min_keys)
 {
-    constexpr int P = kFbpMsSlices / 2;
-    __shared__ __align__(16) FbpMsShared sh;
-    const int z0 = (int)blockIdx.z * kFbpMsSlices;
+    constexpr int P = S / 2;
+    __shared__ __align__(16) FbpMsShared<S> sh;
+    const int z0 = (int)blockIdx.z * S;
     const size_t nprj = (size_t)g.pa * g.px, nimg = (size_t)g.nx * g.ny;
     const float *rz = fprj + (size_t)z0 * nprj;
     const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
@@ -428,9 +430,9 @@ __global__ void __launch_bounds__(kFbpMsThreads) fbp_bp_ms_kernel(const float *_
         }
         __syncthreads();
         // window (pair p, angle k, bin lo_k + r) = (t_{2p}, t_{2p+1}), 0 off the detector
-        for (int e = threadIdx.x; e < kn * kFbpMsSlices * kFbpMsW; e += kFbpMsThreads) {
+        for (int e = threadIdx.x; e < kn * S * kFbpMsW; e += kFbpMsThreads) {
             const int r = e % kFbpMsW, t2 = e / kFbpMsW;
-            const int z = t2 & (kFbpMsSlices - 1), k = t2 >> 3;
+            const int z = t2 % S, k = t2 / S;
             const int bin = sh.slo[k] + r;
             const float *row = rz + (size_t)z * nprj + (size_t)(k0 + k) * g.px;
             const bool in = (unsigned)bin < (unsigned)g.px;
@@ -491,9 +493,9 @@ __global__ void __launch_bounds__(kFbpMsThreads) fbp_bp_ms_kernel(const float *_
     }
     const float two_pa = (float)g.pa * 2.0f;
     const int Y = Y0 + ty;
-    float vmin[kFbpMsSlices];
+    float vmin[S];
 #pragma unroll
-    for (int z = 0; z < kFbpMsSlices; ++z) vmin[z] = INFINITY;
+    for (int z = 0; z < S; ++z) vmin[z] = INFINITY;
     if (Y <= Y1) {
 #pragma unroll
         for (int i = 0; i < kFbpMsPix; ++i) {
@@ -516,14 +518,14 @@ __global__ void __launch_bounds__(kFbpMsThreads) fbp_bp_ms_kernel(const float *_
     }
     if (min_keys != nullptr) {
 #pragma unroll
-        for (int z = 0; z < kFbpMsSlices; ++z) {
+        for (int z = 0; z < S; ++z) {
             float m = vmin[z];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
             if ((threadIdx.x & 31) == 0) sh.red[threadIdx.x >> 5][z] = m;
         }
         __syncthreads();
-        if (threadIdx.x < kFbpMsSlices) {
+        if (threadIdx.x < S) {
             float m = sh.red[0][threadIdx.x];
             for (int i = 1; i < kFbpMsThreads / 32; ++i) m = fminf(m, sh.red[i][threadIdx.x]);
             atomicMin(min_keys + z0 + threadIdx.x, fkey(m));
@@ -616,20 +618,33 @@ int launch_fbp_bp(const KGeom &g, const float2 *trig, const float *fprj, float *
         if (e != cudaSuccess) return xct_cuda_fail(e, "fbp min reset");
     }
     // with the slice-interleaved kernels on, groups of eight slices go through the
-    // eight-slice backprojector and the rest through the per-slice one
-    const int ms = g.ms_chunk > 0 ? (dN / kFbpMsSlices) * kFbpMsSlices : 0;
-    if (ms > 0) {
+    // eight-slice backprojector, pairs of the rest through its two-slice form, and a last
+    // single slice through the per-slice one
+    if (g.ms_chunk > 0 && dN >= 2) {
         const int mtx = (g.nx + kFbpMsT - 1) / kFbpMsT, mty = (g.ny + kFbpMsT - 1) / kFbpMsT;
-        fbp_bp_ms_kernel<<<dim3(mtx * mty, 1, ms / kFbpMsSlices), kFbpMsThreads, 0, st>>>(fprj, img, trig, g, mtx,
-                                                                                          min_keys);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return xct_cuda_fail(e, "fbp_bp_ms_kernel launch");
-        g_xct_launches.fetch_add(1);
-        if (ms == dN) return XCT_OK;
-        fprj += (size_t)ms * g.pa * g.px;
-        img += (size_t)ms * g.nx * g.ny;
-        if (min_keys != nullptr) min_keys += ms;
-        dN -= ms;
+        const int g8 = dN / kFbpMsSlices, g2 = (dN - g8 * kFbpMsSlices) / 2;
+        auto advance = [&](int n) {
+            fprj += (size_t)n * g.pa * g.px;
+            img += (size_t)n * g.nx * g.ny;
+            if (min_keys != nullptr) min_keys += n;
+            dN -= n;
+        };
+        if (g8 > 0) {
+            fbp_bp_ms_kernel<kFbpMsSlices><<<dim3(mtx * mty, 1, g8), kFbpMsThreads, 0, st>>>(fprj, img, trig, g, mtx,
+                                                                                             min_keys);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return xct_cuda_fail(e, "fbp_bp_ms_kernel launch");
+            g_xct_launches.fetch_add(1);
+            advance(g8 * kFbpMsSlices);
+        }
+        if (g2 > 0) {
+            fbp_bp_ms_kernel<2><<<dim3(mtx * mty, 1, g2), kFbpMsThreads, 0, st>>>(fprj, img, trig, g, mtx, min_keys);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return xct_cuda_fail(e, "fbp_bp_ms_kernel launch");
+            g_xct_launches.fetch_add(1);
+            advance(g2 * 2);
+        }
+        if (dN == 0) return XCT_OK;
     }
     dim3 grid(ntx * nty, 1, dN);
     // four rows per thread once the grid gives three waves of its resident CTAs (6 per SM)
