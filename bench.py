@@ -355,17 +355,19 @@ def ctxafs_stack_specs(n_energy, n_slices, seed=3, widths=(512, 1024, 1536, 2048
     (bins = w_s; every width in `widths` equally often, seeded order), energy e has its own
     projection count from `angles` over 180 deg with 0..max_drop of them dropped at random
     (one angle list for all slices of that energy, as reslicing one projection set gives).
-    Returns the widths [n_slices] and the angle arrays [n_energy]."""
+    Returns the widths [n_slices], the angle arrays [n_energy] and, per energy, the full
+    projection count and the kept indices."""
     rng = np.random.default_rng(seed)
     ws = np.resize(np.asarray(widths), n_slices)
     rng.shuffle(ws)
-    angs = []
+    angs, grids = [], []
     for _ in range(n_energy):
         pa = int(rng.choice(angles))
         drop = int(rng.integers(0, int(max_drop * pa) + 1))
         keep = np.sort(rng.choice(pa, pa - drop, replace=False))
         angs.append((keep * (180.0 / pa)).astype(np.float32))
-    return [int(w) for w in ws], angs
+        grids.append((pa, keep))
+    return [int(w) for w in ws], angs, grids
 
 
 def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
@@ -379,7 +381,7 @@ def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
     import torch
     import xct
     from xct import phantom
-    widths, angs = ctxafs_stack_specs(n_energy, n_slices)
+    widths, angs, grids = ctxafs_stack_specs(n_energy, n_slices)
     e_axis, s1, s2 = phantom.xanes_mixture(n_energy, seed=3)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(3)
@@ -388,10 +390,11 @@ def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
     for s_i, w in enumerate(widths):
         sup, f = phantom.xanes_fields(w, 100 + s_i)
         fields.append((torch.from_numpy(sup).cuda(), torch.from_numpy(f).cuda()))
-    sinos, geoms, shapes = [], [], []
+    sinos, geoms, shapes, item_grid = [], [], [], []
     for e in range(n_energy):
         ang = angs[e]
         for s_i, w in enumerate(widths):
+            item_grid.append(grids[e])
             sup, f = fields[s_i]
             img = (sup * (f * float(s1[e]) + (1.0 - f) * float(s2[e])) * 0.02).float().reshape(1, w, w).contiguous()
             p = xct.OSEMPlan(ctx, w, w, w, ang, ss, it)
@@ -471,6 +474,21 @@ def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
     bp.close()
     res["batched_over_plain"] = res["batched"]["value"] / res["per_slice_plain"]["value"]
     res["batched_over_tiled_per_slice"] = res["batched"]["value"] / res["per_slice_tiled"]["value"]
+    # the batched run against the FP32 roofline: algorithmic FLOPs of every item (12 per
+    # forward tap, 5 per backprojection gather, 4 per pixel update and subset; the per-angle
+    # tap and gather counts of each width and full angle grid, summed over the kept angles)
+    counts = {}
+    flop = 0.0
+    for (w, _), (pa_full, keep) in zip(shapes, item_grid):
+        key = (w, pa_full)
+        if key not in counts:
+            counts[key] = algorithmic_counts((np.arange(pa_full) * (180.0 / pa_full)).astype(np.float32), w, w, w)
+        t_fwd, t_bp = counts[key]
+        flop += it * (12.0 * t_fwd[keep].sum() + 5.0 * t_bp[keep].sum() + 4.0 * w * w * ss)
+    peak = xct.fp32_peak_tflops(0)
+    res["roofline"] = {"bound": "fp32", "achieved": flop / (res["batched"]["ms"] * 1e-3) / 1e12, "peak": peak,
+                       "unit": "TFLOP/s", "frac": flop / (res["batched"]["ms"] * 1e-3) / 1e12 / peak,
+                       "flop_per_run": flop}
     return res
 
 
