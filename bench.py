@@ -782,6 +782,29 @@ def profile_case_operators(n=8):
                       "mean": float(back.mean())}))
 
 
+def profile_case_ctxafs(n_energy=16, n_slices=8):
+    """Small case for profilers, the batched CT-XAFS path: a stack of n_energy x n_slices
+    uneven items shaped as the benchmark's (widths 512-2048, 360-1200 angles with drops),
+    one batch plan, one iteration of 10 subsets (30 persistent launches).  ~1.5 GB."""
+    import torch
+    import xct
+    from xct import phantom
+    widths, angs, _ = ctxafs_stack_specs(n_energy, n_slices)
+    ctx = xct.Context(0)
+    rng = np.random.default_rng(5)
+    geoms, sinos, imgs = [], [], []
+    for e in range(n_energy):
+        for w in widths:
+            geoms.append(xct.make_geom(w, w, w, angs[e], 10, 1))
+            sinos.append(torch.from_numpy(rng.uniform(0.5, 1.5, (len(angs[e]), w)).astype(np.float32)).cuda())
+            imgs.append(torch.ones((w, w), device="cuda"))
+    bp = xct.BatchPlan(ctx, geoms, 1)
+    bp.run(sinos, imgs)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "ctxafs", "items": len(geoms), "tuning": bp.tuning()}))
+    bp.close()
+
+
 def profile_case_slices(n=8):
     """Small case for profilers, the slice-interleaved forward projector: n slices of the
     workload (sinograms made with the per-slice forward projector, one launch per 128 angles),
@@ -812,11 +835,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", nargs="?", const="osem", choices=["osem", "slices", "next", "operators"],
+    ap.add_argument("--profile-case", nargs="?", const="osem", choices=["osem", "slices", "next", "operators", "ctxafs"],
                     help="run a small profiling case and exit: osem (one slice, one OS-EM iteration), slices "
                          "(eight slices, one OS-EM iteration, slice-interleaved kernels), next (the components "
-                         "either side of the path, each once) or operators (forward projection and exact adjoint "
-                         "of eight slices)")
+                         "either side of the path, each once), operators (forward projection, exact adjoint and FBP "
+                         "of eight slices) or ctxafs (one iteration of a 128-item CT-XAFS batch plan)")
     args = ap.parse_args()
     if args.profile_case == "osem":
         profile_case()
@@ -829,6 +852,9 @@ def main():
         return
     if args.profile_case == "operators":
         profile_case_operators()
+        return
+    if args.profile_case == "ctxafs":
+        profile_case_ctxafs()
         return
 
     rank = _env_int("RANK", 0)
