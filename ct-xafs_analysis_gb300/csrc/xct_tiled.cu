@@ -1028,7 +1028,7 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
     const int D = g.depth;
     const unsigned wbase = (unsigned)__cvta_generic_to_shared(part);
     const f2x MM = f2_pack(kMagic, kMagic), one2 = f2_pack(1.0f, 1.0f);
-    const f2x hxy = f2_pack(g.hx, g.hy), cij = f2_pack(ci, cj);
+    const f2x hxy = f2_pack(g.hx, g.hy);
     f2x acc[4][P];  // [corner 00, 10, 01, 11][slice pair]
 #pragma unroll
     for (int q = 0; q < 4; ++q)
@@ -1069,9 +1069,17 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
             const float c = scs[k].x, s = scs[k].y;
             const f2x cs2 = f2_pack(c, -s), sc2 = f2_pack(s, c);
             const unsigned wk = wbase + 8u * (unsigned)(k * kAdjGW - sxw[k]);
-            // the candidates: rays Xa, Xa + 1; on each, indices Ya, Ya + 1
+            // the candidates: rays Xa, Xa + 1 (lattice coordinate of the cell centre u0 - 0.717
+            // and up); on each, indices Ya, Ya + 1 (the centre's coordinate along the rays, w0,
+            // is the same on every ray)
             const float u0 = fmaf(di, c, fmaf(-dj, s, g.cx));
+            const float w0 = fmaf(di, s, dj * c) + g.hd;
             const int Xa = (xct_floor_bits(u0 - 0.717f) - XCT_FLOOR_BIAS) + 1;
+            const int Ya = (xct_floor_bits(w0 - 0.717f) - XCT_FLOOR_BIAS) + 1;
+            // Y - hd is exact (hd is a multiple of 0.5), so the second index is the first + 1
+            const float Yc0 = (float)Ya - g.hd;
+            const f2x yy[2] = {f2_pack(Yc0, Yc0), f2_pack(Yc0 + 1.0f, Yc0 + 1.0f)};
+            const bool yin[2] = {(unsigned)Ya < (unsigned)D, (unsigned)(Ya + 1) < (unsigned)D};
             f2x cxy[4];
             int cX[4];
             unsigned valid = 0;
@@ -1080,24 +1088,16 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
                 const int X = Xa + a;
                 const float Xc = (float)X - g.cx;
                 const f2x axy = f2_fma(f2_pack(Xc, Xc), cs2, hxy);  // (ax, ay) as the forward
-                float dx_, dy_;
-                f2_unpack(f2_sub(cij, axy), dx_, dy_);
-                const float yc0 = fmaf(dx_, s, dy_ * c);
-                const int Ya = (xct_floor_bits(yc0 + g.hd - 0.717f) - XCT_FLOOR_BIAS) + 1;
                 const bool xin = (unsigned)X < (unsigned)g.px;
-                // Y - hd is exact (hd is a multiple of 0.5), so the second index is the first + 1
-                const float Yc0 = (float)Ya - g.hd;
 #pragma unroll
                 for (int b = 0; b < 2; ++b) {
-                    const int Y = Ya + b;
-                    const float Yc = Yc0 + (float)b;
-                    const f2x xy = f2_fma(f2_pack(Yc, Yc), sc2, axy);  // (x, y) as the forward
+                    const f2x xy = f2_fma(yy[b], sc2, axy);  // (x, y) as the forward
                     int xb, yb;
                     f2_unpack_bits(f2_add_rd(xy, MM), xb, yb);
                     const int q = 2 * a + b;
                     cxy[q] = xy;
                     cX[q] = X;
-                    if (xb == ibits && yb == jbits && xin && (unsigned)Y < (unsigned)D) valid |= 1u << q;
+                    if (xb == ibits && yb == jbits && xin && yin[b]) valid |= 1u << q;
                 }
             }
             while (valid) {
