@@ -1100,7 +1100,10 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
                     if (xb == ibits && yb == jbits && xin && yin[b]) valid |= 1u << q;
                 }
             }
-            while (valid) {
+            // a unit square holds at most two samples: two passes, then (never seen, but kept
+            // for float-rounded coordinates at the square's corners) any further ones
+#pragma unroll 2
+            for (int pass = 0; valid != 0; ++pass) {
                 const int q = __ffs(valid) - 1;
                 valid &= valid - 1;
                 const f2x xy = q == 0 ? cxy[0] : q == 1 ? cxy[1] : q == 2 ? cxy[2] : cxy[3];
