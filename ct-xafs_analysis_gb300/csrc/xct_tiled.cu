@@ -326,13 +326,6 @@ struct FwdMsTile {
     static_assert(Smem <= 227u * 1024u, "eight-slice tile exceeds shared memory");
 };
 
-__device__ __forceinline__ float4 lds_f4(unsigned addr)
-{
-    float4 v;
-    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
-    return v;
-}
-
 // float -> double for the accumulator without the FP64 pipe (GB300 runs FP64 at a small
 // fraction of the FP32 rate): normal numbers and zero by re-biasing the exponent in integer
 // arithmetic, the rare others through the conversion instruction.
@@ -375,9 +368,10 @@ __global__ void __launch_bounds__(kMsThreads, 1) fwd_ms_kernel(const float *__re
                                                                const float2 *__restrict__ trig, KGeom g, int sub,
                                                                int step, int nrows, int ntx, int chunk)
 {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    float4 *tile = reinterpret_cast<float4 *>(smem_raw);
-    float2 *scs = reinterpret_cast<float2 *>(smem_raw + FwdMsTile<T>::TileBytes);
+    // 128-byte records, read with 128-bit loads
+    extern __shared__ __align__(128) unsigned char ms_smem[];
+    float4 *tile = reinterpret_cast<float4 *>(ms_smem);
+    float2 *scs = reinterpret_cast<float2 *>(ms_smem + FwdMsTile<T>::TileBytes);
     float2 *inv_s = scs + kAngChunk;
     int *xlo_s = reinterpret_cast<int *>(inv_s + kAngChunk);
     int *xhi_s = xlo_s + kAngChunk;
