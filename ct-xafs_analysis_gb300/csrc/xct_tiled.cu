@@ -973,7 +973,8 @@ __global__ void __launch_bounds__(kThreads) adj_ms_kernel(const float *__restric
 // detector and the index within [0, D).  A CTA of 512 threads owns 32 x 16 base texels and
 // writes the 31 x 15 texels whose four base texels it holds, texel (i, j) = A00(i, j) +
 // A10(i-1, j) + A01(i, j-1) + A11(i-1, j-1), after staging the four parts in shared memory.
-// The rays' values of 16 angles at a time are staged per slice by asynchronous copies.
+// The rays' values of 16 angles at a time are staged by asynchronous copies into one of two
+// windows: the next chunk's copies run while this chunk is accumulated.
 // Float sums in angle order: deterministic, and no fixed-point rounding.
 constexpr int kAdjGBX = 32, kAdjGBY = 16;            // base texels per CTA
 constexpr int kAdjGThreads = kAdjGBX * kAdjGBY;      // one per base texel
@@ -981,11 +982,13 @@ constexpr int kAdjGW = 44;                           // staged rays per angle
 constexpr int kAdjGChunk = 16;                       // angles per staging pass
 template <int S>
 struct AdjG {
-    // window: [slice pair][angle][ray] of float2; parts: [corner][slice][thread]
+    // two windows: [slice pair][angle][ray] of float2; parts: [corner][slice][thread];
+    // three slots of (cos, sin) and first staged ray per angle
     static constexpr unsigned PairBytes = (unsigned)(kAdjGChunk * kAdjGW * 8);
-    static constexpr size_t WinBytes = (size_t)(S / 2) * PairBytes;
+    static constexpr unsigned WinBytes = (unsigned)(S / 2) * PairBytes;
     static constexpr size_t CombBytes = (size_t)4 * S * kAdjGThreads * 4;
-    static constexpr size_t Smem = (WinBytes > CombBytes ? WinBytes : CombBytes) + kAdjGChunk * 16;
+    static constexpr size_t SlotBytes = (size_t)3 * kAdjGChunk * 12;
+    static constexpr size_t Smem = (2 * (size_t)WinBytes > CombBytes ? 2 * (size_t)WinBytes : CombBytes) + SlotBytes;
 };
 
 __device__ __forceinline__ f2x lds_f2x(unsigned addr)
@@ -1006,8 +1009,8 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
     constexpr int P = S / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *part = reinterpret_cast<float *>(smem_raw);  // the window, later the parts
-    float2 *scs = reinterpret_cast<float2 *>(smem_raw + AdjG<S>::Smem - kAdjGChunk * 16);
-    int *sxw = reinterpret_cast<int *>(scs + kAdjGChunk);
+    float2 *scs = reinterpret_cast<float2 *>(smem_raw + AdjG<S>::Smem - AdjG<S>::SlotBytes);
+    int *sxw = reinterpret_cast<int *>(scs + 3 * kAdjGChunk);
     const int tx = threadIdx.x % kAdjGBX, ty = threadIdx.x / kAdjGBX;
     const int bx = (int)blockIdx.x % ntx, by = (int)blockIdx.x / ntx;
     const int z0 = (int)blockIdx.z * S;
@@ -1029,40 +1032,65 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
 #pragma unroll
         for (int h = 0; h < P; ++h) acc[q][h] = 0ull;
 
-    for (int k0 = 0; k0 < nang; k0 += kAdjGChunk) {
-        const int kn = min(kAdjGChunk, nang - k0);
-        __syncthreads();  // the previous chunk's reads are done
-        for (int k = threadIdx.x; k < kn; k += kAdjGThreads) {
-            const float2 cs = trig[sub + (k0 + k) * step];
-            scs[k] = cs;
-            // rays whose lattice coordinate meets the block's base squares
-            float umin = 3.0e38f;
+    // Software pipeline over chunks of 16 angles: the rays of chunk ch + 1 are copied into the
+    // other window while chunk ch is accumulated; the angles' (cos, sin) and first staged ray
+    // sit in three slots (chunks ch, ch + 1, ch + 2), the (cos, sin) of chunk ch + 3 in the
+    // registers of threads 0..15.
+    const int nch = (nang + kAdjGChunk - 1) / kAdjGChunk;
+    auto trig_of = [&](int ch) -> float2 {
+        const int a = ch * kAdjGChunk + (int)threadIdx.x;
+        return (ch < nch && (int)threadIdx.x < kAdjGChunk && a < nang) ? __ldg(trig + sub + a * step)
+                                                                        : make_float2(0.0f, 0.0f);
+    };
+    auto prep = [&](int ch, float2 cs) {
+        if (ch >= nch || (int)threadIdx.x >= kAdjGChunk) return;
+        const int at = (ch % 3) * kAdjGChunk + (int)threadIdx.x;
+        scs[at] = cs;
+        // rays whose lattice coordinate meets the block's base squares
+        float umin = 3.0e38f;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float px_ = (float)(bi0 + ((q & 1) ? kAdjGBX : 0)) - g.hx;
-                const float py_ = (float)(bj0 + ((q & 2) ? kAdjGBY : 0)) - g.hy;
-                umin = fminf(umin, px_ * cs.x - py_ * cs.y + g.cx);
-            }
-            sxw[k] = (int)floorf(umin) - 2;
+        for (int q = 0; q < 4; ++q) {
+            const float px_ = (float)(bi0 + ((q & 1) ? kAdjGBX : 0)) - g.hx;
+            const float py_ = (float)(bj0 + ((q & 2) ? kAdjGBY : 0)) - g.hy;
+            umin = fminf(umin, px_ * cs.x - py_ * cs.y + g.cx);
         }
-        __syncthreads();
-        // window (pair p, angle k, ray sxw[k] + r) = (slice 2p, slice 2p + 1), 0 off the detector
+        sxw[at] = (int)floorf(umin) - 2;
+    };
+    // window (pair p, angle k, ray sxw + r) = (slice 2p, slice 2p + 1), 0 off the detector
+    auto stage = [&](int ch) {
+        if (ch >= nch) return;
+        const int k0 = ch * kAdjGChunk, kn = min(kAdjGChunk, nang - k0), sl = (ch % 3) * kAdjGChunk;
+        const unsigned wb = wbase + (unsigned)(ch & 1) * AdjG<S>::WinBytes;
         for (int e = threadIdx.x; e < kn * S * kAdjGW; e += kAdjGThreads) {
             const int r = e % kAdjGW, t2 = e / kAdjGW;
             const int z = t2 % S, k = t2 / S;
-            const int X = sxw[k] + r;
+            const int X = sxw[sl + k] + r;
             const float *row = sz + (size_t)z * nprj + (size_t)(sub + (k0 + k) * step) * g.px;
             const bool in = (unsigned)X < (unsigned)g.px;
-            const unsigned dst = wbase + (unsigned)(z >> 1) * AdjG<S>::PairBytes + 8u * (unsigned)(k * kAdjGW + r) +
+            const unsigned dst = wb + (unsigned)(z >> 1) * AdjG<S>::PairBytes + 8u * (unsigned)(k * kAdjGW + r) +
                                  4u * (unsigned)(z & 1);
             cp_async4(dst, in ? (const void *)(row + X) : (const void *)row, in ? 4u : 0u);
         }
+    };
+    prep(0, trig_of(0));
+    prep(1, trig_of(1));
+    float2 csr = trig_of(2);
+    __syncthreads();
+    stage(0);
+    for (int ch = 0; ch < nch; ++ch) {
+        // this chunk's copies have landed; every thread is past chunk ch - 1, whose window
+        // and slot are reused below
         cp_async_wait_all();
         __syncthreads();
+        prep(ch + 2, csr);
+        csr = trig_of(ch + 3);
+        stage(ch + 1);
+        const int k0 = ch * kAdjGChunk, kn = min(kAdjGChunk, nang - k0), sl = (ch % 3) * kAdjGChunk;
+        const unsigned wb = wbase + (unsigned)(ch & 1) * AdjG<S>::WinBytes;
         for (int k = 0; k < kn; ++k) {
-            const float c = scs[k].x, s = scs[k].y;
+            const float c = scs[sl + k].x, s = scs[sl + k].y;
             const f2x cs2 = f2_pack(c, -s), sc2 = f2_pack(s, c);
-            const unsigned wk = wbase + 8u * (unsigned)(k * kAdjGW - sxw[k]);
+            const unsigned wk = wb + 8u * (unsigned)(k * kAdjGW - sxw[sl + k]);
             // the candidates: rays Xa, Xa + 1 (lattice coordinate of the cell centre u0 - 0.717
             // and up); on each, indices Ya, Ya + 1 (the centre's coordinate along the rays, w0,
             // is the same on every ray)
@@ -1110,7 +1138,7 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
                 f2_unpack(gr, gx, gy);
                 const float w[4] = {gx * gy, fx * gy, gx * fy, fx * fy};
                 const unsigned ad = wk + 8u * (unsigned)X;
-                if (!XCT_IN(ad, wbase, wbase + AdjG<S>::WinBytes - 8, XCT_SITE_ADJ)) continue;
+                if (!XCT_IN(ad, wb, wb + AdjG<S>::WinBytes - 8, XCT_SITE_ADJ)) continue;
                 f2x v[P];
 #pragma unroll
                 for (int h = 0; h < P; ++h) v[h] = lds_f2x(ad + (unsigned)h * AdjG<S>::PairBytes);
