@@ -762,7 +762,10 @@ def profile_case_operators(n=8):
     """Small case for profilers, the operator pair and FBP: the forward projection, the exact
     adjoint and the FBP of n slices of the workload over all 1500 angles, each once (the
     slice-interleaved forward projector, the gather adjoint and the eight-slice FBP
-    backprojector for n = 8).  ~0.5 GB on the device."""
+    backprojector for n = 8; for n = 10 the adjoint is one ten-slice gather).  ~0.5 GB on
+    the device."""
+    if not 1 <= n <= 16:
+        raise SystemExit("--profile-slices must be within 1..16")
     import torch
     import xct
     from xct import phantom
@@ -835,6 +838,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-slices", type=int, default=8,
+                    help="slices of the 'operators' profiling case (8: the eight-slice kernels; 10: the "
+                         "benchmark's batch, the ten-slice gather adjoint)")
     ap.add_argument("--profile-case", nargs="?", const="osem", choices=["osem", "slices", "next", "operators", "ctxafs"],
                     help="run a small profiling case and exit: osem (one slice, one OS-EM iteration), slices "
                          "(eight slices, one OS-EM iteration, slice-interleaved kernels), next (the components "
@@ -851,7 +857,7 @@ def main():
         profile_case_next()
         return
     if args.profile_case == "operators":
-        profile_case_operators()
+        profile_case_operators(args.profile_slices)
         return
     if args.profile_case == "ctxafs":
         profile_case_ctxafs()
