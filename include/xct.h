@@ -248,11 +248,12 @@ int xct_osem2(xct_plan *plan, int dN, int sub, float *d_img, const float *d_rati
  * xct_bp_ref : the reference plain backprojector `backProjection`
  *              (reconstShare.cl:245-275) with ss = 1, sub = 0 (all angles).
  * xct_adj    : the exact adjoint A^T of xct_fwd (d_img = A^T d_sino): the same samples
- *              and bilinear weights, scattered.  Per window of 8 angles, the rays within
- *              2^6 of the window's largest |value| are summed as fixed-point integers (each
- *              contribution rounded by at most 2^-16 of its ray's value); smaller rays, and
- *              windows holding a NaN or an infinity, use float atomics.  Results repeat bit
- *              for bit when every window takes the integer path only.                      */
+ *              and bilinear weights (groups of slices: see the slice-interleaved kernels
+ *              below).  One slice at a time they are scattered: per window of 8 angles,
+ *              the rays within 2^6 of the window's largest |value| are summed as fixed-point
+ *              integers (each contribution rounded by at most 2^-16 of its ray's value);
+ *              smaller rays, and windows holding a NaN or an infinity, use float atomics.
+ *              Results repeat bit for bit when every window takes the integer path only. */
 int xct_fwd(xct_plan *plan, int dN, const float *d_img, float *d_sino, void *stream);
 int xct_bp_ref(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
 int xct_adj(xct_plan *plan, int dN, const float *d_sino, float *d_img, void *stream);
@@ -411,11 +412,17 @@ int xct_batch_plan_tuning(xct_batch_plan *plan, int *fwd_tile, int *ang_chunk);
  *    in a rotated order (no shared-memory bank conflict; a sample's coordinates are found once
  *    for all eight).  Results agree with the per-slice kernel to float rounding of the partial
  *    ray sums;
- *  - backprojection + update (OSEM2) in groups of eight: one bin expression per eight gathers;
- *    bit-identical to the per-slice kernel;
- *  - the exact adjoint (xct_adj and the FISTA adjoint step) in groups of four: each sample's
- *    coordinates and weights serve the four slices; identical to the per-slice kernel where
- *    its fixed-point path applies, else to float rounding.
+ *  - backprojection + update (OSEM2) in groups of eight, and a pair left over in a two-slice
+ *    form: one bin expression per eight (two) gathers; bit-identical to the per-slice kernel;
+ *    the FBP backprojection (xct_fbp_backproject, the FBP and hybrid runs) the same way, also
+ *    bit-identical;
+ *  - the exact adjoint (xct_adj and the FISTA adjoint step) in groups of ten or eight as a
+ *    gather: a thread owns one base texel, finds the samples whose base texel it is with the
+ *    forward projector's own arithmetic and sums their weighted ray values in registers (no
+ *    atomics; float sums in an order fixed by the geometry, so repeatable bit for bit); a
+ *    group of four left over in scatter form, each sample's coordinates and weights serving
+ *    the four slices.  Both agree with the per-slice kernel to float rounding (the scatter
+ *    form exactly where its fixed-point path applies).
  * With it on, a call's slices go in groups through these kernels and the rest through the
  * per-slice ones, and a call that runs as two halves cuts them at a multiple of eight.  The
  * value is the number of subset angles one forward CTA serves (1..128); 0 turns all three
