@@ -24,8 +24,13 @@ Metric: slice-iterations per second (one slice through all 15 subsets once).
                     (widths 512-2048, 360-1200 angles with drops) in one autotuned batch
                     plan, against one call per item (plain and tiled kernels) on a sample
                     scaled by work;
+  ctxafs_grouped -- the CT-XAFS stack with whole energies: 4 energies x 64 slices = 256
+                    items, the 16 slices of one width at one energy sharing a geometry, so
+                    every item is in a geometry group (single-shape plans, slice-interleaved
+                    kernels); against the same plan with groups off (the graph of
+                    persistent launches) and one call per item;
   uniform_batch  -- 16 slices of the per-slice workload through one batch plan: its uniform
-                    route (single-shape plan) against its graph of persistent launches;
+                    route (one geometry group) against its graph of persistent launches;
   parity         -- slice 0 of the timed region against the oracle's full 15 x 4 OS-EM of
                     the same sinogram (rel-L2 and max-abs of peak; the bar 1e-4 / 1e-3);
   small_256      -- the 256^2 workload (180 angles, 10 subsets x 5 it): the GPU at one and at
@@ -370,14 +375,17 @@ def ctxafs_stack_specs(n_energy, n_slices, seed=3, widths=(512, 1024, 1536, 2048
     return [int(w) for w in ws], angs, grids
 
 
-def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
+def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32, compare_graph=False):
     """The CT-XAFS stack at scale: n_energy x n_slices uneven items (widths 512-2048 with
     matching bins, 360-1200 angles with 0-10 % dropped per energy), each slice a two-spectrum
     XANES mixture at its energy, Poisson I0 = 1e5; 10 subsets x 5 iterations.  One autotuned
-    batch plan (graph of persistent launches over a device work queue) reconstructs all
-    items; the per-slice paths (one call per item, plain and tiled kernels) run on a seeded
-    sample of `sample` items and are scaled by the work they did (sum of rays x angles)
-    to the whole stack.  Device-resident inputs, CUDA-event timing."""
+    batch plan reconstructs all items: the slices of one width at one energy share their
+    geometry, and where eight or more do they form a geometry group (a single-shape plan,
+    slice-interleaved kernels); the graph of persistent launches over a device work queue
+    serves the rest.  With compare_graph the same plan also runs with groups off (the graph
+    serving every item).  The per-slice paths (one call per item, plain and tiled kernels)
+    run on a seeded sample of `sample` items and are scaled by the work they did (sum of
+    rays x angles) to the whole stack.  Device-resident inputs, CUDA-event timing."""
     import torch
     import xct
     from xct import phantom
@@ -431,7 +439,7 @@ def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
     t_tune = time.perf_counter()
     res["tuning"] = dict(zip(("fwd_tile", "ang_chunk"), bp.autotune()))
     res["autotune_s"] = time.perf_counter() - t_tune
-    res["route"] = "uniform" if bp.uniform() else "graph"
+    res["groups"], res["grouped_items"] = bp.groups()
     imgs = [torch.ones((w, w), device="cuda") for w, _ in shapes]
 
     def run_batched():
@@ -443,6 +451,19 @@ def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
     ms = timed(run_batched, reps=1)
     res["batched"] = {"value": n_items * it / (ms * 1e-3), "items_per_s": n_items / (ms * 1e-3), "ms": ms,
                       "launches_per_run": (xct.launch_count() - l0) // 2}
+    if compare_graph:
+        kept = [x.clone() for x in imgs]
+        bp.set_grouping(False)
+        ms_g = timed(run_batched, reps=1)
+        bp.set_grouping(True)
+        res["graph_only"] = {"value": n_items * it / (ms_g * 1e-3), "items_per_s": n_items / (ms_g * 1e-3),
+                             "ms": ms_g}
+        res["grouped_over_graph"] = ms_g / ms
+        num = sum(float((a.double() - b.double()).pow(2).sum()) for a, b in zip(kept, imgs))
+        den = sum(float(b.double().pow(2).sum()) for b in imgs)
+        res["rel_l2_grouped_vs_graph"] = (num / den) ** 0.5
+        del kept
+        run_batched()  # the images as the grouped run leaves them, for the comparisons below
     rng = np.random.default_rng(7)
     samp = np.sort(rng.choice(n_items, min(sample, n_items), replace=False))
     frac = work[samp].sum() / work.sum()
@@ -473,6 +494,8 @@ def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32):
             res["rel_l2_batched_vs_per_slice"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
     bp.close()
     res["batched_over_plain"] = res["batched"]["value"] / res["per_slice_plain"]["value"]
+    if compare_graph:
+        res["graph_only_over_plain"] = res["graph_only"]["value"] / res["per_slice_plain"]["value"]
     res["batched_over_tiled_per_slice"] = res["batched"]["value"] / res["per_slice_tiled"]["value"]
     # the batched run against the FP32 roofline: algorithmic FLOPs of every item (12 per
     # forward tap, 5 per backprojection gather, 4 per pixel update and subset; the per-angle
@@ -511,6 +534,8 @@ def uniform_batch(ctx, sino, n=16, reps=2):
     sl = [sino[z] for z in range(n)]
     out = {"slices": n, "slices_per_call": bp.uniform()}
     for name, imgs in (("uniform_route", [arr[z] for z in range(n)]), ("graph", sep)):
+        bp.set_grouping(name == "uniform_route")
+
         def run():
             for x in imgs:
                 x.fill_(1.0)
@@ -986,6 +1011,12 @@ def main():
     except Exception as e:  # reported, never fatal
         batched = {"error": str(e)[:300]}
 
+    # ---- CT-XAFS stack with whole energies: the slices of one width share a geometry ----
+    try:
+        grouped = ctxafs_batched(ctx, n_energy=4, n_slices=64, sample=16, compare_graph=True)
+    except Exception as e:  # reported, never fatal
+        grouped = {"error": str(e)[:300]}
+
     # ---- a uniform batch through the batch plan: its uniform route against its graph ----
     try:
         uniform = uniform_batch(ctx, sino)
@@ -1108,7 +1139,7 @@ def main():
                        "l2": "inputs larger than L2 (each step a new 290 MB batch)",
                        "parallelism": "dp%d over slices" % world},
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "per_slice": per_slice,
-            "ctxafs_batched": batched, "uniform_batch": uniform, "small_256": small, "volume_stream": volume, "next_components": nxt,
+            "ctxafs_batched": batched, "ctxafs_grouped": grouped, "uniform_batch": uniform, "small_256": small, "volume_stream": volume, "next_components": nxt,
             "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "finite": finite,
             "launches_per_step": launches / max(args.steps, 1),
             # library launches before the timed region: the skip count that makes an ncu launch

@@ -10,8 +10,15 @@
 // loop is captured once in a CUDA graph and replayed; the slices' buffer pointers live in a
 // device descriptor table written before each replay, so one plan serves any buffers of
 // the planned shapes.
+//
+// Slices that share one geometry (sizes, centre, modes, angle list) -- in a CT-XAFS stack the
+// slices of one width at one energy -- form a group; a group of at least eight runs through
+// a single-shape plan of its own (the slice-interleaved kernels, two halves of up to eight
+// slices per call on two streams), its slices copied into one contiguous scratch pair when
+// the caller's buffers are not already consecutive.  The graph serves the other slices.
 #include <math.h>
 #include <stdio.h>
+#include <string.h>
 
 #include <algorithm>
 #include <new>
@@ -26,7 +33,7 @@ struct xct_batch_plan {
     std::vector<int> sub;             // subset order (GPU.cpp:564-582)
     std::vector<XctItemDev> host;     // descriptors (pointers filled per run)
     XctItemDev *d_items = nullptr;
-    int *d_bases = nullptr;           // [3][n+1]
+    int *d_bases = nullptr;           // [3][m+1] over the graph's m slices
     int *d_queues = nullptr;          // [it*ss][3]
     float2 *d_trig = nullptr;
     float *d_ratio = nullptr;
@@ -51,10 +58,22 @@ struct xct_batch_plan {
     float *d_cs = nullptr;            // w, beta, x' of every stack
     long long max_vox = 0;
     float cs_lambda = 0.0f;           // the kernels' lambda
-    // uniform batches (every slice one geometry): a single-shape plan that runs them
-    // uni_batch at a time through the slice-interleaved forward projector
-    xct_plan *uni = nullptr;
-    int uni_batch = 0;
+    // geometry groups (at least kGroupMin slices of one geometry): a single-shape plan each,
+    // `batch` slices per call; the graph serves `glist` -- every slice, or with groups in use
+    // the slices of no group (`rest`)
+    struct Group {
+        xct_plan *plan = nullptr;
+        int batch = 0;
+        std::vector<int> items;
+        size_t nprj = 0, nimg = 0;
+    };
+    std::vector<Group> groups;
+    std::vector<int> rest;
+    bool grouping = true;          // xct_batch_plan_set_grouping
+    float *d_gscratch = nullptr;   // [batch][pa][px] sinograms then [batch][ny][nx] images
+    std::vector<int> glist;        // the graph's slices, in descriptor order
+    std::vector<XctItemDev> gdesc; // their descriptors
+    bool glist_corr = false;       // some slice of the graph has a sinogram correction
 };
 
 static void batch_free(xct_batch_plan *p)
@@ -72,32 +91,38 @@ static void batch_free(xct_batch_plan *p)
     cudaFree(p->d_corr_fac);
     cudaFree(p->d_stacks);
     cudaFree(p->d_cs);
-    if (p->uni) xct_osem_plan_destroy(p->uni);
+    cudaFree(p->d_gscratch);
+    for (auto &G : p->groups)
+        if (G.plan) xct_osem_plan_destroy(G.plan);
     delete p;
 }
 
-// Forward tiles (T, chunk) for every slice: work units, their prefix sums (uploaded), the
-// persistent grids; a captured graph is dropped (the next run captures again).
+// Forward tiles (T, chunk) for every slice: work units, their prefix sums over the graph's
+// slices (uploaded), the persistent grids; a captured graph is dropped (the next run
+// captures again).
 static int batch_layout(xct_batch_plan *p, int T, int chunk)
 {
-    const int n = p->n;
-    p->bases.assign(3 * (size_t)(n + 1), 0);
-    for (int i = 0; i < n; ++i) {
+    std::vector<int> units(3 * p->host.size());  // forward, finalize, backprojection units
+    for (size_t i = 0; i < p->host.size(); ++i) {
         XctItemDev &d = p->host[i];
         d.g.fwd_T = T;
         d.g.fwd_chunk = chunk;
-        int fu, fin, bu;
-        xct_batched_units(d.g, d.fwd_ntx, d.fwd_nty, fu, fin, d.bp_ntx, bu);
-        p->bases[0 * (n + 1) + i + 1] = p->bases[0 * (n + 1) + i] + fu;
-        p->bases[1 * (n + 1) + i + 1] = p->bases[1 * (n + 1) + i] + fin;
-        p->bases[2 * (n + 1) + i + 1] = p->bases[2 * (n + 1) + i] + bu;
+        xct_batched_units(d.g, d.fwd_ntx, d.fwd_nty, units[3 * i], units[3 * i + 1], d.bp_ntx, units[3 * i + 2]);
+    }
+    const int m = (int)p->glist.size();
+    p->bases.assign(3 * (size_t)(m + 1), 0);
+    p->glist_corr = false;
+    for (int j = 0; j < m; ++j) {
+        const int i = p->glist[j];
+        for (int q = 0; q < 3; ++q) p->bases[q * (m + 1) + j + 1] = p->bases[q * (m + 1) + j] + units[3 * i + q];
+        p->glist_corr = p->glist_corr || p->host[i].corr_mode > 0;
     }
     XCT_CUDA_TRY(cudaMemcpy(p->d_bases, p->bases.data(), sizeof(int) * p->bases.size(), cudaMemcpyHostToDevice));
     int rc = xct_batched_grids(p->ctx->device, p->ctx->sm_count, T, p->grids);
     if (rc) return rc;
     // the finalize step runs one CTA per unit (ratio row) rather than a persistent grid: its
     // units are short, so a device queue's per-unit latency would dominate
-    p->grids[1] = p->bases[1 * (n + 1) + n];
+    p->grids[1] = p->bases[1 * (m + 1) + m];
     p->fwd_T = T;
     p->fwd_chunk = chunk;
     if (p->exec) {
@@ -118,9 +143,55 @@ static bool same_geom(const xct_geom &a, const xct_geom &b)
            std::equal(a.angles_deg, a.angles_deg + a.pa, b.angles_deg);
 }
 
-// Slices per call of the uniform route: two halves of whole slice groups of the
-// slice-interleaved forward projector when the batch has them.
-static int uniform_batch(int n) { return std::min(n, 2 * fwd_ms_slices()); }
+// A geometry group needs whole slice groups of the slice-interleaved forward projector;
+// its calls take two halves of up to that many slices.
+static const int kGroupMin = XCT_MULTISLICE_SLICES;
+static int group_batch(int n) { return std::min(n, 2 * XCT_MULTISLICE_SLICES); }
+
+// FNV-1a over a geometry's fields and angle bits: equal geometries hash alike.
+static unsigned long long geom_hash(const xct_geom &g)
+{
+    unsigned long long h = 1469598103934665603ull;
+    auto mix = [&](unsigned v) {
+        h ^= v;
+        h *= 1099511628211ull;
+    };
+    const float c = g.center_bin < 0.0f ? (float)g.px * 0.5f : g.center_bin;
+    unsigned cb;
+    memcpy(&cb, &c, 4);
+    const int v[9] = {g.nx, g.ny, g.px, g.pa, g.ss, g.measured_fetch_mode, g.subset_mode, g.correction_mode, (int)cb};
+    for (int q = 0; q < 9; ++q) mix((unsigned)v[q]);
+    for (int a = 0; a < g.pa; ++a) {
+        unsigned b;
+        memcpy(&b, &g.angles_deg[a], 4);
+        mix(b);
+    }
+    return h;
+}
+
+static std::vector<int> all_items(int n)
+{
+    std::vector<int> v(n);
+    for (int i = 0; i < n; ++i) v[i] = i;
+    return v;
+}
+
+// Tune-cache key of the graph's slices (their shapes, in order).
+static std::string graph_key(const xct_batch_plan *p)
+{
+    unsigned long long h = 1469598103934665603ull;  // FNV-1a over the shapes
+    for (int i : p->glist) {
+        const KGeom &g = p->host[i].g;
+        const int v[6] = {g.nx, g.ny, g.px, g.pa, p->host[i].cover ? 1 : 0, 0};
+        for (int q = 0; q < 6; ++q) {
+            h ^= (unsigned)v[q];
+            h *= 1099511628211ull;
+        }
+    }
+    char kb[96];
+    snprintf(kb, sizeof kb, "batch%d-%016llx", (int)p->glist.size(), h);
+    return xct_tune_key(p->ctx->name, 0, 0, 0, 0, p->ss, (int)p->glist.size()) + "|" + kb;
+}
 
 extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms, int it, xct_batch_plan **out)
 {
@@ -232,23 +303,71 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         orat += (size_t)g.pa * g.px;
         oacc += (size_t)((g.pa + g.ss - 1) / g.ss) * g.px;
     }
-    // forward tiles: this batch's cached choice, else the default rule
-    unsigned long long h = 1469598103934665603ull;  // FNV-1a over the shapes
-    for (int i = 0; i < n; ++i) {
-        const int v[6] = {geoms[i].nx, geoms[i].ny, geoms[i].px, geoms[i].pa, geoms[i].subset_mode, 0};
-        for (int q = 0; q < 6; ++q) {
-            h ^= (unsigned)v[q];
-            h *= 1099511628211ull;
+    // geometry groups: slices of one geometry, found through a hash of the geometry and
+    // checked member by member
+    {
+        std::vector<std::pair<unsigned long long, int>> hs(n);
+        for (int i = 0; i < n; ++i) hs[i] = {geom_hash(geoms[i]), i};
+        std::stable_sort(hs.begin(), hs.end());
+        std::vector<char> taken(n, 0);
+        for (size_t a0 = 0; a0 < hs.size();) {
+            size_t a1 = a0;
+            while (a1 < hs.size() && hs[a1].first == hs[a0].first) ++a1;
+            for (size_t u = a0; u < a1; ++u) {
+                const int i = hs[u].second;
+                if (taken[i]) continue;
+                std::vector<int> members{i};
+                taken[i] = 1;
+                for (size_t v = u + 1; v < a1; ++v) {
+                    const int j = hs[v].second;
+                    if (!taken[j] && same_geom(geoms[i], geoms[j])) {
+                        members.push_back(j);
+                        taken[j] = 1;
+                    }
+                }
+                std::sort(members.begin(), members.end());
+                if ((int)members.size() >= kGroupMin) {
+                    xct_batch_plan::Group G;
+                    G.items = members;
+                    p->groups.push_back(std::move(G));
+                } else {
+                    p->rest.insert(p->rest.end(), members.begin(), members.end());
+                }
+            }
+            a0 = a1;
         }
+        std::sort(p->rest.begin(), p->rest.end());
+        std::sort(p->groups.begin(), p->groups.end(),
+                  [](const xct_batch_plan::Group &x, const xct_batch_plan::Group &y) { return x.items[0] < y.items[0]; });
     }
-    char kb[96];
-    snprintf(kb, sizeof kb, "batch%d-%016llx", n, h);
-    p->key = xct_tune_key(ctx->name, 0, 0, 0, 0, ss, n) + "|" + kb;
+    size_t scratch = 0;
+    for (auto &G : p->groups) {
+        xct_geom g = geoms[G.items[0]];
+        g.it = it;
+        g.max_batch = group_batch((int)G.items.size());
+        g.kernels = XCT_KERNELS_TILED;
+        int rc = xct_osem_plan_create(ctx, &g, &G.plan);
+        if (rc) {
+            batch_free(p);
+            return rc;
+        }
+        G.batch = g.max_batch;
+        G.nprj = (size_t)g.pa * g.px;
+        G.nimg = (size_t)g.nx * g.ny;
+        scratch = std::max(scratch, (size_t)G.batch * (G.nprj + G.nimg));
+    }
+    if (scratch > 0 && (e = cudaMalloc(&p->d_gscratch, sizeof(float) * scratch)) != cudaSuccess)
+        return fail(e, "cudaMalloc group scratch");
+    // the graph's slices with groups in use (every slice when all are grouped: the graph
+    // then serves them only with groups off), its tiles: this list's cached choice, else the
+    // default rule
+    p->glist = p->rest.empty() ? all_items(n) : p->rest;
+    p->key = graph_key(p);
     TuneChoice c;
     if (!xct_tune_lookup(p->key, xct_tune_env_path(), c))
         c = xct_tune_default(ctx->sm_count, [&](int T, int ch) {
             long long t = 0;
-            for (int i = 0; i < n; ++i) {
+            for (int i : p->glist) {
                 const int rows = (geoms[i].pa + ss - 1) / ss;
                 t += (long long)((geoms[i].nx + T) / T) * ((geoms[i].ny + T) / T) * ((rows + ch - 1) / ch);
             }
@@ -260,20 +379,6 @@ extern "C" int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms,
         return rc;
     }
     if ((e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
-    bool uniform = n >= 2;
-    for (int i = 1; i < n && uniform; ++i) uniform = same_geom(geoms[0], geoms[i]);
-    if (uniform) {
-        xct_geom g = geoms[0];
-        g.it = it;
-        g.max_batch = uniform_batch(n);
-        g.kernels = XCT_KERNELS_TILED;
-        rc = xct_osem_plan_create(ctx, &g, &p->uni);
-        if (rc) {
-            batch_free(p);
-            return rc;
-        }
-        p->uni_batch = g.max_batch;
-    }
     *out = p;
     return XCT_OK;
 }
@@ -300,7 +405,8 @@ static int capture(xct_batch_plan *p)
     const bool cs = ns > 0;
     cudaError_t e = cudaMemsetAsync(p->d_queues, 0, p->queue_bytes, p->cap);
     if (e != cudaSuccess) rc = xct_cuda_fail(e, "capture memset");
-    if (rc == XCT_OK && p->any_corr) rc = launch_sino_correction_batched(p->d_items, p->n, p->max_px, p->max_pa, p->cap);
+    const int m = (int)p->glist.size();
+    if (rc == XCT_OK && p->glist_corr) rc = launch_sino_correction_batched(p->d_items, m, p->max_px, p->max_pa, p->cap);
     if (rc == XCT_OK && cs) rc = launch_stack_copy(p->d_stacks, ns, p->max_vox, 1, sm, p->cap);
     bool first = true;
     for (int i = 0; i < p->it && rc == XCT_OK; ++i)
@@ -309,7 +415,7 @@ static int capture(xct_batch_plan *p)
                 rc = launch_ista3d_stacks(p->d_stacks, ns, p->max_vox, p->cs_lambda, sm, p->cap);
                 first = false;
             } else {
-                rc = launch_osem_step_batched(p->d_items, p->d_bases, p->n, p->sub[k],
+                rc = launch_osem_step_batched(p->d_items, p->d_bases, m, p->sub[k],
                                               p->d_queues + 3 * (size_t)(i * p->ss + k), p->grids, p->fwd_T, p->cap);
                 if (rc == XCT_OK && cs) rc = launch_fista3d_stacks(p->d_stacks, ns, p->max_vox, p->cs_lambda, sm, p->cap);
             }
@@ -332,21 +438,46 @@ extern "C" int xct_batch_run(xct_batch_plan *p, const float *const *d_sino, floa
     for (int i = 0; i < p->n; ++i)
         if (!d_sino[i] || !d_img[i]) return xct_fail(XCT_E_INVALID, "xct_batch_run: null slice pointer");
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
-    // uniform batch in one [n][pa][px] / [n][ny][nx] pair of arrays, no stacks: the
-    // single-shape plan, uni_batch slices per call
-    if (p->uni && p->stacks.empty()) {
-        const size_t nprj = (size_t)p->host[0].g.pa * p->host[0].g.px, nimg = (size_t)p->host[0].g.nx * p->host[0].g.ny;
-        bool contiguous = true;
-        for (int i = 1; i < p->n && contiguous; ++i)
-            contiguous = d_sino[i] == d_sino[0] + i * nprj && d_img[i] == d_img[0] + i * nimg;
-        if (contiguous) {
-            for (int off = 0; off < p->n; off += p->uni_batch) {
-                const int cnt = std::min(p->uni_batch, p->n - off);
-                int rc = xct_osem_run_device(p->uni, cnt, d_sino[off], d_img[off], nullptr, p->it, stream);
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
+    // the groups (not with compressed sensing, whose stacks the graph serves): their calls
+    // in place when a call's slices are consecutive in one pair of arrays, else through the
+    // scratch pair
+    const bool use_groups = p->grouping && p->stacks.empty() && !p->groups.empty();
+    if (use_groups) {
+        for (const auto &G : p->groups) {
+            for (size_t off = 0; off < G.items.size(); off += (size_t)G.batch) {
+                const int cnt = (int)std::min((size_t)G.batch, G.items.size() - off);
+                const int *ix = G.items.data() + off;
+                bool contiguous = true;
+                for (int j = 1; j < cnt && contiguous; ++j)
+                    contiguous = d_sino[ix[j]] == d_sino[ix[0]] + j * G.nprj && d_img[ix[j]] == d_img[ix[0]] + j * G.nimg;
+                int rc;
+                if (contiguous) {
+                    rc = xct_osem_run_device(G.plan, cnt, d_sino[ix[0]], d_img[ix[0]], nullptr, p->it, stream);
+                } else {
+                    float *gs = p->d_gscratch, *gi = p->d_gscratch + (size_t)cnt * G.nprj;
+                    for (int j = 0; j < cnt; ++j) {
+                        XCT_CUDA_TRY(cudaMemcpyAsync(gs + j * G.nprj, d_sino[ix[j]], sizeof(float) * G.nprj,
+                                                     cudaMemcpyDeviceToDevice, st));
+                        XCT_CUDA_TRY(cudaMemcpyAsync(gi + j * G.nimg, d_img[ix[j]], sizeof(float) * G.nimg,
+                                                     cudaMemcpyDeviceToDevice, st));
+                    }
+                    rc = xct_osem_run_device(G.plan, cnt, gs, gi, nullptr, p->it, stream);
+                    for (int j = 0; j < cnt && rc == XCT_OK; ++j)
+                        XCT_CUDA_TRY(cudaMemcpyAsync(d_img[ix[j]], gi + j * G.nimg, sizeof(float) * G.nimg,
+                                                     cudaMemcpyDeviceToDevice, st));
+                }
                 if (rc) return rc;
             }
-            return XCT_OK;
         }
+        if (p->rest.empty()) return XCT_OK;
+    }
+    // the graph: the slices of no group, or every slice
+    const std::vector<int> want = use_groups ? p->rest : all_items(p->n);
+    if (want != p->glist) {
+        p->glist = want;
+        int rc = batch_layout(p, p->fwd_T, p->fwd_chunk);
+        if (rc) return rc;
     }
     if (!p->exec) {
         int rc = capture(p);
@@ -363,13 +494,16 @@ extern "C" int xct_batch_run(xct_batch_plan *p, const float *const *d_sino, floa
                                 "one array");
         p->stacks[s].img = d_img[f];
     }
-    for (int i = 0; i < p->n; ++i) {
+    const int m = (int)p->glist.size();
+    p->gdesc.resize(m);
+    for (int j = 0; j < m; ++j) {
+        const int i = p->glist[j];
         p->host[i].sino_in = d_sino[i];
         p->host[i].sino = p->host[i].corr_mode > 0 ? p->host[i].corr : d_sino[i];
         p->host[i].img = d_img[i];
+        p->gdesc[j] = p->host[i];
     }
-    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
-    XCT_CUDA_TRY(cudaMemcpyAsync(p->d_items, p->host.data(), sizeof(XctItemDev) * p->n, cudaMemcpyHostToDevice, st));
+    XCT_CUDA_TRY(cudaMemcpyAsync(p->d_items, p->gdesc.data(), sizeof(XctItemDev) * m, cudaMemcpyHostToDevice, st));
     if (!p->stacks.empty())
         XCT_CUDA_TRY(cudaMemcpyAsync(p->d_stacks, p->stacks.data(), sizeof(XctStackDev) * p->stacks.size(),
                                      cudaMemcpyHostToDevice, st));
@@ -377,7 +511,7 @@ extern "C" int xct_batch_run(xct_batch_plan *p, const float *const *d_sino, floa
     // three per OS-EM step (the first step has none with compressed sensing), the
     // correction, and with compressed sensing the setup copy plus two per step
     const long long steps = (long long)p->it * p->ss, cs = p->stacks.empty() ? 0 : 1;
-    g_xct_launches.fetch_add(3 * (steps - cs) + (p->any_corr ? (p->n + 65534) / 65535 : 0) + cs * (1 + 2 * steps),
+    g_xct_launches.fetch_add(3 * (steps - cs) + (p->glist_corr ? (m + 65534) / 65535 : 0) + cs * (1 + 2 * steps),
                              std::memory_order_relaxed);
     return XCT_OK;
 }
@@ -455,12 +589,30 @@ extern "C" int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, 
     return rc;
 }
 
-// Slices per call of the uniform route (0: the batch is not uniform; it always runs as the
-// graph of persistent launches).
+// Slices per call of the uniform route: every slice in one geometry group (0: not so).
 extern "C" int xct_batch_plan_uniform(xct_batch_plan *p, int *slices_per_call)
 {
     if (!p || !slices_per_call) return xct_fail(XCT_E_INVALID, "xct_batch_plan_uniform: null argument");
-    *slices_per_call = p->uni ? p->uni_batch : 0;
+    const bool uni = p->groups.size() == 1 && (int)p->groups[0].items.size() == p->n;
+    *slices_per_call = uni ? p->groups[0].batch : 0;
+    return XCT_OK;
+}
+
+// The geometry groups: how many, and how many slices they hold.
+extern "C" int xct_batch_plan_groups(xct_batch_plan *p, int *ngroups, int *grouped_slices)
+{
+    if (!p || !ngroups || !grouped_slices) return xct_fail(XCT_E_INVALID, "xct_batch_plan_groups: null argument");
+    *ngroups = (int)p->groups.size();
+    *grouped_slices = p->n - (int)p->rest.size();
+    return XCT_OK;
+}
+
+// Groups on (1, the default) or off (0: the graph serves every slice).
+extern "C" int xct_batch_plan_set_grouping(xct_batch_plan *p, int on)
+{
+    if (!p) return xct_fail(XCT_E_INVALID, "xct_batch_plan_set_grouping: plan is null");
+    if (on != 0 && on != 1) return xct_fail(XCT_E_INVALID, "xct_batch_plan_set_grouping: on must be 0 or 1");
+    p->grouping = on != 0;
     return XCT_OK;
 }
 
@@ -480,24 +632,36 @@ extern "C" int xct_batch_plan_autotune(xct_batch_plan *p, const char *cache_path
     XCT_RANGE("xct_batch_plan_autotune");
     if (!p) return xct_fail(XCT_E_INVALID, "xct_batch_plan_autotune: plan is null");
     if (!cache_path) cache_path = xct_tune_env_path();
-    if (p->uni) {  // the uniform route's own tiles
-        int rc = xct_plan_autotune(p->uni, p->uni_batch, cache_path, flags, stream);
+    for (auto &G : p->groups) {  // the groups' own tiles
+        int rc = xct_plan_autotune(G.plan, G.batch, cache_path, flags, stream);
         if (rc) return rc;
     }
+    // the graph's tiles, for the slices it serves as the plan stands (every slice when all
+    // are grouped: the graph then serves them only with groups off)
+    const bool use_groups = p->grouping && p->stacks.empty() && !p->groups.empty();
+    const std::vector<int> want = use_groups && !p->rest.empty() ? p->rest : all_items(p->n);
+    if (want != p->glist) {
+        p->glist = want;
+        int rc = batch_layout(p, p->fwd_T, p->fwd_chunk);
+        if (rc) return rc;
+    }
+    p->key = graph_key(p);
     TuneChoice best;
     if (!(flags & XCT_TUNE_FORCE) && xct_tune_lookup(p->key, cache_path, best))
         return batch_layout(p, best.T, best.chunk);
     XCT_CUDA_TRY(cudaSetDevice(p->ctx->device));
     cudaStream_t st = (cudaStream_t)stream;
+    const int m = (int)p->glist.size();
     size_t maxpix = 0;
     int max_rows = 1;
-    for (const XctItemDev &d : p->host) {
+    for (int i : p->glist) {
+        const XctItemDev &d = p->host[i];
         maxpix = std::max(maxpix, (size_t)d.g.nx * d.g.ny);
         max_rows = std::max(max_rows, (d.g.pa + d.g.ss - 1) / d.g.ss);
     }
     float *scratch = nullptr;
     XCT_CUDA_TRY(cudaMalloc(&scratch, sizeof(float) * maxpix));
-    std::vector<XctItemDev> tmp = p->host;
+    std::vector<XctItemDev> tmp(m);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -508,18 +672,18 @@ extern "C" int xct_batch_plan_autotune(xct_batch_plan *p, const char *cache_path
     for (const TuneChoice &c : xct_tune_candidates(max_rows)) {
         if (rc) break;
         if ((rc = batch_layout(p, c.T, c.chunk))) break;
-        for (int i = 0; i < p->n; ++i) {
-            tmp[i] = p->host[i];
-            tmp[i].img = scratch;
-            tmp[i].sino = nullptr;
+        for (int j = 0; j < m; ++j) {
+            tmp[j] = p->host[p->glist[j]];
+            tmp[j].img = scratch;
+            tmp[j].sino = nullptr;
         }
-        cudaMemcpyAsync(p->d_items, tmp.data(), sizeof(XctItemDev) * p->n, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(p->d_items, tmp.data(), sizeof(XctItemDev) * m, cudaMemcpyHostToDevice, st);
         float tmin = 3.0e38f;
         for (int r = 0; r < 3 && rc == XCT_OK; ++r) {  // first run warms up
             cudaMemsetAsync(p->d_acc, 0, sizeof(double) * p->n_acc, st);
             cudaMemsetAsync(p->d_queues, 0, sizeof(int), st);
             cudaEventRecord(e0, st);
-            rc = launch_fwd_batched(p->d_items, p->d_bases, p->n, p->sub[0], p->d_queues, p->grids[0], c.T, st);
+            rc = launch_fwd_batched(p->d_items, p->d_bases, m, p->sub[0], p->d_queues, p->grids[0], c.T, st);
             cudaEventRecord(e1, st);
             cudaError_t e = cudaEventSynchronize(e1);
             if (rc == XCT_OK && e != cudaSuccess) rc = xct_cuda_fail(e, "xct_batch_plan_autotune");

@@ -57,6 +57,7 @@ EXPORTS = (
     "xct_denoise_sinogram",
     "xct_cs_osem_run_device", "xct_cs_osem_run", "xct_plan_autotune", "xct_plan_tuning", "xct_plan_set_tuning",
     "xct_plan_multislice", "xct_plan_set_multislice", "xct_batch_plan_set_cs", "xct_batch_plan_uniform",
+    "xct_batch_plan_groups", "xct_batch_plan_set_grouping",
     "xct_fista_power_iteration", "xct_fista_set_lipschitz", "xct_fista_run_device", "xct_fista_run",
     "xct_batch_plan_autotune", "xct_batch_plan_tuning", "xct_osem_run_volume", "xct_hybrid_cs_run_device",
     "xct_hybrid_cs_run",
@@ -145,6 +146,8 @@ def load():
     L.xct_cs_osem_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, vp]
     L.xct_batch_plan_set_cs.argtypes = [vp, c_f, ip, ctypes.POINTER(ctypes.c_int)]
     L.xct_batch_plan_uniform.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    L.xct_batch_plan_groups.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.xct_batch_plan_set_grouping.argtypes = [vp, ip]
     L.xct_fista_power_iteration.argtypes = [vp, ip, ip, ip, fp, vp]
     L.xct_fista_set_lipschitz.argtypes = [vp, fp]
     L.xct_fista_run_device.argtypes = [vp, ip, vp, vp, ctypes.POINTER(ctypes.c_int), ip, c_f, c_f, ip, vp]
@@ -604,7 +607,8 @@ def make_geom(nx, ny, px, angles_deg, ss, it, center_bin=None, fetch_mode=FETCH_
 
 class BatchPlan:
     """OS-EM over slices of different shapes (same subset count) in one CUDA graph of
-    persistent launches (xct_batch_plan_create / xct_batch_run)."""
+    persistent launches (xct_batch_plan_create / xct_batch_run); slices that share one
+    geometry, eight or more, run through a single-shape plan of their own (geometry groups)."""
 
     def __init__(self, ctx, geoms, it):
         self._lib = load()
@@ -626,10 +630,20 @@ class BatchPlan:
         return t.value, c.value
 
     def uniform(self):
-        """Slices per call of the uniform route (0: the batch always runs as the graph)."""
+        """Slices per call when every slice is in one geometry group (0: not so)."""
         v = ctypes.c_int()
         _check(self._lib.xct_batch_plan_uniform(self.handle, ctypes.byref(v)))
         return v.value
+
+    def groups(self):
+        """(number of geometry groups, slices they hold)."""
+        g, k = ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.xct_batch_plan_groups(self.handle, ctypes.byref(g), ctypes.byref(k)))
+        return g.value, k.value
+
+    def set_grouping(self, on):
+        """Geometry groups on (the default) or off (the graph serves every slice)."""
+        _check(self._lib.xct_batch_plan_set_grouping(self.handle, 1 if on else 0))
 
     def run(self, sinos, imgs, stream=None):
         n = len(self.geoms)

@@ -131,12 +131,18 @@ int xct_osem_run_volume(xct_plan *plan, int n, const float *const *sino_host, fl
  *     add up to n; nstacks = 0 turns it off), the third axis of the proximal step; every run
  *     then needs each stack's images consecutive in one [dN][ny][nx] array (d_img[i+1] =
  *     d_img[i] + ny*nx within a stack).  Semantics as xct_cs_osem_run_device.
- * A uniform batch (n >= 2 slices of one geometry: sizes, centre, modes and angle list) whose
- * sinograms and images are each one array ([n][pa][px], [n][ny][nx]) and that has no stacks
- * runs through a single-shape plan of the same geometry instead, up to 16 slices per
- * xct_osem_run_device call (the slice-interleaved forward projector serves such slices
- * faster than the persistent launches); other runs of the plan use the graph.
- * xct_batch_plan_uniform reports the slices per call of that route (0: not uniform). */
+ * Geometry groups: slices that share one geometry (sizes, centre, modes and angle list; in a
+ * CT-XAFS stack, the slices of one width at one energy), at least XCT_MULTISLICE_SLICES of
+ * them, form a group that runs through a single-shape plan of that geometry, up to 16 slices
+ * per xct_osem_run_device call (the slice-interleaved kernels serve such slices faster than
+ * the persistent launches): in place when a call's slices are consecutive in one pair of
+ * arrays ([k][pa][px], [k][ny][nx]), else copied into a contiguous scratch pair of the plan
+ * and the images copied back.  The graph serves the other slices; with compressed sensing
+ * (stacks set) it serves every slice.  Results agree with the graph's to float rounding.
+ * xct_batch_plan_groups reports the number of groups and the slices they hold;
+ * xct_batch_plan_set_grouping(plan, 0) turns the groups off (the graph serves every slice),
+ * 1 on again (the default).  xct_batch_plan_uniform reports the slices per call when every
+ * slice is in one group (0: not so). */
 typedef struct xct_batch_plan xct_batch_plan;
 int xct_batch_plan_create(xct_ctx *ctx, int n, const xct_geom *geoms, int it, xct_batch_plan **out);
 int xct_batch_run(xct_batch_plan *plan, const float *const *d_sino, float *const *d_img, void *stream);
@@ -145,6 +151,8 @@ int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, const float
                          float *const *d_img, int it, void *stream);
 int xct_batch_plan_set_cs(xct_batch_plan *plan, float cs_lambda, int nstacks, const int *stack_len);
 int xct_batch_plan_uniform(xct_batch_plan *plan, int *slices_per_call);
+int xct_batch_plan_groups(xct_batch_plan *plan, int *ngroups, int *grouped_slices);
+int xct_batch_plan_set_grouping(xct_batch_plan *plan, int on);
 
 /* ---- OS-EM without any allocation ----------------------------------------------------
  * No counterpart in the reference: the reference allocates its image objects on every call.
@@ -393,8 +401,9 @@ int xct_osem_profile(xct_plan *plan, int dN, const float *d_sino, float *d_img, 
  * geometry (its staging buffers are the input; no caller data is read or written), keeps the
  * fastest, and records it in memory and in cache_path (NULL: XCT_TUNE_CACHE; no file if
  * neither).  A cached entry is reused without timing unless flags has XCT_TUNE_FORCE.
- * Synchronous.  xct_batch_plan_autotune does the same for a batch plan (one choice for all
- * its slices; the next xct_batch_run captures its graph again).  The *_tuning calls report
+ * Synchronous.  xct_batch_plan_autotune does the same for a batch plan: each geometry
+ * group's plan, and one choice for the slices its graph serves (the next xct_batch_run
+ * captures its graph again).  The *_tuning calls report
  * the current choice; xct_plan_set_tuning sets one by hand. */
 #define XCT_TUNE_FORCE 1
 int xct_plan_autotune(xct_plan *plan, int dN, const char *cache_path, int flags, void *stream);

@@ -192,9 +192,10 @@ def test_batched_compressed_sensing_stacks(gpu_ctx, oracle_lib):
 
 def test_uniform_batch_route(gpu_ctx, oracle_lib):
     """A batch of 16 slices of one geometry (512^2, 90 angles; the slice-interleaved forward
-    projector's shape) in one pair of arrays takes the uniform route -- a single-shape plan,
-    16 slices per call -- and gives the single-plan result; the same plan with the images in
-    separate allocations replays its graph of persistent launches; both against the oracle."""
+    projector's shape) is one geometry group: in one pair of arrays it runs in place through
+    a single-shape plan, 16 slices per call, and gives the single-plan result; with the
+    images in separate allocations it runs through the plan's scratch pair; with groups off
+    the same plan replays its graph of persistent launches; all against the oracle."""
     import xct
     from xct import phantom as P
     O = oracle_lib
@@ -207,17 +208,24 @@ def test_uniform_batch_route(gpu_ctx, oracle_lib):
     geoms = [xct.make_geom(n, n, n, ang, ss, it) for _ in range(dn)]
     bp = xct.BatchPlan(gpu_ctx, geoms, it)
     assert bp.uniform() == dn
+    assert bp.groups() == (1, dn)
     plan = xct.OSEMPlan(gpu_ctx, n, n, n, ang, ss, it, max_batch=dn)
     x1 = torch.ones((dn, n, n), device="cuda")
     plan.run_device(d_s, x1)
     arr = torch.ones((dn, n, n), device="cuda")
     bp.run([d_s[z] for z in range(dn)], [arr[z] for z in range(dn)])
+    loose_s = [d_s[z].clone() for z in reversed(range(dn))][::-1]
     sep = [torch.ones((n, n), device="cuda") for _ in range(dn)]
-    bp.run([d_s[z] for z in range(dn)], sep)
+    bp.run(loose_s, sep)
+    bp.set_grouping(False)
+    gsep = [torch.ones((n, n), device="cuda") for _ in range(dn)]
+    bp.run([d_s[z] for z in range(dn)], gsep)
     torch.cuda.synchronize()
     single = x1.cpu().numpy().astype(np.float64)
     routed = arr.cpu().numpy().astype(np.float64)
-    graph = torch.stack(sep).cpu().numpy().astype(np.float64)
+    scratch = torch.stack(sep).cpu().numpy().astype(np.float64)
+    graph = torch.stack(gsep).cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(scratch - routed) / np.linalg.norm(routed) <= 1e-6
     assert np.linalg.norm(routed - single) / np.linalg.norm(single) <= 1e-6
     assert np.linalg.norm(graph - single) / np.linalg.norm(single) <= 1e-6
     for z in (0, dn - 1):
@@ -231,13 +239,14 @@ def test_uniform_batch_route(gpu_ctx, oracle_lib):
     g2 = [xct.make_geom(64, 64, 64, ang, ss, it), xct.make_geom(64, 64, 64, ang + 0.5, ss, it)]
     bp2 = xct.BatchPlan(gpu_ctx, g2, it)
     assert bp2.uniform() == 0
+    assert bp2.groups() == (0, 0)
     bp2.close()
 
 
 def test_uniform_batch_route_with_correction(gpu_ctx, oracle_lib):
-    """A uniform batch whose geometry carries a sinogram correction (mode 3): the uniform
-    route corrects inside the single-shape plan, the graph in its own correction launch;
-    both give the oracle's OS-EM of the corrected sinogram."""
+    """A uniform batch whose geometry carries a sinogram correction (mode 3): the geometry
+    group corrects inside its single-shape plan, the graph (groups off) in its own correction
+    launch; both give the oracle's OS-EM of the corrected sinogram."""
     import xct
     from xct import phantom as P
     O = oracle_lib
@@ -252,6 +261,7 @@ def test_uniform_batch_route_with_correction(gpu_ctx, oracle_lib):
     assert bp.uniform() == dn
     arr = torch.ones((dn, n, n), device="cuda")
     bp.run([d_s[z] for z in range(dn)], [arr[z] for z in range(dn)])
+    bp.set_grouping(False)
     sep = [torch.ones((n, n), device="cuda") for _ in range(dn)]
     bp.run([d_s[z] for z in range(dn)], sep)
     torch.cuda.synchronize()
@@ -264,4 +274,74 @@ def test_uniform_batch_route_with_correction(gpu_ctx, oracle_lib):
         assert np.linalg.norm(routed[z] - ref) / np.linalg.norm(ref) <= 1e-4, z
     # the caller's sinograms are not modified
     assert np.array_equal(d_s.cpu().numpy(), meas)
+    bp.close()
+
+
+def test_geometry_groups_in_a_mixed_batch(gpu_ctx, oracle_lib):
+    """A batch of 27 slices in interleaved order: 16 of geometry A (512^2, 90 angles: the
+    slice-interleaved kernels' shape), 8 of geometry B (80x72 image, 88 bins, 45 angles with
+    3 dropped, centre +1.5 bins, correction mode 2) and 3 of shapes of their own.  A and B
+    are geometry groups (single-shape plans, their slices copied through the scratch pair),
+    the 3 others run in the graph; every slice agrees with the graph serving all 27 (groups
+    off), and slices of each kind with the oracle.  The caller's sinograms are unchanged."""
+    import xct
+    from xct import phantom as P
+    O = oracle_lib
+    ss, it = 5, 2
+    rng = np.random.default_rng(77)
+    angA = P.uniform_angles(90)
+    keepB = np.sort(rng.choice(45, 42, replace=False))
+    angB = (keepB * 4.0).astype(np.float32)
+    kinds = ["A"] * 16 + ["B"] * 8 + ["C0", "C1", "C2"]
+    order = list(rng.permutation(len(kinds)))
+    prmA = P.ellipsoid_params(512, 16, count=8, seed=78)
+    specs, geoms, sinos, host = [], [], [], []
+    za = zb = 0
+    for k in order:
+        kind = kinds[k]
+        if kind == "A":
+            nx = ny = px = 512
+            ang, cx, mode = angA, None, 0
+            img = P.ellipsoid_slice(prmA, za, nx, ny)
+            za += 1
+        elif kind == "B":
+            nx, ny, px, ang, cx, mode = 80, 72, 88, angB, 44 + 1.5, 2
+            m = max(nx, ny)
+            img = P.rasterize_ellipses(P.ellipse_params(m, 4, 90 + zb, axes=(2, m / 4)), m, m)[:ny, :nx].copy()
+            zb += 1
+        else:
+            c = int(kind[1])
+            nx = ny = 40 + 16 * c
+            px, ang, cx, mode = nx + 8, P.uniform_angles(30 + 10 * c), None, 0
+            img = P.rasterize_ellipses(P.ellipse_params(nx, 4, 95 + c, axes=(2, nx / 4)), nx, nx)
+        ccx = px * 0.5 if cx is None else cx
+        meas = P.noisy_log_sinogram(O.projection(img, ang, px, cx=ccx), 1e5, len(specs)).astype(np.float32)
+        specs.append((kind, nx, ny, px, ang, ccx, mode))
+        geoms.append(xct.make_geom(nx, ny, px, ang, ss, it, center_bin=ccx, correction_mode=mode))
+        host.append(meas)
+        sinos.append(torch.from_numpy(meas).cuda().contiguous())
+    bp = xct.BatchPlan(gpu_ctx, geoms, it)
+    assert bp.groups() == (2, 24)
+    assert bp.uniform() == 0
+    grouped = [torch.ones((ny, nx), device="cuda") for _, nx, ny, _, _, _, _ in specs]
+    bp.run(sinos, grouped)
+    bp.set_grouping(False)
+    graph = [torch.ones((ny, nx), device="cuda") for _, nx, ny, _, _, _, _ in specs]
+    bp.run(sinos, graph)
+    torch.cuda.synchronize()
+    checked = set()
+    for i, (kind, nx, ny, px, ang, cx, mode) in enumerate(specs):
+        a = grouped[i].cpu().numpy().astype(np.float64)
+        b = graph[i].cpu().numpy().astype(np.float64)
+        assert np.all(np.isfinite(a)), i
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 1e-6, (i, kind)
+        if kind[0] not in checked:
+            checked.add(kind[0])
+            used = O.sino_correction(host[i], ang, mode) if mode else host[i]
+            ref = O.osem_run(np.ones((ny, nx), np.float32), used, ang, ss, it, cx=cx, order=O.ORDER_LITERAL)
+            assert np.linalg.norm(a - ref) / np.linalg.norm(ref) <= 1e-4, (i, kind)
+            assert np.abs(a - ref).max() <= 1e-3 * np.abs(ref).max(), (i, kind)
+    assert checked == {"A", "B", "C"}
+    for i in range(len(specs)):
+        assert np.array_equal(sinos[i].cpu().numpy(), host[i])
     bp.close()
