@@ -517,10 +517,11 @@ def ctxafs_batched(ctx, n_energy=64, n_slices=8, ss=10, it=5, sample=32, compare
 
 def uniform_batch(ctx, sino, n=16, reps=2):
     """A uniform batch (n slices of the per-slice workload's geometry, 2048^2, 1500 angles,
-    15 x 4) through one batch plan: with the sinograms and images each one array the plan
-    takes its uniform route (a single-shape plan, slice-interleaved forward projector); with
-    images in separate allocations the same plan replays its graph of persistent launches.
-    Slice-iters/s of both, CUDA-event timing, device-resident inputs."""
+    15 x 4) through one batch plan: its slices form one geometry group, which runs through a
+    single-shape plan (slice-interleaved kernels; the sinograms and images each one array);
+    with groups off the same plan replays its graph of persistent launches (images in
+    separate allocations).  Slice-iters/s of both, CUDA-event timing, device-resident
+    inputs."""
     import torch
     import xct
     from xct import phantom
@@ -1017,7 +1018,7 @@ def main():
     except Exception as e:  # reported, never fatal
         grouped = {"error": str(e)[:300]}
 
-    # ---- a uniform batch through the batch plan: its uniform route against its graph ----
+    # ---- a uniform batch through the batch plan: one geometry group against its graph ----
     try:
         uniform = uniform_batch(ctx, sino)
     except Exception as e:  # reported, never fatal

@@ -589,7 +589,7 @@ extern "C" int xct_osem_run_batched(xct_ctx *ctx, int n, const xct_geom *geoms, 
     return rc;
 }
 
-// Slices per call of the uniform route: every slice in one geometry group (0: not so).
+// Slices per call when every slice is in one geometry group (0: not so).
 extern "C" int xct_batch_plan_uniform(xct_batch_plan *p, int *slices_per_call)
 {
     if (!p || !slices_per_call) return xct_fail(XCT_E_INVALID, "xct_batch_plan_uniform: null argument");
