@@ -1911,8 +1911,9 @@ int launch_adj_subset(const KGeom &g, const float2 *trig, const float *sino, flo
     if (dN <= 0) return XCT_OK;
     // with the slice-interleaved kernels on, groups of eight or ten slices take the gather
     // form (its candidate search is shared by the group; for fewer slices the scatter forms
-    // cost less) -- as many groups of ten as leave a multiple of eight, then groups of eight
-    // -- and groups of four the scatter form with shared sample work
+    // cost less) -- the most groups of ten that leave a multiple of eight (a slice costs less
+    // in a group of ten), then groups of eight -- and groups of four the scatter form with
+    // shared sample work
     if (g.ms_chunk > 0 && dN >= 8) {
         const size_t np = (size_t)g.pa * g.px, ni = (size_t)g.nx * g.ny;
         int rc = XCT_OK;
@@ -1922,9 +1923,8 @@ int launch_adj_subset(const KGeom &g, const float2 *trig, const float *sino, flo
             if (base) base += n * ni;
             dN -= n;
         };
-        int tens = 0;
-        while (10 * tens <= dN && (dN - 10 * tens) % 8 != 0) ++tens;
-        if (10 * tens > dN) tens = 0;
+        int tens = dN / 10;
+        while (tens > 0 && (dN - 10 * tens) % 8 != 0) --tens;
         if (tens > 0) {
             if ((rc = launch_adj_gather<10>(g, trig, sino, img, tens, sub, step, nang, base, scale, st))) return rc;
             advance(tens * 10);
