@@ -973,9 +973,10 @@ __global__ void __launch_bounds__(kThreads) adj_ms_kernel(const float *__restric
 // most two sample indices within 0.717 of the centre's projection on the ray; each of those
 // four candidates is evaluated with the forward projector's own arithmetic (fma
 // coordinates, round-down floor) and kept when its base texel is (i, j), the ray is on the
-// detector and the index within [0, D).  A CTA of 512 threads owns 32 x 16 base texels and
-// writes the 31 x 15 texels whose four base texels it holds, texel (i, j) = A00(i, j) +
-// A10(i-1, j) + A01(i, j-1) + A11(i-1, j-1), after staging the four parts in shared memory.
+// detector and the index within [0, D).  A CTA owns 32 x BY base texels (BY = 16 for eight
+// slices, 20 for ten) and writes the 31 x (BY - 1) texels whose four base texels it holds,
+// texel (i, j) = A00(i, j) + A10(i-1, j) + A01(i, j-1) + A11(i-1, j-1), after staging the
+// four parts in shared memory.
 // The rays' values of 16 angles at a time are staged by asynchronous copies into one of two
 // windows: the next chunk's copies run while this chunk is accumulated.  Most squares hold
 // one sample per angle, about 9 % two and 9 % none, so a warp whose lanes each added all
@@ -984,23 +985,26 @@ __global__ void __launch_bounds__(kThreads) adj_ms_kernel(const float *__restric
 // (window address and fractions) and the queues are emptied at the end of the chunk -- about
 // 1.2 passes per angle instead of 1.8.  Float sums in a fixed order given by the geometry:
 // deterministic, and no fixed-point rounding.
-constexpr int kAdjGBX = 32, kAdjGBY = 16;            // base texels per CTA
-constexpr int kAdjGThreads = kAdjGBX * kAdjGBY;      // one per base texel
-constexpr int kAdjGW = 44;                           // staged rays per angle
+constexpr int kAdjGBX = 32;                          // base texels per CTA row
+constexpr int kAdjGW = 44;  // staged rays per angle (a 32 x 20 block needs at most 43)
 constexpr int kAdjGChunk = 16;                       // angles per staging pass
-constexpr unsigned kAdjGQStride = 16u * kAdjGThreads; // bytes between a queue's slots
 template <int S>
 struct AdjG {
+    // base texel rows per CTA (one thread per base texel): 16 at two CTAs per SM (eight
+    // slices, 64 registers), 20 at one (ten slices, 94 registers)
+    static constexpr int BY = S <= 8 ? 16 : 20;
+    static constexpr int Threads = kAdjGBX * BY;
+    static constexpr unsigned QStride = 16u * Threads;  // bytes between a queue's slots
     // two windows: [slice pair][angle][ray] of float2, then the queues: [slot][thread] of
     // (window address, fx, fy); later the parts: [corner][slice][thread]; three slots of
     // (cos, sin) and first staged ray per angle
     static constexpr unsigned PairBytes = (unsigned)(kAdjGChunk * kAdjGW * 8);
     static constexpr unsigned WinBytes = (unsigned)(S / 2) * PairBytes;
-    static constexpr size_t CombBytes = (size_t)4 * S * kAdjGThreads * 4;
+    static constexpr size_t CombBytes = (size_t)4 * S * Threads * 4;
     // queued samples per thread: four where the registers allow (one CTA per SM); none at
     // two CTAs per SM, whose 64 registers a thread would then exceed
     static constexpr int Queue = S > 8 ? 4 : 0;
-    static constexpr size_t QueueBytes = (size_t)Queue * kAdjGQStride;
+    static constexpr size_t QueueBytes = (size_t)Queue * QStride;
     static constexpr size_t SlotBytes = (size_t)3 * kAdjGChunk * 12;
     static constexpr size_t Front = 2 * (size_t)WinBytes + QueueBytes;
     static constexpr size_t Smem = (Front > CombBytes ? Front : CombBytes) + SlotBytes;
@@ -1027,7 +1031,7 @@ __device__ __forceinline__ void lds_q(unsigned addr, unsigned &ad, f2x &fr)
 
 // S (even) slices per CTA; the library launches S = 8 and S = 10 (one CTA per SM).
 template <int S>
-__global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kernel(const float *__restrict__ sino,
+__global__ void __launch_bounds__(AdjG<S>::Threads, S <= 8 ? 2 : 1) adj_gather_kernel(const float *__restrict__ sino,
                                                                      float *__restrict__ img,
                                                                      const float2 *__restrict__ trig, KGeom g,
                                                                      int ntx, int sub, int step, int nang,
@@ -1044,7 +1048,7 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
     const size_t nprj = (size_t)g.pa * g.px, nimg = (size_t)g.nx * g.ny;
     const float *sz = sino + (size_t)z0 * nprj;
     // base texels [bi0, bi0 + 32) x [bj0, bj0 + 16); output texels from bi0 + 1, bj0 + 1
-    const int bi0 = bx * (kAdjGBX - 1) - 1, bj0 = by * (kAdjGBY - 1) - 1;
+    const int bi0 = bx * (kAdjGBX - 1) - 1, bj0 = by * (AdjG<S>::BY - 1) - 1;
     const int i = bi0 + tx, j = bj0 + ty;
     const int ibits = i + XCT_FLOOR_BIAS, jbits = j + XCT_FLOOR_BIAS;
     const float ci = (float)i + 0.5f, cj = (float)j + 0.5f;  // the square's centre
@@ -1102,7 +1106,7 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const float px_ = (float)(bi0 + ((q & 1) ? kAdjGBX : 0)) - g.hx;
-            const float py_ = (float)(bj0 + ((q & 2) ? kAdjGBY : 0)) - g.hy;
+            const float py_ = (float)(bj0 + ((q & 2) ? AdjG<S>::BY : 0)) - g.hy;
             umin = fminf(umin, px_ * cs.x - py_ * cs.y + g.cx);
         }
         sxw[at] = (int)floorf(umin) - 2;
@@ -1112,7 +1116,7 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
         if (ch >= nch) return;
         const int k0 = ch * kAdjGChunk, kn = min(kAdjGChunk, nang - k0), sl = (ch % 3) * kAdjGChunk;
         const unsigned wb = wbase + (unsigned)(ch & 1) * AdjG<S>::WinBytes;
-        for (int e = threadIdx.x; e < kn * S * kAdjGW; e += kAdjGThreads) {
+        for (int e = threadIdx.x; e < kn * S * kAdjGW; e += AdjG<S>::Threads) {
             const int r = e % kAdjGW, t2 = e / kAdjGW;
             const int z = t2 % S, k = t2 / S;
             const int X = sxw[sl + k] + r;
@@ -1180,7 +1184,7 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
                 rest &= rest - 1;
                 const f2x xy = q == 1 ? cxy[1] : q == 2 ? cxy[2] : cxy[3];
                 const int X = Xa + (q >> 1);
-                sts_q(qb + (unsigned)qn * kAdjGQStride, wk + 8u * (unsigned)X, f2_sub(xy, bxy));
+                sts_q(qb + (unsigned)qn * AdjG<S>::QStride, wk + 8u * (unsigned)X, f2_sub(xy, bxy));
                 ++qn;
             }
             now |= rest;
@@ -1196,7 +1200,7 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
         for (int i = 0; i < qn; ++i) {
             unsigned ad;
             f2x fr;
-            lds_q(qb + (unsigned)i * kAdjGQStride, ad, fr);
+            lds_q(qb + (unsigned)i * AdjG<S>::QStride, ad, fr);
             add(ad, fr, wb);
         }
         qn = 0;
@@ -1209,17 +1213,17 @@ __global__ void __launch_bounds__(kAdjGThreads, S <= 8 ? 2 : 1) adj_gather_kerne
         for (int h = 0; h < P; ++h) {
             float a0, a1;
             f2_unpack(acc[cq][h], a0, a1);
-            part[(cq * S + 2 * h) * kAdjGThreads + threadIdx.x] = a0;
-            part[(cq * S + 2 * h + 1) * kAdjGThreads + threadIdx.x] = a1;
+            part[(cq * S + 2 * h) * AdjG<S>::Threads + threadIdx.x] = a0;
+            part[(cq * S + 2 * h + 1) * AdjG<S>::Threads + threadIdx.x] = a1;
         }
     __syncthreads();
     if (tx == 0 || ty == 0 || i >= g.nx || j >= g.ny) return;
     const int t = threadIdx.x;
 #pragma unroll
     for (int z = 0; z < S; ++z) {
-        const float a = part[(0 * S + z) * kAdjGThreads + t] + part[(1 * S + z) * kAdjGThreads + t - 1] +
-                        part[(2 * S + z) * kAdjGThreads + t - kAdjGBX] +
-                        part[(3 * S + z) * kAdjGThreads + t - kAdjGBX - 1];
+        const float a = part[(0 * S + z) * AdjG<S>::Threads + t] + part[(1 * S + z) * AdjG<S>::Threads + t - 1] +
+                        part[(2 * S + z) * AdjG<S>::Threads + t - kAdjGBX] +
+                        part[(3 * S + z) * AdjG<S>::Threads + t - kAdjGBX - 1];
         const size_t o = (size_t)(z0 + z) * nimg + (size_t)j * g.nx + i;
         img[o] = base ? fmaf(scale_out, a, __ldg(base + o)) : a;
     }
@@ -1240,8 +1244,8 @@ static int launch_adj_gather(const KGeom &g, const float2 *trig, const float *si
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AdjG<S>::Smem));
         done[dev].store(true, std::memory_order_release);
     }
-    const int ntx = (g.nx + kAdjGBX - 2) / (kAdjGBX - 1), nty = (g.ny + kAdjGBY - 2) / (kAdjGBY - 1);
-    adj_gather_kernel<S><<<dim3(ntx * nty, 1, groups), kAdjGThreads, AdjG<S>::Smem, st>>>(sino, img, trig, g, ntx, sub,
+    const int ntx = (g.nx + kAdjGBX - 2) / (kAdjGBX - 1), nty = (g.ny + AdjG<S>::BY - 2) / (AdjG<S>::BY - 1);
+    adj_gather_kernel<S><<<dim3(ntx * nty, 1, groups), AdjG<S>::Threads, AdjG<S>::Smem, st>>>(sino, img, trig, g, ntx, sub,
                                                                                          step, nang, base, scale);
     g_xct_launches.fetch_add(1, std::memory_order_relaxed);
     XCT_CUDA_TRY(cudaGetLastError());
