@@ -40,3 +40,32 @@ def test_counts_match_brute_force(nx, ny, px, cx_off):
     want_fwd, want_bp = _brute(angles, nx, ny, px, cx)
     assert np.array_equal(t_fwd.astype(np.int64), want_fwd), (t_fwd, want_fwd)
     assert np.array_equal(t_bp.astype(np.int64), want_bp), (t_bp, want_bp)
+
+
+def _geometry_groups(n_energy, n_slices):
+    """Sizes of the sets of items that share one geometry (width = bins, angle list) in the
+    benchmark's CT-XAFS stack, items taken energy by energy."""
+    from bench import ctxafs_stack_specs
+    widths, angs, _ = ctxafs_stack_specs(n_energy, n_slices)
+    groups = {}
+    for e in range(n_energy):
+        for w in widths:
+            key = (w, angs[e].tobytes())
+            groups[key] = groups.get(key, 0) + 1
+    return sorted(groups.values())
+
+
+def test_ctxafs_stacks_geometry_groups():
+    """The 512-item stack (64 energies x 8 slices) has two slices per width and energy, below
+    the batch plan's group size of eight, so its graph serves every item; the stack with whole
+    energies (4 x 64) has 16 groups of 16, so every item is in a geometry group.  Widths
+    512-2048 each appear equally often; angle counts stay within 360-1200 minus 10 %."""
+    from bench import ctxafs_stack_specs
+    assert _geometry_groups(64, 8) == [2] * 256
+    assert _geometry_groups(4, 64) == [16] * 16
+    widths, angs, grids = ctxafs_stack_specs(4, 64)
+    assert sorted(set(widths)) == [512, 1024, 1536, 2048]
+    assert all(widths.count(w) == 16 for w in (512, 1024, 1536, 2048))
+    for a, (pa, keep) in zip(angs, grids):
+        assert pa in (360, 720, 900, 1200) and 0.9 * pa <= len(a) <= pa
+        assert np.array_equal(a, (keep * (180.0 / pa)).astype(np.float32))
