@@ -139,6 +139,9 @@ int xct_osem_run_volume(xct_plan *plan, int n, const float *const *sino_host, fl
  * arrays ([k][pa][px], [k][ny][nx]), else copied into a contiguous scratch pair of the plan
  * and the images copied back.  The graph serves the other slices; with compressed sensing
  * (stacks set) it serves every slice.  Results agree with the graph's to float rounding.
+ * Each group holds a single-shape plan with the buffers of up to 16 slices of its geometry
+ * (staging, ratio and accumulator: about 0.6 GB for 2048^2 with 1200 angles), so a stack of
+ * many groups holds as many such sets; the graph's buffers cover every slice once.
  * xct_batch_plan_groups reports the number of groups and the slices they hold;
  * xct_batch_plan_set_grouping(plan, 0) turns the groups off (the graph serves every slice),
  * 1 on again (the default).  xct_batch_plan_uniform reports the slices per call when every
